@@ -1,0 +1,144 @@
+"""Generate the golden fixtures under tests/golden/ from the reference binary.
+
+Run in a tree where the reference sources are present (the binary is built
+from them by ``oracle/Makefile`` into ``oracle/_ref/``):
+
+    python tests/golden/make_golden.py
+
+Each fixture is one ``.npz`` holding the planar inputs (``g`` with NaN holes,
+optional ``f`` data term, optional ``mask``), the command-line arguments and
+environment the reference ran with, and its planar output ``out``.
+
+* ``pin_*``   small cases across every option, env var and edge case; the
+              oracle restatement must reproduce them bit for bit.
+* ``conv_*``  single-channel cases run to convergence with the reference
+              recipe ``CG_EPS=rtol*||b|| simpois -s 1 -c -1`` (rtol 1e-7); the
+              GPU solver must agree within 1e-4 relative max-abs.
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle as O  # noqa: E402
+from imscript_gb300 import synth  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def save(name, g, f=None, mask=None, args=(), env=None, out=None, extra=None):
+    d = {"g": g, "args": np.array(json.dumps(list(args))),
+         "env": np.array(json.dumps(env or {})), "out": out}
+    if f is not None:
+        d["f"] = f
+    if mask is not None:
+        d["mask"] = mask
+    if extra:
+        d["extra"] = np.array(json.dumps(extra))
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), **d)
+
+
+def noisy(rng, pd, h, w, frac):
+    x = (rng.standard_normal((pd, h, w)) * 0.5).astype(np.float32)
+    x += synth.gaussian_field(rng, h, w, 3)[None]
+    m = rng.random((h, w)) < frac
+    x[:, m] = np.nan
+    return x
+
+
+def pin_cases(rng):
+    shapes = [(1, 17, 23), (3, 12, 9), (1, 1, 40), (1, 33, 1), (1, 1, 1), (1, 2, 3), (2, 16, 16)]
+    argsets = [
+        [], ["-n", "40"], ["-n", "3", "-s", "1"], ["-s", "2", "-n", "7"],
+        ["-t", "-0.08", "-n", "30"], ["-t", "-1000.01", "-n", "3", "-s", "2"],
+        ["-c", "25"], ["-s", "1", "-c", "-1"], ["-t", "-0.08", "-s", "2", "-c", "30"],
+        ["-t", "0.1", "-n", "12", "-s", "3", "-c", "5"],
+    ]
+    k = 0
+    for (pd, h, w) in shapes:
+        for a in argsets:
+            g = noisy(rng, pd, h, w, 0.35)
+            f = None
+            if k % 2 == 1:
+                f = (rng.standard_normal(g.shape) * 0.05).astype(np.float32)
+            out = O.run_reference(g, f, args=a)
+            save(f"pin_{k:03d}", g, f, args=a, out=out)
+            k += 1
+    # environment smart parameters (smapa.h:44-60)
+    g = noisy(rng, 1, 24, 20, 0.3)
+    f = (rng.standard_normal(g.shape) * 0.05).astype(np.float32)
+    for env, a in [({"PMSFAC": "1.5"}, ["-n", "20"]), ({"PONLIT": "12"}, ["-n", "20"]),
+                   ({"PONLIT": "24"}, ["-n", "20", "-c", "10"]), ({"CG_EPS": "0.01"}, ["-c", "-1"]),
+                   ({"PMSFAC": "2.7", "CG_EPS": "1e-3"}, ["-c", "50", "-s", "3"])]:
+        out = O.run_reference(g, f, args=a, env=env)
+        save(f"pin_{k:03d}", g, f, args=a, env=env, out=out)
+        k += 1
+    # mask image (applied to every channel), including all-known/all-unknown
+    g = noisy(rng, 2, 14, 18, 0.0)
+    mk = (rng.random((14, 18)) < 0.3).astype(np.float32) * 2 - 0.5
+    out = O.run_reference(g, None, mask=mk, args=["-n", "15"])
+    save(f"pin_{k:03d}", g, None, mask=mk, args=["-n", "15"], out=out)
+    k += 1
+    out = O.run_reference(g, None, args=["-n", "5"])  # nothing to fill
+    save(f"pin_{k:03d}", g, None, args=["-n", "5"], out=out)
+    k += 1
+    gall = np.full((1, 9, 11), np.nan, np.float32)
+    fall = (rng.standard_normal(gall.shape) * 0.1).astype(np.float32)
+    out = O.run_reference(gall, fall, args=["-n", "10"])
+    save(f"pin_{k:03d}", gall, fall, args=["-n", "10"], out=out)
+    k += 1
+    # +-Inf known pixels: overwritten by init during the sweeps, restored at the end
+    g = noisy(rng, 1, 15, 15, 0.3)
+    g[0, 3, 4] = np.inf
+    g[0, 10, 2] = -np.inf
+    for a in (["-n", "10"], ["-c", "10"]):
+        out = O.run_reference(g, None, args=a)
+        save(f"pin_{k:03d}", g, None, args=a, out=out)
+        k += 1
+    return k
+
+
+def conv_cases(rng):
+    k = 0
+    specs = [("lap", 64, 64, 0.25, False), ("lap", 80, 48, 0.25, False),
+             ("poi", 64, 64, 0.25, True), ("poi", 57, 71, 0.25, True),
+             ("bih", 40, 40, -0.08, False), ("bih", 36, 44, -0.08, True)]
+    for kind, h, w, t, with_f in specs:
+        img = synth.gaussian_field(rng, h, w, 6)
+        m = synth.disk_mask(rng, h, w, 0.2, rmin=2, rmax=8 if kind == "bih" else 12)
+        img[m] = np.nan
+        g = img[None]
+        f = None
+        if with_f:
+            f = synth.guidance(synth.gaussian_field(rng, h, w, 6))[2][None] * 0.5
+        ckind = 1 if t < 0 else 0
+        bn = float(O.rhs_norm(g, f, ckind)[0])
+        rtol = 1e-7
+        args = ["-s", "1", "-c", "-1", "-t", str(t)]
+        env = {"CG_EPS": repr(rtol * bn)}
+        out = O.run_reference(g, f, args=args, env=env, timeout=3000)
+        rel = float(O.rel_residual(out, g, f, ckind)[0][0])
+        save(f"conv_{kind}_{k:02d}", g, f, args=args, env=env, out=out,
+             extra={"rel_residual": rel, "bnorm": bn, "kind": ckind})
+        print(f"conv_{kind}_{k:02d}: {w}x{h} n={int(np.isnan(g).sum())} rel={rel:.2e}")
+        k += 1
+    return k
+
+
+def main():
+    if not O.have_reference():
+        O.build(reference=True)
+    rng = np.random.default_rng(20261203)
+    n1 = pin_cases(rng)
+    n2 = conv_cases(rng)
+    print(f"wrote {n1} pin cases and {n2} converged cases into {OUT}")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,44 @@
+"""Loading of the golden fixtures in tests/golden/ (shared by CPU and GPU tests)."""
+import glob
+import json
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def parse_args(args, env):
+    """simpois option values as main_simpois reads them (simpois.c:357-360):
+    atof, then truncation to int where the solver takes an int."""
+    opt = {"t": "0.25", "n": "10", "s": "99", "c": "0"}
+    k = 0
+    while k < len(args):
+        a = args[k]
+        if a.startswith("-") and a[1:] in opt:
+            opt[a[1:]] = args[k + 1]
+            k += 2
+        else:
+            k += 1
+    kw = dict(tstep=float(np.float32(float(opt["t"]))), niter=int(float(opt["n"])),
+              scale=int(float(opt["s"])), cgrad=float(opt["c"]))
+    kw["pmsfac"] = float(env.get("PMSFAC", 3))
+    kw["ponlit"] = float(env.get("PONLIT", 0))
+    kw["cg_eps"] = float(env.get("CG_EPS", -1))
+    return kw
+
+
+def load(path):
+    z = np.load(path)
+    d = {k: z[k] for k in z.files}
+    d["args"] = json.loads(str(d["args"]))
+    d["env"] = json.loads(str(d["env"]))
+    d["extra"] = json.loads(str(d["extra"])) if "extra" in d else {}
+    d["f"] = d.get("f")
+    d["mask"] = d.get("mask")
+    d["name"] = os.path.splitext(os.path.basename(path))[0]
+    return d
+
+
+def cases(prefix):
+    return sorted(glob.glob(os.path.join(GOLDEN, prefix + "*.npz")))
