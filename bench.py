@@ -1,0 +1,371 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 simpois fill: filled Mpx/s at a 1e-6 FP64 relative residual.
+
+Workload (default): Poisson with guidance, one 2048 x 2048 x 3 float32 image
+(128 Gaussians per channel), guidance f = div of the forward-difference
+gradient of an independent field, 6 irregular blobs covering 15 % of the
+pixels, seeded synthetic data; every channel solved to an FP64 relative
+residual <= 1e-6 (the workload's own target is 1e-5; 1e-6 is stricter).
+
+A step is one converged solve of the whole image (all channels batched in one
+call).  ``value`` times it with the inputs resident in HBM; ``e2e`` times the
+same solve through the C-ABI host entry point (simpois_solve) from pinned host
+buffers, host-to-device and device-to-host copies included; ``plain`` times
+the same channels solved one per call.  L2 is flushed (a 512 MiB write)
+between timed steps.
+
+``--impl reference`` times the CPU restatement of the reference's CG recipe
+(``CG_EPS = rtol * ||b|| simpois -s 1 -c -1``) on the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+HBM_FALLBACK = 6800.0
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh), "measured"
+    except Exception:
+        return {"hbm_gbs": HBM_FALLBACK}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_workload(name, rank):
+    from imscript_gb300 import synth
+    seed = 1000 * rank
+    if name == "c1":
+        inst = synth.config1(seed=seed, rtol=1e-6)
+        return [inst], "poisson-guided-2048x2048x3 (6 blobs, 15% holes)"
+    if name == "c1s":  # reduced size, for quick checks
+        inst = synth.config1(seed=seed, size=512, rtol=1e-6)
+        return [inst], "poisson-guided-512x512x3 (6 blobs, 15% holes)"
+    if name == "c0":
+        return [synth.config0(seed=seed)], "laplace-512x512x1 (disks, 20% holes)"
+    if name == "c3":
+        return synth.config3(seed=seed), "batched-256-uneven (64..1024 px, 5-60% holes)"
+    if name == "c2":
+        return [synth.config2(seed=seed)], "biharmonic-4096x4096x1 (1024^2 square + 200 scratches)"
+    raise SystemExit(f"unknown workload {name}")
+
+
+# ------------------------------------------------------------------ CPU baseline
+
+def cpu_sample(insts, crop, max_crops, seed=0):
+    """Crops of the workload's channels with their unknowns, for the CPU."""
+    rng = np.random.default_rng(seed)
+    out = []
+    chans = [(inst, l) for inst in insts for l in range(inst.g.shape[0])]
+    tries = 0
+    while len(out) < max_crops and tries < 64 * max_crops:
+        inst, l = chans[tries % len(chans)]
+        tries += 1
+        _, h, w = inst.g.shape
+        y0 = int(rng.integers(0, max(1, h - crop + 1)))
+        x0 = int(rng.integers(0, max(1, w - crop + 1)))
+        g = inst.g[l, y0:y0 + crop, x0:x0 + crop]
+        n = int(np.isnan(g).sum())
+        if 0 < n < g.size:
+            f = None if inst.f is None else inst.f[l, y0:y0 + crop, x0:x0 + crop]
+            out.append((np.ascontiguousarray(g), None if f is None else np.ascontiguousarray(f),
+                        0 if inst.tstep > 0 else 1, inst.rtol))
+    return out
+
+
+def cpu_time(sample, threads):
+    """Run the oracle's restatement of the reference CG recipe on every crop
+    (CG_EPS = rtol * ||b||, -s 1 -c -1), in parallel threads."""
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import oracle
+
+    oracle.lib()
+
+    def one(item):
+        g, f, kind, rtol = item
+        bn = float(oracle.rhs_norm(g[None], None if f is None else f[None], kind)[0])
+        out, it, _ = oracle.cg_extension(g, f, init=np.zeros_like(g), maxit=-1, kind=kind,
+                                         cg_eps=rtol * bn)
+        return int(np.isnan(g).sum()), it
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        res = list(ex.map(one, sample))
+    dt = time.perf_counter() - t0
+    unk = sum(r[0] for r in res)
+    return unk, dt, res
+
+
+def cpu_baseline(insts, budget_s=20.0):
+    threads = os.cpu_count() or 1
+    crop = 384
+    sample = cpu_sample(insts, crop, max_crops=threads)
+    unk, dt, res = cpu_time(sample, threads)
+    return {"value": unk / dt / 1e6, "unit": "filled Mpx/s", "cores": threads, "kind": "port",
+            "sample": f"{len(sample)} crops of {crop}x{crop} px cut from the workload's channels "
+                      f"({unk} unknowns), each solved by the CPU restatement of the reference CG "
+                      f"to FP64 relative residual 1e-6, one crop per thread; {dt:.1f} s"}
+
+
+# ------------------------------------------------------------------ GPU arm
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    from imscript_gb300 import simpois
+    from imscript_gb300 import lib as splib
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    insts, wname = make_workload(args.workload, rank)
+    unknowns = sum(i.unknowns for i in insts)
+    gs = [torch.from_numpy(i.g).to(dev) for i in insts]
+    fs = [None if i.f is None else torch.from_numpy(i.f).to(dev) for i in insts]
+    outs = [torch.empty_like(g) for g in gs]
+    rtol = insts[0].rtol
+    flush = torch.empty(512 * 2 ** 20 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    ctx = simpois.context(local, stream.cuda_stream)
+
+    def step_batched():
+        if len(insts) == 1:
+            _, reps = simpois.solve(gs[0], fs[0], tstep=insts[0].tstep, rtol=rtol, out=outs[0])
+        else:
+            _, reps = simpois.solve_batch(list(zip(gs, fs, [i.tstep for i in insts])), rtol=rtol,
+                                          outs=outs)
+        return reps
+
+    def step_plain():
+        reps = []
+        for g, f, i, o in zip(gs, fs, insts, outs):
+            for l in range(g.shape[0]):
+                _, r = simpois.solve(g[l:l + 1], None if f is None else f[l:l + 1], tstep=i.tstep,
+                                     rtol=rtol, out=o[l:l + 1])
+                reps += r
+        return reps
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def timed(fn, steps):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(steps)]
+        reps = None
+        barrier()
+        torch.cuda.synchronize()
+        for k in range(steps):
+            flush.fill_(float(k))
+            evs[k][0].record(stream)
+            reps = fn()
+            evs[k][1].record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        ms = sum(a.elapsed_time(b) for a, b in evs)
+        return ms, reps
+
+    for _ in range(args.warmup):
+        step_batched()
+    ctx.reset_launches()
+    with ClockSampler(local) as clocks:
+        ms, reps = timed(step_batched, args.steps)
+    launches = ctx.launches()
+    bad = [r for r in reps if r["status"] not in (splib.OK,)]
+    worst = max(r["rel_residual"] for r in reps)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = unknowns * world * args.steps / (ms / 1e3) / 1e6
+
+    # plain: one channel per call
+    for _ in range(max(1, args.warmup // 2)):
+        step_plain()
+    ms_plain, reps_plain = timed(step_plain, args.steps)
+    value_plain = unknowns * args.steps / (ms_plain / 1e3) / 1e6
+
+    # e2e: the C-ABI host entry point, pinned host buffers
+    e2e = None
+    if len(insts) == 1:
+        hg = torch.from_numpy(insts[0].g).pin_memory()
+        hf = None if insts[0].f is None else torch.from_numpy(insts[0].f).pin_memory()
+        ho = torch.empty_like(hg).pin_memory()
+        hin = (hg.numpy(), None if hf is None else hf.numpy(), ho.numpy())
+
+        def step_e2e():
+            _, r = simpois.poisson_solver_separable(hin[0], hin[1], insts[0].tstep, rtol=rtol, out=hin[2])
+            return r
+
+        step_e2e()
+        ms_e2e, _ = timed(step_e2e, args.steps)
+        bi = hg.numel() * 4 + (0 if hf is None else hf.numel() * 4)
+        e2e = {"value": unknowns * args.steps / (ms_e2e / 1e3) / 1e6, "unit": "filled Mpx/s",
+               "h2d_bytes_per_step": bi, "d2h_bytes_per_step": ho.numel() * 4,
+               "ms_per_step": ms_e2e / args.steps}
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+    peaks, src = measured_peaks()
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        cpu = cpu_baseline(insts)
+    line = {
+        "metric": "filled Mpx/s at 1e-6 rel. residual (FP64), batched vs plain on 1 GB300",
+        "value": round(value, 3),
+        "unit": "filled Mpx/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 (FP64 refinement and reductions)",
+        "data": "synthetic (seeded; shapes and distributions of the benchmark workload)",
+        "config": {"workload": wname, "unknown_samples_per_step": unknowns, "rtol": rtol,
+                   "l2": "flushed between timed steps (512 MiB write)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "plain": {"value": round(value_plain, 3), "unit": "filled Mpx/s",
+                  "ms_per_step": ms_plain / args.steps,
+                  "batched_over_plain": round(value / world / value_plain, 3)},
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+        "solver": {"max_rel_residual": worst, "iterations": [r["iterations"] for r in reps],
+                   "refinements": [r["refinements"] for r in reps], "not_ok": len(bad)},
+        "roofline": None,
+        "cpu_baseline": cpu,
+        "peaks_source": src,
+    }
+    print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    insts, wname = make_workload(args.workload, 0)
+    threads = os.cpu_count() or 1
+    sample = cpu_sample(insts, 384, max_crops=threads)
+    for _ in range(min(args.warmup, 1)):
+        cpu_time(sample[: max(1, len(sample) // 4)], threads)
+    tot_unk, tot_t = 0, 0.0
+    for _ in range(args.steps):
+        unk, dt, _ = cpu_time(sample, threads)
+        tot_unk += unk
+        tot_t += dt
+    v = tot_unk / tot_t / 1e6
+    line = {
+        "metric": "filled Mpx/s at 1e-6 rel. residual (FP64), batched vs plain on 1 GB300",
+        "impl": "reference",
+        "value": round(v, 3), "unit": "filled Mpx/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64 CG vectors, f32 stencil (as the reference)",
+        "data": "synthetic (seeded)",
+        "config": {"workload": wname, "rtol": insts[0].rtol},
+        "cpu_baseline": {"value": round(v, 3), "unit": "filled Mpx/s", "cores": threads, "kind": "port",
+                         "sample": f"per step {len(sample)} crops of 384x384 px of the workload, the "
+                                   "reference CG recipe (CG_EPS = rtol*||b||, -s 1 -c -1) in the "
+                                   "oracle's bit-exact C restatement, one crop per host thread"},
+        "e2e": {"value": round(v, 3), "unit": "filled Mpx/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="c1")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

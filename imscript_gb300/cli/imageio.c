@@ -1,0 +1,378 @@
+/*
+ * imageio.c -- iio-compatible image input/output for the simpois command
+ * (see imageio.h for the formats and conventions).
+ */
+#include "imageio.h"
+
+#include <ctype.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <unistd.h>
+
+enum { T_F32, T_F64, T_U8, T_U16, T_U32, T_U64, T_I8, T_I16, T_I32, T_I64 };
+
+/* an interleaved image as read: samples in their file type, plus float */
+typedef struct {
+	int w, h, pd;
+	int type;       /* T_* of the samples on file                      */
+	double *v;      /* w*h*pd interleaved samples, exact in double      */
+} raw_image;
+
+static void *xcalloc(size_t n, size_t s)
+{
+	void *p = calloc(n ? n : 1, s ? s : 1);
+	if (!p) fprintf(stderr, "imageio: out of memory\n");
+	return p;
+}
+
+/* whole stream into memory */
+static unsigned char *slurp(FILE *f, size_t *n)
+{
+	size_t cap = 1 << 16, len = 0;
+	unsigned char *b = malloc(cap);
+	if (!b) return NULL;
+	for (;;) {
+		if (len == cap) {
+			unsigned char *nb = realloc(b, cap *= 2);
+			if (!nb) { free(b); return NULL; }
+			b = nb;
+		}
+		size_t r = fread(b + len, 1, cap - len, f);
+		len += r;
+		if (r == 0) break;
+	}
+	*n = len;
+	return b;
+}
+
+static int type_size(int t)
+{
+	switch (t) {
+	case T_U8: case T_I8: return 1;
+	case T_U16: case T_I16: return 2;
+	case T_F32: case T_U32: case T_I32: return 4;
+	default: return 8;
+	}
+}
+
+/* little-endian sample k of type t at p */
+static double sample_le(const unsigned char *p, int t)
+{
+	uint64_t u = 0;
+	int s = type_size(t);
+	for (int k = s - 1; k >= 0; k--) u = (u << 8) | p[k];
+	switch (t) {
+	case T_U8: return (double)(uint8_t)u;
+	case T_I8: return (double)(int8_t)u;
+	case T_U16: return (double)(uint16_t)u;
+	case T_I16: return (double)(int16_t)u;
+	case T_U32: return (double)(uint32_t)u;
+	case T_I32: return (double)(int32_t)u;
+	case T_U64: return (double)u;
+	case T_I64: return (double)(int64_t)u;
+	case T_F32: { uint32_t b = (uint32_t)u; float f; memcpy(&f, &b, 4); return f; }
+	default: { double d; memcpy(&d, &u, 8); return d; }
+	}
+}
+
+/* ---- NumPy .npy 1.0 (iio.c:3216-3300: shape (h,w,pd); a (1,w,pd) array
+ * with w>1 and pd>1 is read as (w,pd,1); fortran order transposes) */
+static int read_npy(raw_image *x, const unsigned char *b, size_t n)
+{
+	if (n < 10 || b[6] != 1 || b[7] != 0) {
+		fprintf(stderr, "imageio: only NPY 1.0 is supported\n");
+		return 1;
+	}
+	size_t hl = b[8] + 256 * (size_t)b[9];
+	if (10 + hl > n) return 1;
+	char *hdr = xcalloc(hl + 1, 1);
+	if (!hdr) return 1;
+	memcpy(hdr, b + 10, hl);
+	char descr[16] = {0}, order[16] = {0};
+	int h = 1, w = 1, pd = 1;
+	int r = sscanf(hdr, "{'descr': '%15[^']', 'fortran_order': %15[^,], 'shape': (%d, %d, %d",
+			descr, order, &h, &w, &pd);
+	free(hdr);
+	if (r < 3) {
+		fprintf(stderr, "imageio: badly formed npy header\n");
+		return 2;
+	}
+	if (r < 5) pd = 1;
+	if (r < 4) w = h, h = 1;   /* a 1-D array is one row */
+	if (h == 1 && w > 1 && pd > 1) { h = w; w = pd; pd = 1; }
+	const char *d = descr;
+	if (*d == '<' || *d == '>' || *d == '=' || *d == '|') {
+		if (*d == '>' && strcmp(d + 1, "u1") && strcmp(d + 1, "i1")) {
+			fprintf(stderr, "imageio: big-endian npy is not supported\n");
+			return 3;
+		}
+		d++;
+	}
+	int t;
+	if (!strcmp(d, "f4")) t = T_F32;
+	else if (!strcmp(d, "f8")) t = T_F64;
+	else if (!strcmp(d, "u1") || !strcmp(d, "B1")) t = T_U8;
+	else if (!strcmp(d, "u2")) t = T_U16;
+	else if (!strcmp(d, "u4")) t = T_U32;
+	else if (!strcmp(d, "u8")) t = T_U64;
+	else if (!strcmp(d, "i1") || !strcmp(d, "b1")) t = T_I8;
+	else if (!strcmp(d, "i2")) t = T_I16;
+	else if (!strcmp(d, "i4")) t = T_I32;
+	else if (!strcmp(d, "i8")) t = T_I64;
+	else if (!strcmp(d, "c8")) { t = T_F32; pd *= 2; }
+	else if (!strcmp(d, "c16")) { t = T_F64; pd *= 2; }
+	else {
+		fprintf(stderr, "imageio: unrecognized npy type \"%s\"\n", d);
+		return 4;
+	}
+	if (order[0] == 'T') { int tmp = h; h = w; w = tmp; }
+	size_t ns = (size_t)w * h * pd, ts = type_size(t);
+	x->v = xcalloc(ns, sizeof(double));
+	if (!x->v) return 5;
+	size_t avail = (n - 10 - hl) / ts;
+	if (avail < ns) fprintf(stderr, "imageio: npy file smaller than expected\n");
+	for (size_t k = 0; k < ns && k < avail; k++) x->v[k] = sample_le(b + 10 + hl + k * ts, t);
+	if (order[0] == 'T') {   /* stored column-major: transpose the pixels */
+		double *tv = xcalloc(ns, sizeof(double));
+		if (!tv) return 5;
+		for (int j = 0; j < h; j++)
+			for (int i = 0; i < w; i++)
+				for (int l = 0; l < pd; l++)
+					tv[((size_t)j * w + i) * pd + l] = x->v[((size_t)i * h + j) * pd + l];
+		free(x->v);
+		x->v = tv;
+	}
+	x->w = w; x->h = h; x->pd = pd; x->type = t;
+	return 0;
+}
+
+/* ---- PFM: "Pf" gray or "PF" color, rows as stored, little-endian floats */
+static int read_pfm(raw_image *x, const unsigned char *b, size_t n)
+{
+	int pd = b[1] == 'F' ? 3 : 1, w, h, used = 0;
+	float scale;
+	char tmp[128] = {0};
+	memcpy(tmp, b, n < 127 ? n : 127);
+	if (sscanf(tmp + 2, "%d %d %g%n", &w, &h, &scale, &used) != 3) return 1;
+	size_t off = 2 + used + 1;
+	size_t ns = (size_t)w * h * pd;
+	if (off + 4 * ns > n) {
+		fprintf(stderr, "imageio: truncated pfm\n");
+		return 2;
+	}
+	x->v = xcalloc(ns, sizeof(double));
+	if (!x->v) return 3;
+	for (size_t k = 0; k < ns; k++) x->v[k] = sample_le(b + off + 4 * k, T_F32);
+	x->w = w; x->h = h; x->pd = pd; x->type = T_F32;
+	return 0;
+}
+
+/* ---- PNM: P2/P3 ascii, P5/P6 binary (8 or 16 bits, big-endian) */
+static int pnm_int(const unsigned char *b, size_t n, size_t *p, int *v)
+{
+	while (*p < n) {
+		if (b[*p] == '#') { while (*p < n && b[*p] != '\n') (*p)++; }
+		else if (isspace(b[*p])) (*p)++;
+		else break;
+	}
+	if (*p >= n || !isdigit(b[*p])) return 1;
+	long r = 0;
+	while (*p < n && isdigit(b[*p])) r = 10 * r + (b[(*p)++] - '0');
+	*v = (int)r;
+	return 0;
+}
+
+static int read_pnm(raw_image *x, const unsigned char *b, size_t n)
+{
+	char kind = b[1];
+	int pd = (kind == '3' || kind == '6') ? 3 : 1, w, h, mx;
+	size_t p = 2;
+	if (pnm_int(b, n, &p, &w) || pnm_int(b, n, &p, &h) || pnm_int(b, n, &p, &mx)) return 1;
+	size_t ns = (size_t)w * h * pd;
+	x->v = xcalloc(ns, sizeof(double));
+	if (!x->v) return 2;
+	if (kind == '2' || kind == '3') {
+		for (size_t k = 0; k < ns; k++) {
+			int v;
+			if (pnm_int(b, n, &p, &v)) break;
+			x->v[k] = v;
+		}
+	} else {
+		p++;   /* the single whitespace after maxval */
+		int bps = mx > 255 ? 2 : 1;
+		for (size_t k = 0; k < ns && p + bps <= n; k++, p += bps)
+			x->v[k] = bps == 1 ? b[p] : 256 * b[p] + b[p + 1];
+	}
+	x->w = w; x->h = h; x->pd = pd; x->type = mx > 255 ? T_U16 : T_U8;
+	return 0;
+}
+
+/* ---- ASC: "w h 1 pd" header then planar samples (iio.c:2796-2830) */
+static int read_asc(raw_image *x, const unsigned char *b, size_t n)
+{
+	char *s = xcalloc(n + 1, 1);
+	if (!s) return 1;
+	memcpy(s, b, n);
+	int w, h, d, pd, used;
+	if (sscanf(s, "%d %d %d %d%n", &w, &h, &d, &pd, &used) != 4 || d != 1) { free(s); return 1; }
+	size_t ns = (size_t)w * h * pd;
+	double *planar = xcalloc(ns, sizeof(double));
+	x->v = xcalloc(ns, sizeof(double));
+	if (!planar || !x->v) { free(s); free(planar); return 2; }
+	char *save = NULL, *tok = strtok_r(s + used, " \n", &save);
+	for (size_t k = 0; k < ns && tok; k++, tok = strtok_r(NULL, " \n", &save)) planar[k] = atof(tok);
+	for (size_t i = 0; i < (size_t)w * h; i++)
+		for (int l = 0; l < pd; l++) x->v[i * pd + l] = planar[(size_t)w * h * l + i];
+	free(planar);
+	free(s);
+	x->w = w; x->h = h; x->pd = pd; x->type = T_F32;
+	return 0;
+}
+
+static int read_raw(const char *name, raw_image *x)
+{
+	FILE *f = strcmp(name, "-") ? fopen(name, "rb") : stdin;
+	if (!f) {
+		fprintf(stderr, "imageio: can not open file \"%s\" in mode \"r\"\n", name);
+		return 1;
+	}
+	size_t n = 0;
+	unsigned char *b = slurp(f, &n);
+	if (f != stdin) fclose(f);
+	if (!b) return 1;
+	int r = 1;
+	if (n >= 4 && b[0] == 0x93 && b[1] == 'N' && b[2] == 'U' && b[3] == 'M') r = read_npy(x, b, n);
+	else if (n >= 2 && b[0] == 'P' && (b[1] == 'f' || b[1] == 'F')) r = read_pfm(x, b, n);
+	else if (n >= 2 && b[0] == 'P' && strchr("2356", b[1])) r = read_pnm(x, b, n);
+	else {
+		int t[4];
+		char head[256] = {0};
+		memcpy(head, b, n < 255 ? n : 255);
+		if (sscanf(head, "%d %d %d %d", t, t + 1, t + 2, t + 3) == 4 && t[2] == 1)
+			r = read_asc(x, b, n);
+		else
+			fprintf(stderr, "imageio: unrecognized format of \"%s\"\n", name);
+	}
+	free(b);
+	if (r) fprintf(stderr, "imageio: could not read image \"%s\"\n", name);
+	return r;
+}
+
+float *imgio_read_split(const char *name, int *w, int *h, int *pd)
+{
+	raw_image x = {0};
+	if (read_raw(name, &x)) { free(x.v); return NULL; }
+	size_t np = (size_t)x.w * x.h;
+	float *o = xcalloc(np * x.pd, sizeof(float));
+	if (o)
+		for (size_t i = 0; i < np; i++)
+			for (int l = 0; l < x.pd; l++) o[np * l + i] = (float)x.v[i * x.pd + l];
+	free(x.v);
+	*w = x.w; *h = x.h; *pd = x.pd;
+	return o;
+}
+
+/* gray value in the sample type of the file, then float (iio.c:1230-1300) */
+static float gray_of(const double *p, int type)
+{
+	double g = .299 * p[0] + .587 * p[1] + .114 * p[2];
+	switch (type) {
+	case T_U8: return (float)(uint8_t)g;
+	case T_U16: return (float)(uint16_t)g;
+	case T_F64: return (float)g;
+	default: return (float)g;
+	}
+}
+
+float *imgio_read_gray(const char *name, int *w, int *h)
+{
+	raw_image x = {0};
+	if (read_raw(name, &x)) { free(x.v); return NULL; }
+	size_t np = (size_t)x.w * x.h;
+	float *o = NULL;
+	if (x.pd == 1 || x.pd == 3 || x.pd == 4) {
+		o = xcalloc(np, sizeof(float));
+		if (o)
+			for (size_t i = 0; i < np; i++)
+				o[i] = x.pd == 1 ? (float)x.v[i] : gray_of(x.v + i * x.pd, x.type);
+	} else {
+		fprintf(stderr, "imageio: non-scalarizable image \"%s\"\n", name);
+	}
+	free(x.v);
+	*w = x.w; *h = x.h;
+	return o;
+}
+
+/* ---------------------------------------------------------------- writing */
+
+static int suffix(const char *s, const char *suf)
+{
+	size_t a = strlen(s), b = strlen(suf);
+	return a >= b && !strcmp(s + a - b, suf);
+}
+
+static FILE *open_out(const char *name)
+{
+	FILE *f = strcmp(name, "-") ? fopen(name, "wb") : stdout;
+	if (!f) fprintf(stderr, "imageio: can not open file \"%s\" in mode \"w\"\n", name);
+	return f;
+}
+
+static int close_out(FILE *f)
+{
+	if (f == stdout) return fflush(f) ? 1 : 0;
+	return fclose(f) ? 1 : 0;
+}
+
+int imgio_write_split(const char *name, const float *x, int w, int h, int pd)
+{
+	size_t np = (size_t)w * h, ns = np * pd;
+	if (!strcmp(name, "-") && isatty(1)) {
+		printf("IMAGE %dx%d,%d float\n", w, h, pd);
+		return 0;
+	}
+	float *v = malloc(sizeof(float) * (ns ? ns : 1));   /* interleaved */
+	if (!v) return 1;
+	for (size_t i = 0; i < np; i++)
+		for (int l = 0; l < pd; l++) v[i * pd + l] = x[np * l + i];
+	int rc = 0;
+	FILE *f = open_out(name);
+	if (!f) { free(v); return 1; }
+	if ((suffix(name, ".pfm")) && (pd == 1 || pd == 3)) {
+		fprintf(f, "P%c\n%d %d\n%g\n", pd > 1 ? 'F' : 'f', w, h, -1.0);
+		rc = fwrite(v, sizeof(float), ns, f) != ns;
+	} else if ((suffix(name, ".ppm") || suffix(name, ".pgm")) && (pd == 1 || pd == 3)) {
+		fprintf(f, "P%c\n%d %d\n%g\n", pd > 1 ? '3' : '2', w, h, 255.0);
+		for (size_t k = 0; k < ns; k++) fprintf(f, "%d\n", (int)v[k]);
+	} else if (suffix(name, ".csv") && pd == 1) {
+		for (size_t k = 0; k < ns; k++) fprintf(f, "%.9g%c", v[k], (k + 1) % w ? ',' : '\n');
+	} else if (suffix(name, ".txt") && (pd == 1 || w == 1 || h == 1)) {
+		/* rows of w samples; a single row or column of pd-vectors is
+		 * written one pixel per line */
+		size_t rw = pd == 1 ? (size_t)w : (size_t)pd;
+		for (size_t k = 0; k < ns; k++) fprintf(f, "%.9g%c", v[k], (k + 1) % rw ? ' ' : '\n');
+	} else if (suffix(name, ".asc")) {
+		fprintf(f, "%d %d 1 %d\n", w, h, pd);
+		for (size_t k = 0; k < ns; k++) fprintf(f, "%.9g\n", x[k]);   /* planar */
+	} else {
+		char hdr[256];
+		int n = snprintf(hdr, sizeof hdr,
+				"{'descr': '<f4', 'fortran_order': False, 'shape': (%d, %d, %d)}", h, w, pd);
+		int total = ((10 + n + 1 + 15) / 16) * 16;
+		unsigned char pre[10] = {0x93, 'N', 'U', 'M', 'P', 'Y', 1, 0, 0, 0};
+		pre[8] = (total - 10) % 256;
+		pre[9] = (total - 10) / 256;
+		fwrite(pre, 1, 10, f);
+		fwrite(hdr, 1, n, f);
+		for (int k = 10 + n; k < total - 1; k++) fputc(' ', f);
+		fputc('\n', f);
+		rc = fwrite(v, sizeof(float), ns, f) != ns;
+	}
+	rc |= close_out(f);
+	free(v);
+	if (rc) fprintf(stderr, "imageio: error writing \"%s\"\n", name);
+	return rc;
+}

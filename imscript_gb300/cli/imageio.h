@@ -1,0 +1,30 @@
+/*
+ * imageio.h -- the image reading and writing the simpois command needs,
+ * following iio's conventions (iio.h:33-43, iio.c:5164-5346, 6166-6300):
+ *
+ *  - images are returned "split": planar float, x[w*h*l + w*j + i];
+ *  - "-" names stdin (reading) or stdout (writing);
+ *  - the input format is sniffed from the first bytes: NumPy .npy (1.0,
+ *    every numeric dtype), PFM ("Pf"/"PF"), PNM ("P2","P3","P5","P6") and the
+ *    ASC text format ("w h 1 pd" header, planar samples);
+ *  - the output format follows the file-name suffix: .pfm (1 or 3 channels),
+ *    .ppm/.pgm (1 or 3 channels, ASCII integers), .asc, .npy; any other name,
+ *    and a stdout that is not a terminal, get NumPy .npy.  A terminal stdout
+ *    gets the one-line "IMAGE wxh,pd float" summary.
+ *
+ * Errors print a message and return NULL / nonzero; nothing exits.
+ */
+#ifndef SIMPOIS_IMAGEIO_H
+#define SIMPOIS_IMAGEIO_H
+
+/* Planar float image of *w x *h x *pd, or NULL with a message on stderr. */
+float *imgio_read_split(const char *name, int *w, int *h, int *pd);
+
+/* Single-channel float image; 3 (RGB) and 4 (RGBA) channel images are
+ * converted to gray with the weights .299 .587 .114 (iio.c:1230-1300). */
+float *imgio_read_gray(const char *name, int *w, int *h);
+
+/* Write a planar float image; returns 0 on success. */
+int imgio_write_split(const char *name, const float *x, int w, int h, int pd);
+
+#endif

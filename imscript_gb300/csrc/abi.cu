@@ -1,0 +1,524 @@
+// abi.cu -- the C ABI of libsimpois_gpu (include/simpois_gpu.h): contexts,
+// parameter handling, the host/device/batched entry points, the adjoint, and
+// the drop-in poisson_solver_separable / poisson_rec symbols.
+#include <math.h>
+#include <stdarg.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <mutex>
+
+#include "common.cuh"
+#include "solvers.h"
+
+// ------------------------------------------------------------------ context plumbing
+
+int ctx_fail(simpois_ctx *ctx, int status, const char *fmt, ...)
+{
+	char buf[512];
+	va_list ap;
+	va_start(ap, fmt);
+	vsnprintf(buf, sizeof buf, fmt, ap);
+	va_end(ap);
+	if (ctx) ctx->last_error = buf;
+	return status;
+}
+
+int ctx_arena_reserve(simpois_ctx *ctx, size_t bytes)
+{
+	if (bytes <= ctx->arena_cap) return SIMPOIS_OK;
+	if (ctx->arena) {
+		cudaStreamSynchronize(ctx->stream);
+		cudaFree(ctx->arena);
+		ctx->arena = nullptr;
+		ctx->arena_cap = 0;
+	}
+	size_t cap = bytes + bytes / 8 + (1 << 20);
+	if (cudaMalloc((void **)&ctx->arena, cap) != cudaSuccess) {
+		cudaGetLastError();
+		return ctx_fail(ctx, SIMPOIS_ENOMEM, "cannot allocate %zu bytes of device memory", cap);
+	}
+	ctx->arena_cap = cap;
+	return SIMPOIS_OK;
+}
+
+int ctx_pinned_reserve(simpois_ctx *ctx, size_t bytes)
+{
+	if (bytes <= ctx->pinned_cap) return SIMPOIS_OK;
+	if (ctx->pinned) {
+		cudaStreamSynchronize(ctx->stream);
+		cudaFreeHost(ctx->pinned);
+		ctx->pinned = nullptr;
+		ctx->pinned_cap = 0;
+	}
+	size_t cap = bytes < 65536 ? 65536 : bytes + bytes / 4;
+	if (cudaMallocHost((void **)&ctx->pinned, cap) != cudaSuccess) {
+		cudaGetLastError();
+		return ctx_fail(ctx, SIMPOIS_ENOMEM, "cannot allocate %zu bytes of pinned memory", cap);
+	}
+	ctx->pinned_cap = cap;
+	return SIMPOIS_OK;
+}
+
+int ctx_io_reserve(simpois_ctx *ctx, size_t bytes)
+{
+	if (bytes <= ctx->io_cap) return SIMPOIS_OK;
+	if (ctx->io) {
+		cudaStreamSynchronize(ctx->stream);
+		cudaFree(ctx->io);
+		ctx->io = nullptr;
+		ctx->io_cap = 0;
+	}
+	if (cudaMalloc((void **)&ctx->io, bytes) != cudaSuccess) {
+		cudaGetLastError();
+		return ctx_fail(ctx, SIMPOIS_ENOMEM, "cannot allocate %zu bytes of device memory", bytes);
+	}
+	ctx->io_cap = bytes;
+	return SIMPOIS_OK;
+}
+
+namespace {
+
+// per-channel NaN counts of a planar image
+__global__ void k_count_nan(const float *__restrict__ g, size_t cs, int *__restrict__ counts)
+{
+	size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+	int l = blockIdx.y;
+	int c = (k < cs && isnan(g[cs * l + k])) ? 1 : 0;
+	for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+	if ((threadIdx.x & 31) == 0 && c) atomicAdd(counts + l, c);
+}
+
+int check_dims(simpois_ctx *ctx, int w, int h, int pd)
+{
+	if (w <= 0 || h <= 0 || pd <= 0)
+		return ctx_fail(ctx, SIMPOIS_EINVAL, "bad image size %dx%dx%d", w, h, pd);
+	if ((long long)w * h >= (1LL << 31))
+		return ctx_fail(ctx, SIMPOIS_EINVAL, "image of %dx%d exceeds 2^31 pixels per channel", w, h);
+	return SIMPOIS_OK;
+}
+
+int worst(int a, int b) { return a > b ? a : b; }
+
+// Reference schedule with per-channel unknown counts in the reports.
+int run_reference(simpois_ctx *ctx, float *out, const float *in, const float *dat, int w, int h, int pd,
+		const simpois_params *p, simpois_report *rep)
+{
+	size_t ws_bytes = ref_workspace_bytes(w, h, pd, dat != nullptr) + 256 * pd + 4096;
+	int rc = ctx_arena_reserve(ctx, ws_bytes);
+	if (rc) return rc;
+	int *counts = (int *)(ctx->arena + ws_bytes - 256 * pd - 2048);
+	SP_CUDA(ctx, cudaMemsetAsync(counts, 0, sizeof(int) * pd, ctx->stream));
+	size_t cs = (size_t)w * h;
+	dim3 G((unsigned)((cs + 255) / 256), pd);
+	k_count_nan<<<G, 256, 0, ctx->stream>>>(in, cs, counts);
+	ctx->launches++;
+	SP_LAUNCH_CHECK(ctx);
+	rc = ref_solve(ctx, out, in, dat, w, h, pd, p, rep, ctx->arena);
+	if (rc) return rc;
+	rc = ctx_pinned_reserve(ctx, 65536);
+	if (rc) return rc;
+	int *hc = (int *)ctx->pinned;
+	SP_CUDA(ctx, cudaMemcpyAsync(hc, counts, sizeof(int) * pd, cudaMemcpyDeviceToHost, ctx->stream));
+	SP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+	for (int l = 0; l < pd; l++) {
+		rep[l].unknowns = hc[l];
+		rep[l].refinements = 0;
+		rep[l].rel_residual = -1;
+		rep[l].rel_residual_out = -1;
+	}
+	return SIMPOIS_OK;
+}
+
+// Converged schedule over the channels of several images; the singular
+// channels (no known pixel) are redone with the reference schedule.
+int run_converged(simpois_ctx *ctx, const simpois_image *im, int n, const simpois_params *p,
+		simpois_report *rep)
+{
+	std::vector<MgProblem> probs;
+	std::vector<int> img_of;
+	for (int k = 0; k < n; k++) {
+		float t = im[k].tstep;
+		if (t < -1000)
+			return ctx_fail(ctx, SIMPOIS_EINVAL,
+				"the triharmonic operator (tstep < -1000) has no converged schedule; use rtol = 0");
+		size_t cs = (size_t)im[k].w * im[k].h;
+		for (int l = 0; l < im[k].pd; l++) {
+			MgProblem q;
+			q.g = im[k].in + cs * l;
+			q.f = im[k].dat ? im[k].dat + cs * l : nullptr;
+			q.out = im[k].out + cs * l;
+			q.w = im[k].w;
+			q.h = im[k].h;
+			q.kind = t < 0 ? 1 : 0;
+			q.rtol = im[k].rtol > 0 ? im[k].rtol : p->rtol;
+			probs.push_back(q);
+			img_of.push_back(k);
+		}
+	}
+	MgOptions opt;
+	opt.max_iter = p->max_iter > 0 ? p->max_iter : 500;
+	opt.use_mg = !(p->flags & SIMPOIS_FLAG_NO_MG);
+	opt.use_graph = !(p->flags & SIMPOIS_FLAG_NO_GRAPH);
+	opt.out_resid = (p->flags & SIMPOIS_FLAG_OUT_RESID) != 0;
+	int rc = SIMPOIS_OK;
+	// one batched solve per operator kind
+	for (int kind = 0; kind < 2; kind++) {
+		std::vector<MgProblem> sub;
+		std::vector<int> where;
+		for (size_t q = 0; q < probs.size(); q++)
+			if (probs[q].kind == kind) {
+				sub.push_back(probs[q]);
+				where.push_back((int)q);
+			}
+		if (sub.empty()) continue;
+		std::vector<simpois_report> r(sub.size());
+		rc = mg_solve(ctx, sub.data(), (int)sub.size(), opt, r.data());
+		if (rc) return rc;
+		for (size_t q = 0; q < sub.size(); q++) rep[where[q]] = r[q];
+	}
+	// singular channels: the reference schedule, as the reference would run them
+	for (size_t q = 0; q < probs.size(); q++) {
+		if (rep[q].status != SIMPOIS_SINGULAR) continue;
+		simpois_params pr = *p;
+		pr.tstep = im[img_of[q]].tstep;
+		pr.rtol = 0;
+		simpois_report r1;
+		rc = run_reference(ctx, probs[q].out, probs[q].g, probs[q].f, probs[q].w, probs[q].h, 1, &pr, &r1);
+		if (rc) return rc;
+		rep[q].iterations = r1.iterations;
+	}
+	return SIMPOIS_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ public API
+
+extern "C" {
+
+void simpois_default_params(simpois_params *p)
+{
+	if (!p) return;
+	memset(p, 0, sizeof *p);
+	p->tstep = 0.25f;
+	p->niter = 10;
+	p->scale = 99;
+	p->cgit = 0;
+	p->pmsfac = 3;
+	p->ponlit = 0;
+	p->cg_eps = -1;
+	p->rtol = 0;
+	p->max_iter = 0;
+	p->flags = 0;
+}
+
+static void env_double(const char *name, double *v)
+{
+	const char *s = getenv(name);
+	double y;
+	if (s && sscanf(s, "%lf", &y) == 1) *v = y;
+}
+
+void simpois_params_from_env(simpois_params *p)
+{
+	if (!p) return;
+	env_double("PMSFAC", &p->pmsfac);
+	env_double("PONLIT", &p->ponlit);
+	env_double("CG_EPS", &p->cg_eps);
+	env_double("SIMPOIS_RTOL", &p->rtol);
+}
+
+const char *simpois_strerror(int status)
+{
+	switch (status) {
+	case SIMPOIS_OK: return "ok";
+	case SIMPOIS_EINVAL: return "invalid argument";
+	case SIMPOIS_ENOMEM: return "out of memory";
+	case SIMPOIS_NOT_CONVERGED: return "tolerance not reached within the iteration cap";
+	case SIMPOIS_BREAKDOWN: return "Krylov breakdown";
+	case SIMPOIS_ECUDA: return "CUDA error";
+	case SIMPOIS_ENODEV: return "no usable CUDA device";
+	case SIMPOIS_SINGULAR: return "no known pixel: singular system";
+	}
+	return "unknown status";
+}
+
+const char *simpois_last_error(const simpois_ctx *ctx)
+{
+	return ctx ? ctx->last_error.c_str() : "";
+}
+
+int simpois_create(simpois_ctx **out, int device, void *stream)
+{
+	if (!out) return SIMPOIS_EINVAL;
+	*out = nullptr;
+	int ndev = 0;
+	if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+		cudaGetLastError();
+		return SIMPOIS_ENODEV;
+	}
+	if (device < 0 || device >= ndev) return SIMPOIS_EINVAL;
+	if (cudaSetDevice(device) != cudaSuccess) {
+		cudaGetLastError();
+		return SIMPOIS_ENODEV;
+	}
+	simpois_ctx *c = new (std::nothrow) simpois_ctx();
+	if (!c) return SIMPOIS_ENOMEM;
+	c->device = device;
+	c->stream = (cudaStream_t)stream;
+	cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+	if (cudaStreamCreateWithFlags(&c->capture_stream, cudaStreamNonBlocking) != cudaSuccess) {
+		cudaGetLastError();
+		delete c;
+		return SIMPOIS_ECUDA;
+	}
+	*out = c;
+	return SIMPOIS_OK;
+}
+
+int simpois_destroy(simpois_ctx *ctx)
+{
+	if (!ctx) return SIMPOIS_OK;
+	cudaSetDevice(ctx->device);
+	cudaStreamSynchronize(ctx->stream);
+	if (ctx->arena) cudaFree(ctx->arena);
+	if (ctx->io) cudaFree(ctx->io);
+	if (ctx->pinned) cudaFreeHost(ctx->pinned);
+	if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
+	delete ctx;
+	return SIMPOIS_OK;
+}
+
+int simpois_solve_device(simpois_ctx *ctx, float *out, const float *in, const float *dat, int w, int h,
+		int pd, const simpois_params *params, simpois_report *reports)
+{
+	if (!ctx || !out || !in) return ctx_fail(ctx, SIMPOIS_EINVAL, "null context or buffer");
+	int rc = check_dims(ctx, w, h, pd);
+	if (rc) return rc;
+	simpois_params p;
+	if (params) p = *params; else simpois_default_params(&p);
+	if (cudaSetDevice(ctx->device) != cudaSuccess) return ctx_fail(ctx, SIMPOIS_ECUDA, "cudaSetDevice");
+	std::vector<simpois_report> rep(pd);
+	memset(rep.data(), 0, sizeof(simpois_report) * pd);
+	if (p.rtol > 0) {
+		simpois_image im = {in, dat, out, w, h, pd, p.tstep, p.rtol};
+		rc = run_converged(ctx, &im, 1, &p, rep.data());
+	} else {
+		rc = run_reference(ctx, out, in, dat, w, h, pd, &p, rep.data());
+	}
+	if (rc) return rc;
+	SP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+	int st = SIMPOIS_OK;
+	for (int l = 0; l < pd; l++) st = worst(st, rep[l].status == SIMPOIS_SINGULAR ? SIMPOIS_OK : rep[l].status);
+	if (reports) memcpy(reports, rep.data(), sizeof(simpois_report) * pd);
+	return st;
+}
+
+int simpois_solve(simpois_ctx *ctx, float *out, const float *in, const float *dat, int w, int h, int pd,
+		const simpois_params *params, simpois_report *reports)
+{
+	if (!ctx || !out || !in) return ctx_fail(ctx, SIMPOIS_EINVAL, "null context or buffer");
+	int rc = check_dims(ctx, w, h, pd);
+	if (rc) return rc;
+	if (cudaSetDevice(ctx->device) != cudaSuccess) return ctx_fail(ctx, SIMPOIS_ECUDA, "cudaSetDevice");
+	size_t n = (size_t)w * h * pd;
+	size_t bytes = n * sizeof(float);
+	size_t slot = (bytes + 255) / 256 * 256;
+	rc = ctx_io_reserve(ctx, slot * (dat ? 3 : 2));
+	if (rc) return rc;
+	float *din = (float *)ctx->io, *dout = (float *)(ctx->io + slot);
+	float *ddat = dat ? (float *)(ctx->io + 2 * slot) : nullptr;
+	cudaStream_t s = ctx->stream;
+	SP_CUDA(ctx, cudaMemcpyAsync(din, in, bytes, cudaMemcpyHostToDevice, s));
+	if (dat) SP_CUDA(ctx, cudaMemcpyAsync(ddat, dat, bytes, cudaMemcpyHostToDevice, s));
+	int st = simpois_solve_device(ctx, dout, din, ddat, w, h, pd, params, reports);
+	if (st != SIMPOIS_OK && st != SIMPOIS_NOT_CONVERGED && st != SIMPOIS_BREAKDOWN) return st;
+	SP_CUDA(ctx, cudaMemcpyAsync(out, dout, bytes, cudaMemcpyDeviceToHost, s));
+	SP_CUDA(ctx, cudaStreamSynchronize(s));
+	return st;
+}
+
+int simpois_solve_batch(simpois_ctx *ctx, const simpois_image *images, int n, const simpois_params *params,
+		simpois_report *reports)
+{
+	if (!ctx || (!images && n > 0) || n < 0) return ctx_fail(ctx, SIMPOIS_EINVAL, "bad batch");
+	simpois_params p;
+	if (params) p = *params; else simpois_default_params(&p);
+	if (cudaSetDevice(ctx->device) != cudaSuccess) return ctx_fail(ctx, SIMPOIS_ECUDA, "cudaSetDevice");
+	int total = 0;
+	for (int k = 0; k < n; k++) {
+		if (!images[k].in || !images[k].out) return ctx_fail(ctx, SIMPOIS_EINVAL, "image %d: null buffer", k);
+		int rc = check_dims(ctx, images[k].w, images[k].h, images[k].pd);
+		if (rc) return rc;
+		total += images[k].pd;
+	}
+	std::vector<simpois_report> rep(total);
+	memset(rep.data(), 0, sizeof(simpois_report) * total);
+	// converged images share one batched solve; reference-schedule images run one by one
+	std::vector<simpois_image> conv;
+	std::vector<int> conv_first;
+	int base = 0, rc = SIMPOIS_OK;
+	for (int k = 0; k < n; k++) {
+		double rtol = images[k].rtol > 0 ? images[k].rtol : p.rtol;
+		if (rtol > 0) {
+			conv.push_back(images[k]);
+			conv_first.push_back(base);
+		} else {
+			simpois_params pk = p;
+			pk.tstep = images[k].tstep;
+			rc = run_reference(ctx, images[k].out, images[k].in, images[k].dat, images[k].w, images[k].h,
+					images[k].pd, &pk, rep.data() + base);
+			if (rc) return rc;
+		}
+		base += images[k].pd;
+	}
+	if (!conv.empty()) {
+		int nch = 0;
+		for (auto &im : conv) nch += im.pd;
+		std::vector<simpois_report> r(nch);
+		rc = run_converged(ctx, conv.data(), (int)conv.size(), &p, r.data());
+		if (rc) return rc;
+		int q = 0;
+		for (size_t k = 0; k < conv.size(); k++)
+			for (int l = 0; l < conv[k].pd; l++) rep[conv_first[k] + l] = r[q++];
+	}
+	SP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+	int st = SIMPOIS_OK;
+	for (int l = 0; l < total; l++) st = worst(st, rep[l].status == SIMPOIS_SINGULAR ? SIMPOIS_OK : rep[l].status);
+	if (reports) memcpy(reports, rep.data(), sizeof(simpois_report) * total);
+	return st;
+}
+
+int simpois_residual_device(simpois_ctx *ctx, const float *u, const float *in, const float *dat, int w, int h,
+		int pd, int kind, double *rel, double *bnorm)
+{
+	if (!ctx || !u || !in || !rel) return ctx_fail(ctx, SIMPOIS_EINVAL, "null context or buffer");
+	int rc = check_dims(ctx, w, h, pd);
+	if (rc) return rc;
+	if (kind != 0 && kind != 1) return ctx_fail(ctx, SIMPOIS_EINVAL, "kind must be 0 or 1");
+	if (cudaSetDevice(ctx->device) != cudaSuccess) return ctx_fail(ctx, SIMPOIS_ECUDA, "cudaSetDevice");
+	size_t cs = (size_t)w * h;
+	std::vector<MgProblem> probs(pd);
+	std::vector<const float *> us(pd);
+	for (int l = 0; l < pd; l++) {
+		probs[l].g = in + cs * l;
+		probs[l].f = dat ? dat + cs * l : nullptr;
+		probs[l].out = nullptr;
+		probs[l].w = w;
+		probs[l].h = h;
+		probs[l].kind = kind;
+		probs[l].rtol = 0;
+		us[l] = u + cs * l;
+	}
+	std::vector<double> bn(pd);
+	rc = mg_residual(ctx, probs.data(), us.data(), pd, rel, bn.data());
+	if (rc) return rc;
+	if (bnorm) memcpy(bnorm, bn.data(), sizeof(double) * pd);
+	return SIMPOIS_OK;
+}
+
+int simpois_adjoint_device(simpois_ctx *ctx, const float *grad_out, const float *in, int w, int h, int pd,
+		float *grad_in, float *grad_dat, const simpois_params *params, simpois_report *reports)
+{
+	if (!ctx || !grad_out || !in || !grad_in) return ctx_fail(ctx, SIMPOIS_EINVAL, "null context or buffer");
+	int rc = check_dims(ctx, w, h, pd);
+	if (rc) return rc;
+	simpois_params p;
+	if (params) p = *params; else simpois_default_params(&p);
+	if (p.tstep < 0)
+		return ctx_fail(ctx, SIMPOIS_EINVAL, "the adjoint covers the symmetric 5-point operator (tstep > 0)");
+	if (cudaSetDevice(ctx->device) != cudaSuccess) return ctx_fail(ctx, SIMPOIS_ECUDA, "cudaSetDevice");
+	size_t cs = (size_t)w * h;
+	std::vector<MgProblem> probs(pd);
+	std::vector<const float *> go(pd);
+	std::vector<float *> gi(pd), gd(pd);
+	for (int l = 0; l < pd; l++) {
+		probs[l].g = in + cs * l;
+		probs[l].f = nullptr;
+		probs[l].out = nullptr;
+		probs[l].w = w;
+		probs[l].h = h;
+		probs[l].kind = 0;
+		probs[l].rtol = p.rtol > 0 ? p.rtol : 1e-6;
+		go[l] = grad_out + cs * l;
+		gi[l] = grad_in + cs * l;
+		gd[l] = grad_dat ? grad_dat + cs * l : nullptr;
+	}
+	MgOptions opt;
+	opt.max_iter = p.max_iter > 0 ? p.max_iter : 500;
+	opt.use_mg = !(p.flags & SIMPOIS_FLAG_NO_MG);
+	opt.use_graph = !(p.flags & SIMPOIS_FLAG_NO_GRAPH);
+	opt.mode = MG_ADJOINT;
+	opt.grad_out = go.data();
+	opt.grad_in = gi.data();
+	opt.grad_dat = gd.data();
+	std::vector<simpois_report> rep(pd);
+	memset(rep.data(), 0, sizeof(simpois_report) * pd);
+	rc = mg_solve(ctx, probs.data(), pd, opt, rep.data());
+	if (rc) return rc;
+	SP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+	int st = SIMPOIS_OK;
+	for (int l = 0; l < pd; l++) st = worst(st, rep[l].status == SIMPOIS_SINGULAR ? SIMPOIS_OK : rep[l].status);
+	if (reports) memcpy(reports, rep.data(), sizeof(simpois_report) * pd);
+	return st;
+}
+
+long long simpois_launch_count(const simpois_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+void simpois_reset_launch_count(simpois_ctx *ctx)
+{
+	if (ctx) ctx->launches = 0;
+}
+
+// ------------------------------------------------------------------ drop-in symbols
+
+static std::mutex g_dropin_mu;
+static simpois_ctx *g_dropin_ctx = nullptr;
+static simpois_params g_dropin_env;
+static bool g_dropin_env_read = false;
+
+static int dropin_solve(float *out, float *in, float *dat, int w, int h, int pd, float tstep, int niter,
+		int scale, int cgit)
+{
+	std::lock_guard<std::mutex> lock(g_dropin_mu);
+	if (!g_dropin_env_read) {
+		simpois_default_params(&g_dropin_env);
+		simpois_params_from_env(&g_dropin_env);
+		g_dropin_env_read = true;
+	}
+	int rc = SIMPOIS_OK;
+	if (!g_dropin_ctx) rc = simpois_create(&g_dropin_ctx, 0, nullptr);
+	if (rc) {
+		fprintf(stderr, "simpois: %s\n", simpois_strerror(rc));
+		return rc;
+	}
+	simpois_params p = g_dropin_env;
+	p.tstep = tstep;
+	p.niter = niter;
+	p.scale = scale;
+	p.cgit = cgit;
+	rc = simpois_solve(g_dropin_ctx, out, in, dat, w, h, pd, &p, nullptr);
+	if (rc != SIMPOIS_OK)
+		fprintf(stderr, "simpois: %s (%s)\n", simpois_strerror(rc), simpois_last_error(g_dropin_ctx));
+	return rc;
+}
+
+void poisson_solver_separable(float *out, float *in, float *dat, int w, int h, int pd, float tstep, int niter,
+		int scale, float cgrad)
+{
+	int rc = dropin_solve(out, in, dat, w, h, pd, tstep, niter, scale, (int)cgrad);
+	if (rc != SIMPOIS_OK && rc != SIMPOIS_NOT_CONVERGED && rc != SIMPOIS_BREAKDOWN && out && in && out != in &&
+			w > 0 && h > 0 && pd > 0)
+		memcpy(out, in, sizeof(float) * (size_t)w * h * pd);
+}
+
+void poisson_rec(float *u, float *g, float *f, int w, int h, float tstep, int niter, int scale, int cgit)
+{
+	int rc = dropin_solve(u, g, f, w, h, 1, tstep, niter, scale, cgit);
+	if (rc != SIMPOIS_OK && rc != SIMPOIS_NOT_CONVERGED && rc != SIMPOIS_BREAKDOWN && u && g && u != g && w > 0 &&
+			h > 0)
+		memcpy(u, g, sizeof(float) * (size_t)w * h);
+}
+
+}  // extern "C"

@@ -1,0 +1,108 @@
+// common.cuh -- shared internals of libsimpois_gpu: the context, the device
+// arena, error plumbing and the block-reduction helpers every solver kernel
+// uses.  Target: sm_103a (GB300), one process per GPU.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/simpois_gpu.h"
+
+// ---------------------------------------------------------------- context
+
+struct simpois_ctx {
+	int device = 0;
+	cudaStream_t stream = nullptr;
+	// private stream used only to capture CUDA graphs (capture is not
+	// allowed on the legacy default stream); graphs replay on `stream`
+	cudaStream_t capture_stream = nullptr;
+	int sm_count = 0;
+	std::string last_error;
+
+	// device arena: one allocation reused by every solve on this context
+	char *arena = nullptr;
+	size_t arena_cap = 0;
+
+	// pinned host staging for small read-backs (counts, flags, reports)
+	char *pinned = nullptr;
+	size_t pinned_cap = 0;
+
+	// staging for the host-pointer entry point
+	char *io = nullptr;
+	size_t io_cap = 0;
+
+	// kernel launches issued (graph replays count their kernel nodes)
+	long long launches = 0;
+};
+
+// Record a message on the context and return the status.
+int ctx_fail(simpois_ctx *ctx, int status, const char *fmt, ...);
+
+// Ensure the arena holds at least `bytes`; the previous contents are lost.
+int ctx_arena_reserve(simpois_ctx *ctx, size_t bytes);
+int ctx_pinned_reserve(simpois_ctx *ctx, size_t bytes);
+int ctx_io_reserve(simpois_ctx *ctx, size_t bytes);
+
+#define SP_CUDA(ctx, call)                                                    \
+	do {                                                                  \
+		cudaError_t e_ = (call);                                      \
+		if (e_ != cudaSuccess)                                        \
+			return ctx_fail((ctx), SIMPOIS_ECUDA, "%s: %s (%s:%d)", \
+				#call, cudaGetErrorString(e_), __FILE__,      \
+				__LINE__);                                    \
+	} while (0)
+
+#define SP_LAUNCH_CHECK(ctx) SP_CUDA(ctx, cudaGetLastError())
+
+// Bump allocator laid over the arena: offsets are planned on the host first
+// (Layout::take), then bound to the arena base.
+struct Layout {
+	size_t off = 0;
+	size_t take(size_t bytes, size_t align = 256)
+	{
+		off = (off + align - 1) / align * align;
+		size_t o = off;
+		off += bytes;
+		return o;
+	}
+};
+
+// ---------------------------------------------------------------- device helpers
+
+#define SP_TILE 32          // tiles are 32 x 32 pixels
+#define SP_BLOCK_X 32
+#define SP_BLOCK_Y 8
+#define SP_THREADS (SP_BLOCK_X * SP_BLOCK_Y)
+#define SP_ROWS (SP_TILE / SP_BLOCK_Y)
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+	return v;
+}
+
+// Block sum of `v` over all threads of the block, returned to thread 0.
+// Deterministic: fixed shuffle tree then a fixed order over the warps.
+template <int NT>
+__device__ __forceinline__ double block_sum(double v, double *sh)
+{
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	v = warp_sum(v);
+	if (lane == 0) sh[warp] = v;
+	__syncthreads();
+	double r = 0;
+	if (threadIdx.x == 0) {
+#pragma unroll
+		for (int k = 0; k < NT / 32; k++) r += sh[k];
+	}
+	__syncthreads();
+	return r;
+}
+
+// Clamp-to-edge index (the Neumann extension of simpois.c:25-32).
+__device__ __forceinline__ int clampi(int v, int n) { return v < 0 ? 0 : (v >= n ? n - 1 : v); }

@@ -1,0 +1,171 @@
+/*
+ * simpois_gpu.h -- C ABI of the GB300 (sm_103a) simpois hole-filling solver.
+ *
+ * The library fills the NaN pixels of planar float images by Laplace, Poisson
+ * (with a data term) or biharmonic interpolation.  Two schedules are offered:
+ *
+ *  - the reference schedule (params.rtol == 0): the octave pyramid of
+ *    imscript's `poisson_rec` (simpois.c:247-285) with `niter` colour-ordered
+ *    Gauss-Seidel sweeps per level and the FP64 conjugate-gradient refinement
+ *    `-c` selects (cleant_cgpois.c:197-278, minicg.c:24-56);
+ *  - the converged schedule (params.rtol > 0): a multigrid-preconditioned
+ *    conjugate gradient in FP32 inside an FP64 iterative refinement, run until
+ *    the FP64 relative residual ||b - A u|| / ||b|| of the CG operator
+ *    (5-point -Laplacian for tstep > 0, 13-point bilaplacian for tstep < 0)
+ *    is at most rtol, for every channel of every image independently.
+ *
+ * Images are planar: sample (channel l, row j, column i) of a w x h x pd
+ * image is at x[w*h*l + w*j + i], the layout of iio's *_split functions
+ * (iio.h:42-43).  NaN marks an unknown pixel; every other value is copied to
+ * the output bit for bit.
+ *
+ * Every entry point returns a status code and never exits the process.  Host
+ * buffers are owned by the caller and are not retained after the call
+ * returns.  A context is bound to one device and one stream; calls on one
+ * context must not overlap (one context per host thread).
+ */
+#ifndef SIMPOIS_GPU_H
+#define SIMPOIS_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define SIMPOIS_OK            0
+#define SIMPOIS_EINVAL        1  /* invalid argument                          */
+#define SIMPOIS_ENOMEM        2  /* device or host allocation failed          */
+#define SIMPOIS_NOT_CONVERGED 3  /* rtol not reached within the iteration cap */
+#define SIMPOIS_BREAKDOWN     4  /* Krylov breakdown (p.Ap <= 0 or not finite)*/
+#define SIMPOIS_ECUDA         5  /* CUDA runtime error                        */
+#define SIMPOIS_ENODEV        6  /* no usable CUDA device                     */
+#define SIMPOIS_SINGULAR      7  /* a channel has no known pixel: the system
+                                    is singular; the reference schedule's
+                                    result is returned for it                 */
+
+typedef struct simpois_ctx simpois_ctx;
+
+/* Solver parameters.  The first four are the simpois options -t -n -s -c
+ * (simpois.c:357-360) with the reference's defaults; the next three are the
+ * environment "smart parameters" PMSFAC, PONLIT, CG_EPS (simpois.c:244-245,
+ * cleant_cgpois.c:125).  simpois_default_params() fills the defaults. */
+typedef struct {
+	float  tstep;     /* -t  0.25; > 0 Laplace/Poisson, < 0 biharmonic,
+	                           < -1000 triharmonic (reference schedule only) */
+	int    niter;     /* -n  10;  Gauss-Seidel sweeps per level             */
+	int    scale;     /* -s  99;  maximum number of octaves                  */
+	int    cgit;      /* -c  0;   CG iterations per level, -1 = #unknowns   */
+	double pmsfac;    /* PMSFAC 3: data-term factor per octave               */
+	double ponlit;    /* PONLIT 0: iterate only at the level of this width   */
+	double cg_eps;    /* CG_EPS -1: absolute CG tolerance (< 0 = default)    */
+	double rtol;      /* 0 = reference schedule; > 0 converged schedule      */
+	int    max_iter;  /* converged schedule: cap on PCG iterations per
+	                     channel, summed over refinements (0 = 500)          */
+	int    flags;     /* SIMPOIS_FLAG_* bits                                 */
+} simpois_params;
+
+/* converged schedule: skip the multigrid preconditioner (plain CG) */
+#define SIMPOIS_FLAG_NO_MG       0x1
+/* converged schedule: launch the iterations eagerly, without CUDA graphs */
+#define SIMPOIS_FLAG_NO_GRAPH    0x2
+/* compute rel_residual_out (the FP64 residual of the stored float output) */
+#define SIMPOIS_FLAG_OUT_RESID   0x4
+
+/* Per-channel result record. */
+typedef struct {
+	int    status;           /* SIMPOIS_* code of this channel               */
+	int    unknowns;         /* NaN pixels of this channel                   */
+	int    iterations;       /* PCG iterations (converged schedule) or CG
+	                            iterations at the finest level (reference)   */
+	int    refinements;      /* FP64 refinement steps (converged schedule)   */
+	double rel_residual;     /* FP64 relative residual of the solver state   */
+	double rel_residual_out; /* same, of the float output (FLAG_OUT_RESID)  */
+} simpois_report;
+
+/* One image of a batch: device pointers, planar layout.  dat may be NULL. */
+typedef struct {
+	const float *in;
+	const float *dat;
+	float       *out;
+	int          w, h, pd;
+	float        tstep;   /* per image; overrides params->tstep            */
+	double       rtol;    /* per image; overrides params->rtol when > 0    */
+} simpois_image;
+
+/* Fill *p with the simpois defaults (-t 0.25 -n 10 -s 99 -c 0, PMSFAC 3,
+ * PONLIT 0, CG_EPS -1, rtol 0). */
+void simpois_default_params(simpois_params *p);
+
+/* Read PMSFAC, PONLIT, CG_EPS and SIMPOIS_RTOL from the environment into *p,
+ * the way the reference's smart parameters do (smapa.h:44-60). */
+void simpois_params_from_env(simpois_params *p);
+
+/* Create a context on `device`, issuing work on `stream` (a cudaStream_t,
+ * NULL = the legacy default stream). */
+int simpois_create(simpois_ctx **ctx, int device, void *stream);
+int simpois_destroy(simpois_ctx *ctx);
+
+/* Text for a status code; the last error message recorded on a context. */
+const char *simpois_strerror(int status);
+const char *simpois_last_error(const simpois_ctx *ctx);
+
+/* Solve one planar w x h x pd image held in HOST memory (the work of
+ * poisson_solver_separable, simpois.c:288-302).  dat may be NULL.  reports,
+ * if not NULL, receives pd records.  Returns the worst channel status. */
+int simpois_solve(simpois_ctx *ctx, float *out, const float *in,
+		const float *dat, int w, int h, int pd,
+		const simpois_params *params, simpois_report *reports);
+
+/* Same, with every pointer in DEVICE memory; the call returns when the
+ * output is written (the context's stream is synchronised). */
+int simpois_solve_device(simpois_ctx *ctx, float *out, const float *in,
+		const float *dat, int w, int h, int pd,
+		const simpois_params *params, simpois_report *reports);
+
+/* Solve n images of possibly different sizes in one batched solve (device
+ * pointers).  reports receives sum(pd) records in image order. */
+int simpois_solve_batch(simpois_ctx *ctx, const simpois_image *images, int n,
+		const simpois_params *params, simpois_report *reports);
+
+/* FP64 relative residual of a float output `u` (device pointers) for every
+ * channel: kind 0 = 5-point -Laplacian, 1 = 13-point bilaplacian; unknowns
+ * are the NaN pixels of `in`.  rel and bnorm receive pd values (host). */
+int simpois_residual_device(simpois_ctx *ctx, const float *u, const float *in,
+		const float *dat, int w, int h, int pd, int kind, double *rel,
+		double *bnorm);
+
+/* Adjoint of the converged Laplace/Poisson fill (device pointers).  Given
+ * grad_out = dL/d(out), solves A lambda = grad_out on the unknowns (A is the
+ * symmetric 5-point operator) and writes
+ *   grad_in[k]  = grad_out[k] + sum over unknown 5-neighbours p of lambda[p]
+ *                 at known pixels k, 0 at unknown pixels;
+ *   grad_dat[p] = -lambda[p] at unknown pixels, 0 elsewhere (may be NULL).
+ * params->rtol is the tolerance of the adjoint solve (0 = 1e-6). */
+int simpois_adjoint_device(simpois_ctx *ctx, const float *grad_out,
+		const float *in, int w, int h, int pd, float *grad_in,
+		float *grad_dat, const simpois_params *params,
+		simpois_report *reports);
+
+/* Instrumentation (no counterpart in the reference): the number of kernel
+ * launches this context has issued (a graph replay counts its kernel nodes),
+ * and a reset. */
+long long simpois_launch_count(const simpois_ctx *ctx);
+void simpois_reset_launch_count(simpois_ctx *ctx);
+
+/* Drop-in replacements with the reference's signatures.  They run on device
+ * 0 through a process-wide context and, like the reference, return nothing;
+ * a failure is printed to stderr and leaves `out` holding the input.
+ *   poisson_solver_separable   simpois.c:288-290
+ *   poisson_rec                simpois.c:247-248 (one channel)
+ * The smart parameters PMSFAC, PONLIT, CG_EPS and SIMPOIS_RTOL are read from
+ * the environment once, as in the reference. */
+void poisson_solver_separable(float *out, float *in, float *dat, int w, int h,
+		int pd, float tstep, int niter, int scale, float cgrad);
+void poisson_rec(float *u, float *g, float *f, int w, int h, float tstep,
+		int niter, int scale, int cgit);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SIMPOIS_GPU_H */

@@ -131,13 +131,96 @@ def conv_cases(rng):
     return k
 
 
+def cli_cases():
+    """Texts and exit codes of the reference command (no image work)."""
+    import subprocess
+    import tempfile
+    res = {}
+    for a in (["-h"], ["--help"], ["--version"], ["-?"]):
+        r = subprocess.run([O.REF_BIN] + a, capture_output=True, text=True)
+        res[" ".join(a)] = {"stdout": r.stdout, "stderr": r.stderr, "rc": r.returncode}
+    r = subprocess.run([O.REF_BIN, "-n", "3", "stray"], capture_output=True, text=True)
+    res["stray"] = {"stdout": r.stdout, "stderr": r.stderr.replace(O.REF_BIN, "ARGV0"),
+                    "rc": r.returncode}
+    with tempfile.TemporaryDirectory() as td:
+        a = os.path.join(td, "a.npy")
+        b = os.path.join(td, "b.npy")
+        np.save(a, np.zeros((4, 5, 1), np.float32))
+        np.save(b, np.zeros((4, 6, 1), np.float32))
+        r = subprocess.run([O.REF_BIN, "-i", a, "-f", b, "-o", os.path.join(td, "o.npy")],
+                           capture_output=True, text=True)
+        res["mismatch_if"] = {"stdout": r.stdout, "stderr": r.stderr, "rc": r.returncode}
+        r = subprocess.run([O.REF_BIN, "-i", a, "-m", b, "-o", os.path.join(td, "o.npy")],
+                           capture_output=True, text=True)
+        res["mismatch_im"] = {"stdout": r.stdout, "stderr": r.stderr, "rc": r.returncode}
+    with open(os.path.join(OUT, "cli.json"), "w") as fh:
+        json.dump(res, fh, indent=1)
+    return len(res)
+
+
+def io_cases():
+    """How the reference reads and writes each format: an all-known image
+    (nothing to fill) read from format X and written as npy, and read from
+    npy and written as format Y."""
+    import subprocess
+    import tempfile
+    rng = np.random.default_rng(77)
+    res = {}
+    img3 = (rng.random((5, 7, 3)) * 200).astype(np.float32)
+    img1 = (rng.random((6, 4, 1)) * 200).astype(np.float32)
+    with tempfile.TemporaryDirectory() as td:
+        for tag, img in (("c3", img3), ("c1", img1)):
+            src = os.path.join(td, f"{tag}.npy")
+            np.save(src, img)
+            for ext in ("npy", "pfm", "ppm", "pgm", "asc", "tif", "txt"):
+                dst = os.path.join(td, f"{tag}_out.{ext}")
+                subprocess.run([O.REF_BIN, "-i", src, "-o", dst], check=True)
+                res[f"write_{tag}_{ext}"] = list(open(dst, "rb").read())
+        # readers: npy dtypes, 2-D npy, pnm (ascii, binary), asc
+        cases = {}
+        cases["u8_hw"] = np.arange(20, dtype=np.uint8).reshape(4, 5)
+        cases["i16_hwc"] = (np.arange(24, dtype=np.int16) - 7).reshape(2, 4, 3)
+        cases["f8_hwc"] = rng.standard_normal((3, 2, 2))
+        cases["u2_hw"] = (np.arange(6, dtype=np.uint16) * 1000).reshape(2, 3)
+        for k, a in cases.items():
+            p = os.path.join(td, k + ".npy")
+            np.save(p, a)
+            o = os.path.join(td, k + "_o.npy")
+            subprocess.run([O.REF_BIN, "-i", p, "-o", o], check=True)
+            res[f"read_{k}"] = {"in": list(open(p, "rb").read()), "out": list(open(o, "rb").read())}
+        texts = {"p2": b"P2\n3 2\n255\n0 1 2\n3 4 255\n", "p5": b"P5\n2 2\n255\n\x00\x10\x20\xff",
+                 "p6": b"P6\n1 2\n255\n\x01\x02\x03\x04\x05\x06"}
+        for k, t in texts.items():
+            p = os.path.join(td, k)
+            open(p, "wb").write(t)
+            o = os.path.join(td, k + "_o.npy")
+            subprocess.run([O.REF_BIN, "-i", p, "-o", o], check=True)
+            res[f"read_{k}"] = {"in": list(t), "out": list(open(o, "rb").read())}
+        # mask: RGB uint8 ppm turned gray by the reference's weights
+        img = synth.gaussian_field(rng, 4, 6, 2)[None]
+        np.save(os.path.join(td, "g.npy"), O.to_hwc(img))
+        mk = b"P6\n6 4\n255\n" + bytes(rng.integers(0, 2, 72, dtype=np.uint8).tolist())
+        open(os.path.join(td, "m.ppm"), "wb").write(mk)
+        o = os.path.join(td, "gm.npy")
+        subprocess.run([O.REF_BIN, "-i", os.path.join(td, "g.npy"), "-m", os.path.join(td, "m.ppm"),
+                        "-n", "0", "-o", o], check=True)
+        res["mask_rgb"] = {"g": O.to_hwc(img).ravel().tolist(), "mask": list(mk),
+                           "out": list(open(o, "rb").read())}
+    with open(os.path.join(OUT, "io.json"), "w") as fh:
+        json.dump(res, fh)
+    return len(res)
+
+
 def main():
     if not O.have_reference():
         O.build(reference=True)
     rng = np.random.default_rng(20261203)
     n1 = pin_cases(rng)
     n2 = conv_cases(rng)
-    print(f"wrote {n1} pin cases and {n2} converged cases into {OUT}")
+    n3 = cli_cases()
+    n4 = io_cases()
+    print(f"wrote {n1} pin cases, {n2} converged cases, {n3} CLI cases and {n4} I/O cases "
+          f"into {OUT}")
 
 
 if __name__ == "__main__":

@@ -1,0 +1,195 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle.
+
+* reference schedule: bit-exact against the oracle's colour-ordered
+  restatement (same float operations, same sweep classes), within 1e-5 where
+  the FP64 CG runs (its dot products are summed in another order);
+* converged schedule: within 1e-4 relative max-abs of the reference's own
+  converged output (golden fixtures) and of the FP64 direct solve, FP64
+  relative residual <= rtol, known pixels bit-exact.
+"""
+import numpy as np
+import pytest
+
+from golden_cases import cases, load, parse_args
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def sp():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from imscript_gb300 import simpois
+    return simpois
+
+
+def _bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+def _cuda(a):
+    return torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda()
+
+
+def _run_ref_schedule(sp, g, f, kw, device):
+    kw = dict(kw)
+    opts = dict(tstep=kw.pop("tstep"), niter=kw.pop("niter"), scale=kw.pop("scale"),
+                cgrad=kw.pop("cgrad"), pmsfac=kw.pop("pmsfac"), ponlit=kw.pop("ponlit"),
+                cg_eps=kw.pop("cg_eps"))
+    allow = (0, 4)
+    if device:
+        out, reps = sp.poisson_solver_separable(_cuda(g), None if f is None else _cuda(f), **opts,
+                                                allow=allow)
+        return out.cpu().numpy(), reps
+    return sp.poisson_solver_separable(g, f, **opts, allow=allow)
+
+
+@pytest.mark.parametrize("path", cases("pin_"), ids=lambda p: p.rsplit("/", 1)[-1][:-4])
+def test_reference_schedule_matches_colour_oracle(sp, oracle_mod, path):
+    d = load(path)
+    kw = parse_args(d["args"], d["env"])
+    g = d["g"]
+    if d["mask"] is not None:
+        g = oracle_mod.apply_mask(g, d["mask"])
+    want = oracle_mod.poisson_solver_separable(g, d["f"], order="colour", **kw)
+    got, reps = _run_ref_schedule(sp, g, d["f"], kw, device=True)
+    if kw["cgrad"] == 0 or int(kw["cgrad"]) < -1:
+        assert np.array_equal(_bits(got), _bits(want)), "GS/pyramid path must be bit-exact"
+    else:
+        fin = np.isfinite(want)
+        scale = max(1.0, float(np.abs(want[fin]).max())) if fin.any() else 1.0
+        assert np.array_equal(fin, np.isfinite(got))
+        assert np.array_equal(_bits(got[~fin]), _bits(want[~fin]))
+        assert np.allclose(got[fin], want[fin], rtol=0, atol=1e-5 * scale)
+        known = ~np.isnan(g)
+        assert np.array_equal(_bits(got[known]), _bits(g[known]))
+
+
+def test_reference_schedule_host_entry_equals_device_entry(sp, oracle_mod):
+    rng = np.random.default_rng(7)
+    g = rng.standard_normal((2, 45, 61)).astype(np.float32)
+    g[:, rng.random((45, 61)) < 0.3] = np.nan
+    kw = parse_args(["-n", "17"], {})
+    a, _ = _run_ref_schedule(sp, g, None, kw, device=False)
+    b, _ = _run_ref_schedule(sp, g, None, kw, device=True)
+    assert np.array_equal(_bits(a), _bits(b))
+    want = oracle_mod.poisson_solver_separable(g, None, order="colour", **kw)
+    assert np.array_equal(_bits(a), _bits(want))
+
+
+@pytest.mark.parametrize("path", cases("conv_"), ids=lambda p: p.rsplit("/", 1)[-1][:-4])
+def test_converged_matches_reference_converged(sp, oracle_mod, path):
+    from oracle import fp64
+    d = load(path)
+    kind = d["extra"]["kind"]
+    g, f, ref = d["g"], d["f"], d["out"]
+    tstep = -0.08 if kind else 0.25
+    out, reps = sp.poisson_solver_separable(_cuda(g), None if f is None else _cuda(f), tstep,
+                                            rtol=1e-6)
+    out = out.cpu().numpy()
+    unk = np.isnan(g)
+    assert np.array_equal(_bits(out[~unk]), _bits(g[~unk])), "known pixels must be bit-exact"
+    r = reps[0]
+    assert r["status"] == 0 and r["rel_residual"] <= 1e-6
+    scale = np.abs(ref[unk]).max()
+    assert np.abs(out[unk] - ref[unk]).max() <= 1e-4 * scale
+    x = fp64.solve(g[0], None if f is None else f[0], kind)
+    assert np.abs(out[0][unk[0]] - x[unk[0]]).max() <= 1e-4 * np.abs(x[unk[0]]).max()
+    rel = oracle_mod.rel_residual(out, g, f, kind)[0][0]
+    assert rel < 2e-6, "FP32 output stays near the storage floor"
+
+
+def _random_case(rng, h, w, frac, rmax, with_f, kind):
+    from imscript_gb300 import synth
+    img = synth.gaussian_field(rng, h, w, 8)
+    m = synth.disk_mask(rng, h, w, frac, rmin=1.5, rmax=rmax)
+    img[m] = np.nan
+    f = None
+    if with_f:
+        f = synth.guidance(synth.gaussian_field(rng, h, w, 8))[2][None]
+    return img[None], f
+
+
+@pytest.mark.parametrize("kind,h,w,frac,rmax,with_f", [
+    (0, 96, 128, 0.3, 14, False), (0, 130, 77, 0.5, 20, True), (0, 33, 300, 0.2, 9, True),
+    (0, 1, 200, 0.4, 3, False), (0, 200, 1, 0.4, 3, True), (0, 7, 5, 0.5, 2, False),
+    (1, 64, 80, 0.15, 6, False), (1, 71, 53, 0.2, 5, True),
+])
+def test_converged_random_vs_fp64(sp, oracle_mod, kind, h, w, frac, rmax, with_f):
+    from oracle import fp64
+    rng = np.random.default_rng(h * 1000 + w + kind)
+    g, f = _random_case(rng, h, w, frac, rmax, with_f, kind)
+    if not np.isnan(g).any() or np.isnan(g).all():
+        pytest.skip("degenerate draw")
+    tstep = -0.08 if kind else 0.25
+    out, reps = sp.poisson_solver_separable(_cuda(g), None if f is None else _cuda(f), tstep,
+                                            rtol=1e-6, flags=4)
+    out = out.cpu().numpy()
+    r = reps[0]
+    assert r["status"] == 0, r
+    assert r["rel_residual"] <= 1e-6
+    unk = np.isnan(g[0])
+    x = fp64.solve(g[0], None if f is None else f[0], kind)
+    err = np.abs(out[0][unk] - x[unk]).max() / max(np.abs(x[unk]).max(), 1e-30)
+    assert err <= 1e-4
+    rel_cpu = oracle_mod.rel_residual(out, g, f, kind)[0][0]
+    assert abs(rel_cpu - r["rel_residual_out"]) <= 1e-3 * rel_cpu + 1e-12
+
+
+def test_batched_equals_plain_bit_exact(sp):
+    """Each problem of a batch computes exactly what it computes alone."""
+    from imscript_gb300 import synth
+    insts = synth.config3(seed=5, n=6, smin=40, smax=150)
+    imgs = [(_cuda(i.g), None if i.f is None else _cuda(i.f)) for i in insts]
+    outs, reps = sp.solve_batch(imgs, rtol=1e-6)
+    k = 0
+    for (g, f), o in zip(imgs, outs):
+        solo, r1 = sp.solve(g, f, rtol=1e-6)
+        assert torch.equal(o.view(torch.int32), solo.view(torch.int32))
+        for rr in r1:
+            assert reps[k]["iterations"] == rr["iterations"]
+            assert reps[k]["rel_residual"] <= 1e-6
+            k += 1
+
+
+def test_all_known_and_all_unknown(sp, oracle_mod):
+    rng = np.random.default_rng(1)
+    g = rng.standard_normal((1, 20, 30)).astype(np.float32)
+    out, reps = sp.poisson_solver_separable(_cuda(g), rtol=1e-6)
+    assert np.array_equal(_bits(out.cpu().numpy()), _bits(g))
+    assert reps[0]["unknowns"] == 0 and reps[0]["rel_residual"] == 0
+    # no known pixel: singular; the reference schedule's answer is returned
+    gn = np.full((1, 12, 9), np.nan, np.float32)
+    f = (rng.standard_normal(gn.shape) * 0.1).astype(np.float32)
+    out, reps = sp.poisson_solver_separable(_cuda(gn), _cuda(f), rtol=1e-6)
+    assert reps[0]["status"] == 7
+    want = oracle_mod.poisson_solver_separable(gn, f, order="colour")
+    assert np.array_equal(_bits(out.cpu().numpy()), _bits(want))
+
+
+def test_residual_entry_matches_oracle(sp, oracle_mod):
+    rng = np.random.default_rng(3)
+    g, f = _random_case(rng, 60, 70, 0.3, 8, True, 0)
+    u = np.where(np.isnan(g), rng.standard_normal(g.shape).astype(np.float32), g)
+    for kind in (0, 1):
+        rel, bn = sp.residual(_cuda(u), _cuda(g), _cuda(f), kind)
+        want, wbn = oracle_mod.rel_residual(u, g, f, kind)
+        assert abs(rel[0] - want[0]) <= 1e-9 * want[0]
+        assert abs(bn[0] - wbn[0]) <= 1e-9 * wbn[0]
+
+
+def test_dropin_symbol_matches_oracle(sp, oracle_mod):
+    """poisson_solver_separable with the reference's exact signature."""
+    import ctypes
+    from imscript_gb300 import lib
+    L = lib.load()
+    rng = np.random.default_rng(9)
+    g = rng.standard_normal((3, 23, 31)).astype(np.float32)
+    g[:, rng.random((23, 31)) < 0.35] = np.nan
+    out = np.zeros_like(g)
+    L.poisson_solver_separable(out.ctypes.data, g.ctypes.data, None, 31, 23, 3,
+                               ctypes.c_float(0.25), 25, 99, ctypes.c_float(0))
+    want = oracle_mod.poisson_solver_separable(g, None, niter=25, order="colour")
+    assert np.array_equal(_bits(out), _bits(want))
