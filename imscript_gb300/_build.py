@@ -21,7 +21,7 @@ INCLUDE = os.path.join(ROOT, "include")
 LIB = os.path.join(OUT, "libsimpois_gpu.so")
 CLI_BIN = os.path.join(OUT, "simpois")
 
-CU_SOURCES = ["abi.cu", "ref_schedule.cu", "mg_solver.cu"]
+CU_SOURCES = ["abi.cu", "ref_schedule.cu", "mg_solver.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr"]
 

@@ -65,7 +65,8 @@ class Image(ctypes.Structure):
 EXPORTS = [
     "simpois_default_params", "simpois_params_from_env", "simpois_create", "simpois_destroy",
     "simpois_strerror", "simpois_last_error", "simpois_solve", "simpois_solve_device",
-    "simpois_solve_batch", "simpois_residual_device", "simpois_adjoint_device",
+    "simpois_solve_batch", "simpois_residual_device", "simpois_residual_device_noalloc",
+    "simpois_adjoint_device",
     "simpois_launch_count", "simpois_reset_launch_count",
     "poisson_solver_separable", "poisson_rec",
 ]
@@ -110,6 +111,7 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
         L.simpois_residual_device.argtypes = [vp, vp, vp, vp, ip, ip, ip, ip,
                                               ctypes.POINTER(ctypes.c_double),
                                               ctypes.POINTER(ctypes.c_double)]
+        L.simpois_residual_device_noalloc.argtypes = L.simpois_residual_device.argtypes
         L.simpois_adjoint_device.argtypes = [vp, vp, vp, ip, ip, ip, vp, vp, P, R]
         L.simpois_launch_count.argtypes = [vp]
         L.simpois_launch_count.restype = ctypes.c_longlong

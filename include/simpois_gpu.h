@@ -134,6 +134,19 @@ int simpois_residual_device(simpois_ctx *ctx, const float *u, const float *in,
 		const float *dat, int w, int h, int pd, int kind, double *rel,
 		double *bnorm);
 
+/* simpois_residual_device without any memory allocation (no counterpart in
+ * the reference).  For callers that may not allocate device memory where
+ * they check a result -- a device budget fully reserved up front, a path that
+ * must not enter an allocator.  Its scratch is a fixed 1 MiB + 4 KiB array
+ * inside the library (held on each GPU that loads the library until exit);
+ * at most 16,777,216 pixels per channel and 64 channels, else SIMPOIS_EINVAL.
+ * The first call on a device looks up the array's device address: make it
+ * before any stream capture on that device.  All calls share the array, so
+ * calls that overlap on the GPU race: serialise them. */
+int simpois_residual_device_noalloc(simpois_ctx *ctx, const float *u,
+		const float *in, const float *dat, int w, int h, int pd, int kind,
+		double *rel, double *bnorm);
+
 /* Adjoint of the converged Laplace/Poisson fill (device pointers).  Given
  * grad_out = dL/d(out), solves A lambda = grad_out on the unknowns (A is the
  * symmetric 5-point operator) and writes
