@@ -1,0 +1,142 @@
+"""The simpois command: texts, argument handling, exit codes and image I/O
+against the reference command's own behaviour (fixtures from the reference
+binary, tests/golden/cli.json and io.json); end-to-end solves on the GPU."""
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+@pytest.fixture(scope="module")
+def cli():
+    from imscript_gb300 import _build
+    _build.build()
+    return _build.CLI_BIN
+
+
+@pytest.fixture(scope="module")
+def harness(tmp_path_factory):
+    out = str(tmp_path_factory.mktemp("h") / "imageio_harness")
+    cli_dir = os.path.join(ROOT, "imscript_gb300", "cli")
+    subprocess.run(["gcc", "-O1", "-std=gnu99", "-I", cli_dir, os.path.join(ROOT, "tests", "imageio_harness.c"),
+                    os.path.join(cli_dir, "imageio.c"), "-o", out, "-lm"], check=True)
+    return out
+
+
+def _fixtures(name):
+    with open(os.path.join(GOLDEN, name)) as fh:
+        return json.load(fh)
+
+
+@pytest.mark.parametrize("arg", ["-h", "--help", "--version", "-?"])
+def test_help_texts(cli, arg):
+    want = _fixtures("cli.json")[arg]
+    r = subprocess.run([cli, arg], capture_output=True, text=True)
+    assert (r.stdout, r.stderr, r.returncode) == (want["stdout"], want["stderr"], want["rc"])
+
+
+def test_stray_argument_prints_usage_and_fails(cli):
+    want = _fixtures("cli.json")["stray"]
+    r = subprocess.run([cli, "-n", "3", "stray"], capture_output=True, text=True)
+    assert r.returncode == want["rc"] == 1
+    assert r.stderr.replace(cli, "ARGV0") == want["stderr"]
+
+
+@pytest.mark.parametrize("which,flag", [("mismatch_if", "-f"), ("mismatch_im", "-m")])
+def test_size_mismatch_exit_codes(cli, tmp_path, which, flag):
+    want = _fixtures("cli.json")[which]
+    a, b = str(tmp_path / "a.npy"), str(tmp_path / "b.npy")
+    np.save(a, np.zeros((4, 5, 1), np.float32))
+    np.save(b, np.zeros((4, 6, 1), np.float32))
+    r = subprocess.run([cli, "-i", a, flag, b, "-o", str(tmp_path / "o.npy")], capture_output=True,
+                       text=True)
+    assert (r.stderr, r.returncode) == (want["stderr"], want["rc"])
+
+
+IO = None
+
+
+def _io():
+    global IO
+    if IO is None:
+        IO = _fixtures("io.json")
+    return IO
+
+
+@pytest.mark.parametrize("tag", ["c3", "c1"])
+@pytest.mark.parametrize("ext", ["npy", "pfm", "ppm", "pgm", "asc", "tif", "txt"])
+def test_writers_match_reference_bytes(harness, tmp_path, tag, ext):
+    rng = np.random.default_rng(77)
+    img3 = (rng.random((5, 7, 3)) * 200).astype(np.float32)
+    img1 = (rng.random((6, 4, 1)) * 200).astype(np.float32)
+    src = str(tmp_path / "src.npy")
+    np.save(src, img3 if tag == "c3" else img1)
+    dst = str(tmp_path / f"out.{ext}")
+    subprocess.run([harness, "write", src, dst], check=True)
+    assert list(open(dst, "rb").read()) == _io()[f"write_{tag}_{ext}"]
+
+
+@pytest.mark.parametrize("key", ["u8_hw", "i16_hwc", "f8_hwc", "u2_hw", "p2", "p5", "p6"])
+def test_readers_match_reference(harness, tmp_path, key):
+    d = _io()[f"read_{key}"]
+    src = str(tmp_path / ("in.npy" if "_" in key else key))
+    open(src, "wb").write(bytes(d["in"]))
+    dst = str(tmp_path / "o.npy")
+    subprocess.run([harness, "read", src, dst], check=True)
+    assert list(open(dst, "rb").read()) == d["out"]
+
+
+def test_gray_mask_conversion_matches_reference(harness, tmp_path):
+    d = _io()["mask_rgb"]
+    mp = str(tmp_path / "m.ppm")
+    open(mp, "wb").write(bytes(d["mask"]))
+    dst = str(tmp_path / "m.npy")
+    subprocess.run([harness, "gray", mp, dst], check=True)
+    gray = np.load(dst)[..., 0]
+    g = np.array(d["g"], np.float32).reshape(gray.shape)
+    ref = np.frombuffer(bytes(d["out"]), np.uint8)
+    out = np.load(dst.replace("m.npy", "m.npy"))
+    want = np.where(gray > 0, np.nan, g)
+    # the reference (-n 0) filled nothing: NaN where the gray mask is > 0
+    import io
+    refimg = np.load(io.BytesIO(bytes(d["out"])))[..., 0]
+    assert np.array_equal(np.isnan(refimg), np.isnan(want))
+    assert ref.size > 0 and out.size > 0
+
+
+@pytest.mark.gpu
+def test_cli_end_to_end_matches_oracle(cli, tmp_path, oracle_mod):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    rng = np.random.default_rng(5)
+    g = rng.standard_normal((2, 40, 52)).astype(np.float32)
+    g[:, rng.random((40, 52)) < 0.3] = np.nan
+    f = (rng.standard_normal(g.shape) * 0.1).astype(np.float32)
+    pi, pf, po = str(tmp_path / "i.npy"), str(tmp_path / "f.npy"), str(tmp_path / "o.npy")
+    np.save(pi, oracle_mod.to_hwc(g))
+    np.save(pf, oracle_mod.to_hwc(f))
+    env = {k: v for k, v in os.environ.items() if k not in ("PMSFAC", "PONLIT", "CG_EPS", "SIMPOIS_RTOL")}
+    subprocess.run([cli, "-i", pi, "-f", pf, "-n", "12", "-o", po], check=True, env=env)
+    got = oracle_mod.from_hwc(np.load(po))
+    want = oracle_mod.poisson_solver_separable(g, f, niter=12, order="colour")
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    # stdin -> stdout, mask file, converged schedule through SIMPOIS_RTOL
+    pm = str(tmp_path / "m.npy")
+    m = (rng.random((40, 52)) < 0.2).astype(np.float32)
+    np.save(pm, m)
+    env2 = dict(env, SIMPOIS_RTOL="1e-6")
+    r = subprocess.run([cli, "-m", pm], input=open(pi, "rb").read(), capture_output=True, env=env2,
+                       check=True)
+    import io
+    out = oracle_mod.from_hwc(np.load(io.BytesIO(r.stdout)))
+    gm = oracle_mod.apply_mask(g, m)
+    rel, _ = oracle_mod.rel_residual(out, gm, None, 0)
+    assert np.all(rel < 2e-6)
+    known = ~np.isnan(gm)
+    assert np.array_equal(out[known].view(np.uint32), gm[known].view(np.uint32))
