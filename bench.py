@@ -116,6 +116,9 @@ def make_workload(name, rank):
         return synth.config3(seed=seed), "batched-256-uneven (64..1024 px, 5-60% holes)"
     if name == "c2":
         return [synth.config2(seed=seed)], "biharmonic-4096x4096x1 (1024^2 square + 200 scratches)"
+    if name == "c2s":  # reduced size, for quick checks
+        return [synth.config2(seed=seed, size=1024, hole=256, n_scratch=50)], \
+            "biharmonic-1024x1024x1 (256^2 square + 50 scratches)"
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -252,6 +255,41 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = unknowns * world * args.steps / (ms / 1e3) / 1e6
+    if args.quick:
+        if rank == 0:
+            print(json.dumps({"value": value, "ms_per_step": ms / args.steps, "gpu_launches": launches,
+                              "iterations": [r["iterations"] for r in reps], "max_rel": worst}))
+        return
+
+    # kernel roofline: one more step of the same workload on the same stream,
+    # launches issued eagerly with a CUDA-event pair around each main-loop
+    # kernel; achieved = algorithmic bytes / event-timed duration
+    ctx.reset_kernel_stats()
+    flush.fill_(0.0)
+    if len(insts) == 1:
+        simpois.solve(gs[0], fs[0], tstep=insts[0].tstep, rtol=rtol, out=outs[0], flags=splib.FLAG_KTIMER)
+    else:
+        simpois.solve_batch(list(zip(gs, fs, [i.tstep for i in insts])), rtol=rtol, outs=outs,
+                            flags=splib.FLAG_KTIMER)
+    torch.cuda.synchronize()
+    kstats = ctx.kernel_stats()
+    peaks, peak_src = measured_peaks()
+    hbm = float(peaks.get("hbm_gbs", HBM_FALLBACK))
+    kernels = {}
+    for name, k in kstats.items():
+        gbs = k["bytes"] / (k["ms"] * 1e-3) / 1e9 if k["ms"] > 0 else 0.0
+        kernels[name] = {"launches": k["launches"], "ms_total": round(k["ms"], 4),
+                         "avg_us": round(1e3 * k["ms"] / max(1, k["launches"]), 2),
+                         "bytes_per_launch": k["bytes"] / max(1, k["launches"]),
+                         "achieved_gbs": round(gbs, 1)}
+    roofline = None
+    if kernels:
+        dom = max(kernels, key=lambda n: kernels[n]["ms_total"])
+        d = kernels[dom]
+        roofline = {"kernel": dom, "bound": "hbm", "achieved": d["achieved_gbs"], "peak": hbm, "unit": "GB/s",
+                    "frac": round(d["achieved_gbs"] / hbm, 4), "traffic": None,
+                    "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
+                    else "fallback 6.8 TB/s"}
 
     # plain: one channel per call
     for _ in range(max(1, args.warmup // 2)):
@@ -282,7 +320,7 @@ def run_ours(args):
         if world > 1:
             dist.destroy_process_group()
         return
-    peaks, src = measured_peaks()
+    src = peak_src
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         cpu = cpu_baseline(insts)
@@ -310,7 +348,8 @@ def run_ours(args):
         "clocks": clocks.summary(),
         "solver": {"max_rel_residual": worst, "iterations": [r["iterations"] for r in reps],
                    "refinements": [r["refinements"] for r in reps], "not_ok": len(bad)},
-        "roofline": None,
+        "roofline": roofline,
+        "kernels": kernels,
         "cpu_baseline": cpu,
         "peaks_source": src,
     }
@@ -360,6 +399,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="c1")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quick", action="store_true",
+                    help="batched solves only, short JSON (for profiling runs)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -161,6 +161,8 @@ int run_converged(simpois_ctx *ctx, const simpois_image *im, int n, const simpoi
 	opt.use_mg = !(p->flags & SIMPOIS_FLAG_NO_MG);
 	opt.use_graph = !(p->flags & SIMPOIS_FLAG_NO_GRAPH);
 	opt.out_resid = (p->flags & SIMPOIS_FLAG_OUT_RESID) != 0;
+	opt.fused = !(p->flags & SIMPOIS_FLAG_UNFUSED);
+	opt.ktimer = (p->flags & SIMPOIS_FLAG_KTIMER) != 0;
 	int rc = SIMPOIS_OK;
 	// one batched solve per operator kind
 	for (int kind = 0; kind < 2; kind++) {
@@ -286,6 +288,8 @@ int simpois_destroy(simpois_ctx *ctx)
 	if (ctx->io) cudaFree(ctx->io);
 	if (ctx->pinned) cudaFreeHost(ctx->pinned);
 	if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
+	for (cudaEvent_t e : ctx->evpool) cudaEventDestroy(e);
+	if (ctx->solve_exec) cudaGraphExecDestroy(ctx->solve_exec);
 	delete ctx;
 	return SIMPOIS_OK;
 }
@@ -449,6 +453,7 @@ int simpois_adjoint_device(simpois_ctx *ctx, const float *grad_out, const float 
 	opt.max_iter = p.max_iter > 0 ? p.max_iter : 500;
 	opt.use_mg = !(p.flags & SIMPOIS_FLAG_NO_MG);
 	opt.use_graph = !(p.flags & SIMPOIS_FLAG_NO_GRAPH);
+	opt.fused = !(p.flags & SIMPOIS_FLAG_UNFUSED);
 	opt.mode = MG_ADJOINT;
 	opt.grad_out = go.data();
 	opt.grad_in = gi.data();
@@ -465,6 +470,27 @@ int simpois_adjoint_device(simpois_ctx *ctx, const float *grad_out, const float 
 }
 
 long long simpois_launch_count(const simpois_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+const char *simpois_kernel_stats(simpois_ctx *ctx)
+{
+	if (!ctx) return "{}";
+	std::string j = "{";
+	char buf[256];
+	for (size_t k = 0; k < ctx->kstats.size(); k++) {
+		const auto &st = ctx->kstats[k];
+		snprintf(buf, sizeof buf, "%s\"%s\": {\"launches\": %lld, \"ms\": %.6f, \"bytes\": %.0f}",
+				k ? ", " : "", st.name.c_str(), st.launches, st.ms, st.bytes);
+		j += buf;
+	}
+	j += "}";
+	ctx->kstats_json = j;
+	return ctx->kstats_json.c_str();
+}
+
+void simpois_reset_kernel_stats(simpois_ctx *ctx)
+{
+	if (ctx) ctx->kstats.clear();
+}
 
 void simpois_reset_launch_count(simpois_ctx *ctx)
 {

@@ -37,6 +37,22 @@ struct simpois_ctx {
 
 	// kernel launches issued (graph replays count their kernel nodes)
 	long long launches = 0;
+
+	// kernel timer (SIMPOIS_FLAG_KTIMER): per-kernel launches, CUDA-event
+	// milliseconds and algorithmic bytes, accumulated across solves
+	struct KStat {
+		std::string name;
+		long long launches;
+		double ms, bytes;
+	};
+	std::vector<KStat> kstats;
+	std::vector<cudaEvent_t> evpool;
+	std::string kstats_json;
+
+	// the last device-driven solve graph and the plan it was built for
+	cudaGraphExec_t solve_exec = nullptr;
+	std::string solve_sig;
+	long long solve_nodes_outer = 0, solve_nodes_inner = 0, solve_nodes_top = 0;
 };
 
 // Record a message on the context and return the status.

@@ -56,17 +56,23 @@ struct LevelDev {
 	int w, h;
 	uint8_t *mask;   // 1 = unknown
 	float *b;        // right-hand side (level 0: the PCG residual r)
-	float *z;        // correction (level 0: the preconditioned residual)
+	float *z;        // correction (level 0: the preconditioned residual);
+	                 // fused path: the pre-smoothed correction
+	float *z2;       // fused path: the correction after the coarse
+	                 // correction and post-smoothing (level 0: the PCG z)
 };
 
 struct ProbDev {
 	int nlev, kind, w, h;
+	int nfine;           // fused path: levels below this one use the tile
+	                     // kernels; levels nfine.. are solved by k_coarse5
 	const float *g;      // input channel
 	const float *rhs;    // fill: f (sign -1) ; adjoint: grad_out (sign +1)
 	float rhs_sign;
 	float *out;
 	double *U;           // FP64 solution image (g or 0 at the known pixels)
 	float *x, *p, *q;    // level-0 PCG vectors
+	float *p2;           // fused path: second search-direction buffer
 	double rtol;
 	LevelDev lv[MAXLEV];
 };
@@ -80,8 +86,13 @@ struct ProbState {
 };
 
 struct Globals {
-	int inner_count;   // problems whose inner solve is running
-	int pad[31];
+	int inner_count;    // problems whose inner solve is running
+	int outer_count;    // problems whose refinement is running
+	int guard_inner;    // inner-loop bodies run since the loop started
+	int guard_outer;    // refinement bodies run
+	int n_inner;        // inner-loop bodies run in total (launch accounting)
+	int n_outer;        // refinement bodies run in total
+	int pad[26];
 };
 
 // ------------------------------------------------------------------ stencils
@@ -89,6 +100,17 @@ struct Globals {
 __constant__ int8_t c_di13[12] = {1, 0, -1, 0, 1, 1, -1, -1, 2, 0, -2, 0};
 __constant__ int8_t c_dj13[12] = {0, 1, 0, -1, 1, -1, 1, -1, 0, 2, 0, -2};
 __constant__ float c_cf13[12] = {-8, -8, -8, -8, 2, 2, 2, 2, 1, 1, 1, 1};
+
+// num / diag for a Gauss-Seidel update.  The 5-point diagonals 4, 2 and 1 are
+// powers of two: multiplying by their reciprocal is exact and gives the same
+// float as the division, at a fraction of the instructions.
+__device__ __forceinline__ float gs_div(float num, float diag)
+{
+	if (diag == 4.f) return num * 0.25f;
+	if (diag == 2.f) return num * 0.5f;
+	if (diag == 1.f) return num;
+	return num / diag;
+}
 
 // Split the masked operator at unknown (i, j) of a level into its diagonal
 // (coefficients of the stencil points that clamp onto the pixel itself) and
@@ -176,6 +198,33 @@ __device__ bool problem_sum2(double v0, double v1, int prob, const int *__restri
 	if (threadIdx.x == 0) {
 		tot[0] = a0;
 		tot[1] = a1;
+		st[prob].cnt = 0;
+	}
+	return true;
+}
+
+// problem_sum2 for a single value (one block reduction instead of two).
+__device__ bool problem_sum1(double v0, int prob, const int *__restrict__ tbeg, const int *__restrict__ tcnt,
+		double *partial, ProbState *st, double *tot, double *sh)
+{
+	__shared__ bool am_last;
+	double s0 = block_sum<SP_THREADS>(v0, sh);
+	if (threadIdx.x == 0) {
+		partial[2 * blockIdx.x] = s0;
+		__threadfence();
+		unsigned prev = atomicAdd(&st[prob].cnt, 1u);
+		am_last = prev == (unsigned)tcnt[prob] - 1;
+	}
+	__syncthreads();
+	if (!am_last) return false;
+	__threadfence();
+	double a0 = 0;
+	const int b0 = tbeg[prob], n = tcnt[prob];
+	for (int k = threadIdx.x; k < n; k += SP_THREADS) a0 += __ldcg(partial + 2 * (b0 + k));
+	a0 = block_sum<SP_THREADS>(a0, sh);
+	if (threadIdx.x == 0) {
+		tot[0] = a0;
+		tot[1] = 0;
 		st[prob].cnt = 0;
 	}
 	return true;
@@ -301,12 +350,15 @@ __global__ void k_compact(const int4 *const *__restrict__ all, const int *const 
 template <int K>
 __global__ void k_resid64(const ProbDev *__restrict__ P, ProbState *st, const int4 *__restrict__ tl,
 		const int *__restrict__ tbeg, const int *__restrict__ tcnt, double *partial,
-		Globals *gl, int first)
+		Globals *gl)
 {
 	__shared__ double sh[32];
 	int4 t = tl[blockIdx.x];
 	const int prob = t.x;
 	if (!st[prob].outer_active) return;
+	// the first refinement step also forms ||b||; every block of the problem
+	// reads `outer` before the problem's last block changes it
+	const bool first = st[prob].outer == 0;
 	const ProbDev &pr = P[prob];
 	const LevelDev &L = pr.lv[0];
 	int i = tile_i(t);
@@ -342,6 +394,7 @@ __global__ void k_resid64(const ProbDev *__restrict__ P, ProbState *st, const in
 			s.outer_active = 0;
 			s.inner_active = 0;
 			if (s.status == SIMPOIS_OK && !ok) s.status = SIMPOIS_NOT_CONVERGED;
+			atomicSub(&gl->outer_count, 1);
 		} else {
 			s.outer += 1;
 			s.iter = 0;
@@ -353,6 +406,47 @@ __global__ void k_resid64(const ProbDev *__restrict__ P, ProbState *st, const in
 			atomicAdd(&gl->inner_count, 1);
 		}
 	}
+}
+
+// After compaction: a problem without unknowns is finished before it starts;
+// outer_count = the problems that have an unknown.
+__global__ void k_init_counts(ProbState *st, const int *__restrict__ tcnt, int n, Globals *gl)
+{
+	__shared__ int cnt;
+	if (threadIdx.x == 0) cnt = 0;
+	__syncthreads();
+	for (int p = threadIdx.x; p < n; p += blockDim.x) {
+		if (tcnt[p] > 0)
+			atomicAdd(&cnt, 1);
+		else
+			st[p].outer_active = 0;
+	}
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		gl->outer_count = cnt;
+		gl->inner_count = 0;
+		gl->guard_outer = 0;
+		gl->guard_inner = 0;
+		gl->n_inner = 0;
+		gl->n_outer = 0;
+	}
+}
+
+// Condition of a device-side WHILE loop: continue while problems are still
+// running (count > 0) and the loop has run fewer than gmax bodies.  `reset`
+// marks the evaluation before the loop's first body.
+__global__ void k_setcond(cudaGraphConditionalHandle h, Globals *gl, int outer, int reset, int gmax)
+{
+	if (threadIdx.x != 0) return;
+	int *guard = outer ? &gl->guard_outer : &gl->guard_inner;
+	const int count = outer ? gl->outer_count : gl->inner_count;
+	if (reset) {
+		*guard = 0;
+	} else {
+		*guard += 1;
+		if (outer) gl->n_outer += 1; else gl->n_inner += 1;
+	}
+	cudaGraphSetConditional(h, (count > 0 && *guard < gmax) ? 1u : 0u);
 }
 
 // U += x at the unknowns (end of an inner solve)
@@ -419,7 +513,7 @@ __global__ void k_spmv(const ProbDev *__restrict__ P, ProbState *st, const int4 
 		}
 	}
 	double tot[2];
-	if (problem_sum2(pq, 0.0, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
+	if (problem_sum1(pq, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
 		ProbState &s = st[prob];
 		double a = s.rho / tot[0];
 		if (!(tot[0] > 0) || !isfinite(a)) {
@@ -434,8 +528,9 @@ __global__ void k_spmv(const ProbDev *__restrict__ P, ProbState *st, const int4 
 }
 
 // x += alpha p; r -= alpha q; r.r; the inner stopping test
-__global__ void k_xr(const ProbDev *__restrict__ P, ProbState *st, const int4 *__restrict__ tl,
-		const int *__restrict__ tbeg, const int *__restrict__ tcnt, double *partial, Globals *gl)
+__global__ void __launch_bounds__(SP_THREADS, 8) k_xr(const ProbDev *__restrict__ P, ProbState *st, const int4 *__restrict__ tl,
+		const int *__restrict__ tbeg, const int *__restrict__ tcnt, double *partial, Globals *gl,
+		int use_p2)
 {
 	__shared__ double sh[32];
 	int4 t = tl[blockIdx.x];
@@ -444,22 +539,35 @@ __global__ void k_xr(const ProbDev *__restrict__ P, ProbState *st, const int4 *_
 	const ProbDev &pr = P[prob];
 	const LevelDev &L = pr.lv[0];
 	const float a = (float)st[prob].alpha;
+	const float *pv = use_p2 ? pr.p2 : pr.p;
 	int i = tile_i(t);
 	double rr = 0;
+	// all loads of the four rows first (they depend only on coordinates)
+	uint8_t m[SP_ROWS];
+	float xv[SP_ROWS], pk[SP_ROWS], bk[SP_ROWS], qk[SP_ROWS];
+	int kk[SP_ROWS];
+#pragma unroll
 	for (int r = 0; r < SP_ROWS; r++) {
-		int j = tile_j(t, r);
-		if (i < pr.w && j < pr.h) {
-			size_t k = (size_t)j * pr.w + i;
-			if (L.mask[k]) {
-				pr.x[k] += a * pr.p[k];
-				float rk = L.b[k] - a * pr.q[k];
-				L.b[k] = rk;
-				rr += (double)rk * rk;
-			}
+		const int j = tile_j(t, r);
+		const bool in = i < pr.w && j < pr.h;
+		kk[r] = in ? j * pr.w + i : 0;
+		m[r] = in ? L.mask[kk[r]] : 0;
+		xv[r] = in ? pr.x[kk[r]] : 0.f;
+		pk[r] = in ? pv[kk[r]] : 0.f;
+		bk[r] = in ? L.b[kk[r]] : 0.f;
+		qk[r] = in ? pr.q[kk[r]] : 0.f;
+	}
+#pragma unroll
+	for (int r = 0; r < SP_ROWS; r++) {
+		if (m[r]) {
+			pr.x[kk[r]] = xv[r] + a * pk[r];
+			const float rk = bk[r] - a * qk[r];
+			L.b[kk[r]] = rk;
+			rr += (double)rk * rk;
 		}
 	}
 	double tot[2];
-	if (problem_sum2(rr, 0.0, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
+	if (problem_sum1(rr, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
 		ProbState &s = st[prob];
 		s.rr = tot[0];
 		s.iter += 1;
@@ -491,7 +599,7 @@ __global__ void k_rz(const ProbDev *__restrict__ P, ProbState *st, const int4 *_
 		}
 	}
 	double tot[2];
-	if (problem_sum2(rz, 0.0, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
+	if (problem_sum1(rz, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
 		ProbState &s = st[prob];
 		if (!(tot[0] > 0) || !isfinite(tot[0])) {
 			// r = 0 exactly, or a preconditioner that is not positive here
@@ -554,7 +662,7 @@ __global__ void k_smooth(const ProbDev *__restrict__ P, const ProbState *__restr
 			if (L.mask[k]) {
 				float d, o;
 				split<K>(L, L.z, i, j, d, o);
-				L.z[k] = (L.b[k] - o) / d;
+				L.z[k] = gs_div(L.b[k] - o, d);
 			}
 		}
 	}
@@ -640,11 +748,423 @@ __global__ void k_coarsest(const ProbDev *__restrict__ P, const ProbState *__res
 				if (k < n && m[k] && colour_of(K, i, j) == c) {
 					float d, o;
 					split<K>(Ls, z, i, j, d, o);
-					z[k] = (b[k] - o) / d;
+					z[k] = gs_div(b[k] - o, d);
 				}
 				__syncthreads();
 			}
 	if (k < n) L.z[k] = m[k] ? z[k] : 0.f;
+}
+
+// ------------------------------------------------------------------ fused 5-point V-cycle
+//
+// Overlapped tiling: a block loads its 32 x 32 tile plus a halo of FH pixels
+// into shared memory and runs the colour sweeps on shrinking regions, so each
+// level costs two launches (pre, post) instead of eleven.  A pixel of the halo
+// is updated from exactly the values the block that owns it uses, so the
+// fused cycle computes what the per-sweep kernels compute, bit for bit (the
+// float operations are issued in the same order as in split<0>).
+
+constexpr int FH = 2 * NU5;           // halo: one pixel per half-sweep
+constexpr int FR = SP_TILE + 2 * FH;  // side of the shared region (40)
+constexpr int FN = FR * FR;
+// Levels with max(w, h) <= coarse_max() run in k_coarse5, one block per
+// problem.  Default 64 (measured best on 2048^2 x 3 against 32 and 128);
+// SIMPOIS_COARSE_MAX (8..128) overrides it.
+// SIMPOIS_VERBOSE=1: print each refinement step's residual to stderr
+bool verbose()
+{
+	static bool v = [] {
+		const char *e = getenv("SIMPOIS_VERBOSE");
+		return e && atoi(e) > 0;
+	}();
+	return v;
+}
+
+int coarse_max()
+{
+	static int v = [] {
+		const char *e = getenv("SIMPOIS_COARSE_MAX");
+		int x = e ? atoi(e) : 64;
+		return x < 8 ? 8 : (x > 128 ? 128 : x);
+	}();
+	return v;
+}
+
+// 5-point Gauss-Seidel update of region cell c (region side R), in place:
+// z = (b - off) / diag with off = -(sum of the unknown in-image neighbours),
+// the neighbours taken in split<0>'s order (E, W, S, N).
+__device__ __forceinline__ void gs5_cell(float *z, const float *b, const uint8_t *m, int c, int R,
+		int gi, int gj, int w, int h)
+{
+	float diag = 4.f, off = 0.f;
+	if (gi + 1 < w) { if (m[c + 1]) off -= z[c + 1]; } else diag -= 1.f;
+	if (gi > 0)     { if (m[c - 1]) off -= z[c - 1]; } else diag -= 1.f;
+	if (gj + 1 < h) { if (m[c + R]) off -= z[c + R]; } else diag -= 1.f;
+	if (gj > 0)     { if (m[c - R]) off -= z[c - R]; } else diag -= 1.f;
+	z[c] = gs_div(b[c] - off, diag);
+}
+
+// A z at region cell c, as split<0> then d*z + off
+__device__ __forceinline__ float az5_cell(const float *z, const uint8_t *m, int c, int R, int gi, int gj,
+		int w, int h)
+{
+	float diag = 4.f, off = 0.f;
+	if (gi + 1 < w) { if (m[c + 1]) off -= z[c + 1]; } else diag -= 1.f;
+	if (gi > 0)     { if (m[c - 1]) off -= z[c - 1]; } else diag -= 1.f;
+	if (gj + 1 < h) { if (m[c + R]) off -= z[c + R]; } else diag -= 1.f;
+	if (gj > 0)     { if (m[c - R]) off -= z[c - R]; } else diag -= 1.f;
+	return diag * z[c] + off;
+}
+
+// Pre-smoothing from z = 0 (NU5 forward red-black sweeps), residual, and its
+// restriction (sum over the children) into b of level l+1.  Writes z of level
+// l (the pre-smoothed correction).
+__global__ void __launch_bounds__(SP_THREADS) k_pre5(const ProbDev *__restrict__ P, const ProbState *__restrict__ st,
+		const int4 *__restrict__ tl, int l)
+{
+	__shared__ float sb[FN], sz[FN];
+	__shared__ uint8_t sm[FN];
+	const int4 t = tl[blockIdx.x];
+	const ProbDev &pr = P[t.x];
+	if (!st[t.x].inner_active || l >= pr.nfine) return;
+	const LevelDev L = pr.lv[l];
+	const int x0 = t.y * SP_TILE - FH, y0 = t.z * SP_TILE - FH;
+	// every load depends only on the coordinates, so all are in flight at once
+#pragma unroll
+	for (int it = 0; it < (FN + SP_THREADS - 1) / SP_THREADS; it++) {
+		const int c = threadIdx.x + it * SP_THREADS;
+		if (c < FN) {
+			const int ry = c / FR, rx = c - ry * FR, gi = x0 + rx, gj = y0 + ry;
+			const bool in = gi >= 0 && gi < L.w && gj >= 0 && gj < L.h;
+			const size_t k = in ? (size_t)gj * L.w + gi : 0;
+			const uint8_t m = in ? L.mask[k] : 0;
+			const float bv = in ? L.b[k] : 0.f;
+			sm[c] = m;
+			sb[c] = m ? bv : 0.f;
+			sz[c] = 0.f;
+		}
+	}
+	__syncthreads();
+	// half-sweep s updates colour s&1 on the region [s, FR-s)^2; at s = 0 the
+	// neighbours are all 0, so the outermost ring needs no outside value
+	for (int s = 0; s < 2 * NU5; s++) {
+		const int colour = s & 1, lo = s, hi = FR - s;
+		for (int q = threadIdx.x; q < FN / 2; q += SP_THREADS) {
+			const int ry = q / (FR / 2);
+			const int rx = 2 * (q - ry * (FR / 2)) + ((colour ^ (x0 + y0 + ry)) & 1);
+			const int c = ry * FR + rx, gi = x0 + rx, gj = y0 + ry;
+			if (rx < lo || rx >= hi || ry < lo || ry >= hi || !sm[c]) continue;
+			if (s == 0) {
+				float diag = 4.f - (gi + 1 >= L.w) - (gi <= 0) - (gj + 1 >= L.h) - (gj <= 0);
+				sz[c] = gs_div(sb[c] - 0.f, diag);
+			} else {
+				gs5_cell(sz, sb, sm, c, FR, gi, gj, L.w, L.h);
+			}
+		}
+		__syncthreads();
+	}
+	// write the pre-smoothed correction of the tile
+	for (int c = threadIdx.x; c < SP_TILE * SP_TILE; c += SP_THREADS) {
+		const int ty = c >> 5, tx = c & 31, gi = x0 + FH + tx, gj = y0 + FH + ty;
+		if (gi < L.w && gj < L.h) L.z[(size_t)gj * L.w + gi] = sz[(ty + FH) * FR + tx + FH];
+	}
+	// restriction: one coarse cell per thread (16 x 16 per tile)
+	const LevelDev C = pr.lv[l + 1];
+	const int ci = t.y * (SP_TILE / 2) + (threadIdx.x & 15), cj = t.z * (SP_TILE / 2) + (threadIdx.x >> 4);
+	if (ci < C.w && cj < C.h && C.mask[(size_t)cj * C.w + ci]) {
+		float acc = 0.f;
+		for (int bb = 0; bb < 2; bb++)
+			for (int aa = 0; aa < 2; aa++) {
+				const int fi = 2 * ci + aa, fj = 2 * cj + bb;
+				if (fi < L.w && fj < L.h) {
+					const int c = (fj - y0) * FR + (fi - x0);
+					acc += sb[c] - az5_cell(sz, sm, c, FR, fi, fj, L.w, L.h);
+				}
+			}
+		C.b[(size_t)cj * C.w + ci] = 1.f * acc;
+	}
+}
+
+// Coarse correction (injection from z2 of level l+1) and post-smoothing
+// (NU5 backward sweeps); writes z2 of level l.  At level 0 also r.z and the
+// PCG scalars beta, rho (the last tile of the problem to finish).
+__global__ void __launch_bounds__(SP_THREADS) k_post5(const ProbDev *__restrict__ P, ProbState *st,
+		const int4 *__restrict__ tl, int l, const int *__restrict__ tbeg, const int *__restrict__ tcnt,
+		double *partial, Globals *gl)
+{
+	__shared__ float sb[FN], sz[FN];
+	__shared__ uint8_t sm[FN];
+	__shared__ double sh[32];
+	const int4 t = tl[blockIdx.x];
+	const int prob = t.x;
+	const ProbDev &pr = P[prob];
+	if (!st[prob].inner_active || l >= pr.nfine) return;
+	const LevelDev L = pr.lv[l], C = pr.lv[l + 1];
+	const int x0 = t.y * SP_TILE - FH, y0 = t.z * SP_TILE - FH;
+#pragma unroll
+	for (int it = 0; it < (FN + SP_THREADS - 1) / SP_THREADS; it++) {
+		const int c = threadIdx.x + it * SP_THREADS;
+		if (c < FN) {
+			const int ry = c / FR, rx = c - ry * FR, gi = x0 + rx, gj = y0 + ry;
+			const bool in = gi >= 0 && gi < L.w && gj >= 0 && gj < L.h;
+			const size_t k = in ? (size_t)gj * L.w + gi : 0;
+			const size_t kc = in ? (size_t)(gj >> 1) * C.w + (gi >> 1) : 0;
+			const uint8_t m = in ? L.mask[k] : 0;
+			const float bv = in ? L.b[k] : 0.f;
+			const float zv = in ? L.z[k] : 0.f;
+			const uint8_t cm = in ? C.mask[kc] : 0;
+			const float cz = in ? C.z2[kc] : 0.f;
+			sm[c] = m;
+			sb[c] = m ? bv : 0.f;
+			sz[c] = m ? (cm ? zv + cz : zv) : 0.f;
+		}
+	}
+	__syncthreads();
+	for (int s = 0; s < 2 * NU5; s++) {
+		const int colour = 1 - (s & 1), lo = s + 1, hi = FR - s - 1;
+		for (int q = threadIdx.x; q < FN / 2; q += SP_THREADS) {
+			const int ry = q / (FR / 2);
+			const int rx = 2 * (q - ry * (FR / 2)) + ((colour ^ (x0 + y0 + ry)) & 1);
+			const int c = ry * FR + rx, gi = x0 + rx, gj = y0 + ry;
+			if (rx < lo || rx >= hi || ry < lo || ry >= hi || !sm[c]) continue;
+			gs5_cell(sz, sb, sm, c, FR, gi, gj, L.w, L.h);
+		}
+		__syncthreads();
+	}
+	double rz = 0;
+	for (int c = threadIdx.x; c < SP_TILE * SP_TILE; c += SP_THREADS) {
+		const int ty = c >> 5, tx = c & 31, gi = x0 + FH + tx, gj = y0 + FH + ty;
+		if (gi < L.w && gj < L.h) {
+			const int rc = (ty + FH) * FR + tx + FH;
+			L.z2[(size_t)gj * L.w + gi] = sz[rc];
+			if (sm[rc]) rz += (double)sb[rc] * (double)sz[rc];
+		}
+	}
+	if (l != 0) return;
+	double tot[2];
+	if (problem_sum1(rz, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
+		ProbState &s = st[prob];
+		if (!(tot[0] > 0) || !isfinite(tot[0])) {
+			if (tot[0] != 0) s.status = SIMPOIS_BREAKDOWN;
+			s.inner_active = 0;
+			atomicSub(&gl->inner_count, 1);
+		} else {
+			s.beta = s.rho > 0 ? tot[0] / s.rho : 0.0;
+			s.rho = tot[0];
+		}
+	}
+}
+
+// Shared-memory layout of the coarse levels of one problem.
+struct CoarseLayout {
+	int off_m[MAXLEV], off_b[MAXLEV], off_z[MAXLEV];   // byte offsets
+	int bytes;
+};
+
+__device__ __host__ inline CoarseLayout coarse_layout(const int *lw, const int *lh, int c, int L)
+{
+	CoarseLayout cl;
+	int o = 0;
+	for (int l = c; l < L; l++) {
+		const int n = lw[l] * lh[l];
+		cl.off_b[l] = o;
+		o += 4 * n;
+		cl.off_z[l] = o;
+		o += 4 * n;
+	}
+	for (int l = c; l < L; l++) {
+		cl.off_m[l] = o;
+		o += lw[l] * lh[l];
+	}
+	cl.bytes = (o + 15) / 16 * 16;
+	return cl;
+}
+
+// One red-black half-sweep (colour) over a whole level held in shared memory;
+// the 1024 threads map to 32 x 32 (half-columns, rows) of the colour's cells.
+__device__ __forceinline__ void smem_sweep5(float *z, const float *b, const uint8_t *m, int w, int h, int colour)
+{
+	const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+	const int hw = (w + 1) >> 1;
+	for (int j = ty; j < h; j += 32)
+		for (int k = tx; k < hw; k += 32) {
+			const int i = 2 * k + ((colour ^ j) & 1);
+			const int c = j * w + i;
+			if (i < w && m[c]) gs5_cell(z, b, m, c, w, i, j, w, h);
+		}
+	__syncthreads();
+}
+
+// The V-cycle below level nfine of every problem, one block per problem, all
+// in shared memory: the same sweeps, restriction and injection as the tile
+// kernels, with the coarsest level (<= 4 x 4) getting COARSE_SWEEPS symmetric
+// sweeps.  Reads b of level nfine, writes z2 of level nfine.  When nfine == 0
+// (a problem no larger than coarse_max()) it also forms r.z and the PCG scalars.
+__global__ void __launch_bounds__(1024) k_coarse5(const ProbDev *__restrict__ P, ProbState *st, Globals *gl)
+{
+	extern __shared__ __align__(16) unsigned char smem[];
+	__shared__ double sh[32];
+	const int prob = blockIdx.x;
+	if (!st[prob].inner_active) return;
+	const ProbDev &pr = P[prob];
+	const int c0 = pr.nfine, L = pr.nlev;
+	int lw[MAXLEV], lh[MAXLEV];
+	for (int l = 0; l < L; l++) { lw[l] = pr.lv[l].w; lh[l] = pr.lv[l].h; }
+	const CoarseLayout cl = coarse_layout(lw, lh, c0, L);
+	auto Zs = [&](int l) { return (float *)(smem + cl.off_z[l]); };
+	auto Bs = [&](int l) { return (float *)(smem + cl.off_b[l]); };
+	auto Ms = [&](int l) { return (uint8_t *)(smem + cl.off_m[l]); };
+	for (int l = c0; l < L; l++) {
+		const uint8_t *gm = pr.lv[l].mask;
+		uint8_t *m = Ms(l);
+		float *z = Zs(l), *b = Bs(l);
+		for (int c = threadIdx.x; c < lw[l] * lh[l]; c += blockDim.x) {
+			const uint8_t mv = gm[c];
+			m[c] = mv;
+			z[c] = 0.f;
+			if (l == c0) b[c] = mv ? pr.lv[l].b[c] : 0.f;
+		}
+	}
+	__syncthreads();
+	// down
+	for (int l = c0; l + 1 < L; l++) {
+		float *z = Zs(l), *b = Bs(l);
+		const uint8_t *m = Ms(l);
+		for (int s = 0; s < NU5; s++) {
+			smem_sweep5(z, b, m, lw[l], lh[l], 0);
+			smem_sweep5(z, b, m, lw[l], lh[l], 1);
+		}
+		float *bc = Bs(l + 1);
+		const uint8_t *mc = Ms(l + 1);
+		const int wc = lw[l + 1], hc = lh[l + 1];
+		for (int c = threadIdx.x; c < wc * hc; c += blockDim.x) {
+			const int cj = c / wc, ci = c - cj * wc;
+			if (!mc[c]) continue;
+			float acc = 0.f;
+			for (int bb = 0; bb < 2; bb++)
+				for (int aa = 0; aa < 2; aa++) {
+					const int fi = 2 * ci + aa, fj = 2 * cj + bb;
+					if (fi < lw[l] && fj < lh[l]) {
+						const int f = fj * lw[l] + fi;
+						acc += b[f] - az5_cell(z, m, f, lw[l], fi, fj, lw[l], lh[l]);
+					}
+				}
+			bc[c] = 1.f * acc;
+		}
+		__syncthreads();
+	}
+	{   // coarsest
+		const int l = L - 1;
+		float *z = Zs(l), *b = Bs(l);
+		const uint8_t *m = Ms(l);
+		for (int s = 0; s < COARSE_SWEEPS; s++) {
+			smem_sweep5(z, b, m, lw[l], lh[l], 0);
+			smem_sweep5(z, b, m, lw[l], lh[l], 1);
+			smem_sweep5(z, b, m, lw[l], lh[l], 1);
+			smem_sweep5(z, b, m, lw[l], lh[l], 0);
+		}
+	}
+	// up
+	for (int l = L - 2; l >= c0; l--) {
+		float *z = Zs(l), *b = Bs(l);
+		const uint8_t *m = Ms(l);
+		const float *zc = Zs(l + 1);
+		const uint8_t *mc = Ms(l + 1);
+		const int wc = lw[l + 1];
+		for (int c = threadIdx.x; c < lw[l] * lh[l]; c += blockDim.x) {
+			const int j = c / lw[l], i = c - j * lw[l];
+			const int kc = (j >> 1) * wc + (i >> 1);
+			if (m[c] && mc[kc]) z[c] += zc[kc];
+		}
+		__syncthreads();
+		for (int s = 0; s < NU5; s++) {
+			smem_sweep5(z, b, m, lw[l], lh[l], 1);
+			smem_sweep5(z, b, m, lw[l], lh[l], 0);
+		}
+	}
+	const float *z = Zs(c0), *b = Bs(c0);
+	const uint8_t *m = Ms(c0);
+	double rz = 0;
+	for (int c = threadIdx.x; c < lw[c0] * lh[c0]; c += blockDim.x) {
+		pr.lv[c0].z2[c] = m[c] ? z[c] : 0.f;
+		if (m[c]) rz += (double)b[c] * (double)z[c];
+	}
+	if (c0 != 0) return;
+	rz = block_sum<1024>(rz, sh);
+	if (threadIdx.x == 0) {
+		ProbState &s = st[prob];
+		if (!(rz > 0) || !isfinite(rz)) {
+			if (rz != 0) s.status = SIMPOIS_BREAKDOWN;
+			s.inner_active = 0;
+			atomicSub(&gl->inner_count, 1);
+		} else {
+			s.beta = s.rho > 0 ? rz / s.rho : 0.0;
+			s.rho = rz;
+		}
+	}
+}
+
+// p_new = z + beta p_old on the tile and a 1-pixel halo (as k_pupdate), then
+// q = A p_new and alpha = rho / (p_new . q) (as k_spmv<0>).  p_old and p_new
+// are different buffers (the halo of a neighbour must still see p_old).
+__global__ void __launch_bounds__(SP_THREADS) k_spmv5(const ProbDev *__restrict__ P, ProbState *st,
+		const int4 *__restrict__ tl, const int *__restrict__ tbeg, const int *__restrict__ tcnt, double *partial,
+		Globals *gl, int new_is_p2)
+{
+	constexpr int R = SP_TILE + 2, N = R * R;
+	__shared__ float sp[N];
+	__shared__ uint8_t sm[N];
+	__shared__ double sh[32];
+	const int4 t = tl[blockIdx.x];
+	const int prob = t.x;
+	if (!st[prob].inner_active) return;
+	const ProbDev &pr = P[prob];
+	const LevelDev L = pr.lv[0];
+	const float beta = (float)st[prob].beta;
+	const float *pold = new_is_p2 ? pr.p : pr.p2;
+	float *pnew = new_is_p2 ? pr.p2 : pr.p;
+	const int x0 = t.y * SP_TILE - 1, y0 = t.z * SP_TILE - 1;
+#pragma unroll
+	for (int it = 0; it < (N + SP_THREADS - 1) / SP_THREADS; it++) {
+		const int c = threadIdx.x + it * SP_THREADS;
+		if (c < N) {
+			const int ry = c / R, rx = c - ry * R, gi = x0 + rx, gj = y0 + ry;
+			const bool in = gi >= 0 && gi < L.w && gj >= 0 && gj < L.h;
+			const size_t k = in ? (size_t)gj * L.w + gi : 0;
+			const uint8_t m = in ? L.mask[k] : 0;
+			const float zv = in ? L.z2[k] : 0.f;
+			const float po = (in && beta != 0.f) ? pold[k] : 0.f;
+			sm[c] = m;
+			sp[c] = m ? (beta != 0.f ? zv + beta * po : zv) : 0.f;
+		}
+	}
+	__syncthreads();
+	double pq = 0;
+	for (int c = threadIdx.x; c < SP_TILE * SP_TILE; c += SP_THREADS) {
+		const int ty = c >> 5, tx = c & 31, gi = x0 + 1 + tx, gj = y0 + 1 + ty;
+		const int rc = (ty + 1) * R + tx + 1;
+		if (gi < L.w && gj < L.h && sm[rc]) {
+			const size_t k = (size_t)gj * L.w + gi;
+			const float pk = sp[rc];
+			const float qk = az5_cell(sp, sm, rc, R, gi, gj, L.w, L.h);
+			pnew[k] = pk;
+			pr.q[k] = qk;
+			pq += (double)pk * (double)qk;
+		}
+	}
+	double tot[2];
+	if (problem_sum1(pq, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
+		ProbState &s = st[prob];
+		double a = s.rho / tot[0];
+		if (!(tot[0] > 0) || !isfinite(a)) {
+			s.status = SIMPOIS_BREAKDOWN;
+			s.inner_active = 0;
+			s.alpha = 0;
+			atomicSub(&gl->inner_count, 1);
+		} else {
+			s.alpha = a;
+		}
+	}
 }
 
 // out = unknown ? (float)U : g over all tiles (fill)
@@ -764,7 +1284,74 @@ struct Plan {
 	const float **gout = nullptr;
 	float **gin = nullptr, **gdat = nullptr;
 	long long *nl = nullptr;   // the context's launch counter
+	int fused = 0;             // 5-point fused V-cycle (k_pre5/k_coarse5/k_post5)
+	int nfine_max = 0;         // largest nfine over the problems
+	int coarse_smem = 0;       // dynamic shared memory of k_coarse5
+	struct KTimer *kt = nullptr;   // kernel timer, or null
 };
+
+// Kernel timer: an event pair around each launch of the main-loop kernels,
+// with the launch's algorithmic bytes counted over the active tiles of the
+// problems still iterating (read back before each launch group).
+struct KTimer {
+	struct Rec {
+		const char *name;
+		cudaEvent_t a, b;
+		double bytes;
+	};
+	simpois_ctx *ctx;
+	std::vector<Rec> recs;
+	std::vector<int> tiles;         // tiles[l * n + p]: active tiles of problem p at level l
+	std::vector<int> coarse_cells;  // cells of the k_coarse5 top level per problem
+	std::vector<char> active;       // inner_active per problem (host copy)
+	size_t next_ev = 0;
+	int n = 0;
+	cudaEvent_t ev()
+	{
+		if (next_ev == ctx->evpool.size()) {
+			cudaEvent_t e;
+			cudaEventCreate(&e);
+			ctx->evpool.push_back(e);
+		}
+		return ctx->evpool[next_ev++];
+	}
+	double px(int l) const
+	{
+		double s = 0;
+		for (int p = 0; p < n; p++)
+			if (active[p]) s += (double)tiles[l * n + p] * SP_TILE * SP_TILE;
+		return s;
+	}
+	double cells() const
+	{
+		double s = 0;
+		for (int p = 0; p < n; p++)
+			if (active[p]) s += coarse_cells[p];
+		return s;
+	}
+};
+
+// algorithmic bytes per tile pixel of each timed kernel (reads + writes)
+constexpr double BPX_PRE5 = 1 + 4 + 4 + 0.25 + 1;         // mask, b, z; coarse mask, coarse b
+constexpr double BPX_POST5 = 1 + 4 + 4 + 1 + 0.25 + 4;    // mask, b, z, coarse z2, coarse mask; z2
+constexpr double BPX_SPMV5 = 1 + 4 + 4 + 4 + 4;           // mask, z2, p_old; p_new, q
+constexpr double BPX_XR = 1 + 4 + 4 + 4 + 4 + 4 + 4;      // mask, x, p, b, q; x, b
+constexpr double BPX_RESID64 = 1 + 8 + 4 + 4 + 4;         // mask, U, rhs; b, x
+constexpr double BPX_UADD = 1 + 8 + 4 + 8;                // mask, U, x; U
+constexpr double BPC_COARSE5 = 1 + 4 + 4 + 0.34;          // per top coarse cell: mask, b; z2; coarser masks
+
+#define KT_BEGIN(pl, s)                                            \
+	cudaEvent_t kt_a_ = nullptr;                               \
+	if ((pl).kt) {                                             \
+		kt_a_ = (pl).kt->ev();                             \
+		cudaEventRecord(kt_a_, s);                         \
+	}
+#define KT_END(pl, s, nm, by)                                      \
+	if ((pl).kt) {                                             \
+		cudaEvent_t kt_b_ = (pl).kt->ev();                 \
+		cudaEventRecord(kt_b_, s);                         \
+		(pl).kt->recs.push_back({nm, kt_a_, kt_b_, (by)}); \
+	}
 
 inline int ntiles(int v) { return (v + SP_TILE - 1) / SP_TILE; }
 
@@ -827,9 +1414,191 @@ void launch_iteration(const Plan &pl, const MgOptions &opt, cudaStream_t s)
 	const int nt = pl.nact[0];
 	k_pupdate<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0]); ++*pl.nl;
 	k_spmv<K><<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl); ++*pl.nl;
-	k_xr<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl); ++*pl.nl;
+	k_xr<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl, 0); ++*pl.nl;
 	launch_precond<K>(pl, opt, s);
 	k_rz<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl); ++*pl.nl;
+}
+
+// Fused 5-point V-cycle: k_pre5 down the fine levels, k_coarse5 for the rest,
+// k_post5 back up; r.z and beta come out of k_post5 at level 0 (or k_coarse5
+// for problems without fine levels).
+// Kernel timer: refresh the host copy of which problems are still iterating.
+void kt_refresh(const Plan &pl, cudaStream_t s)
+{
+	if (!pl.kt) return;
+	std::vector<ProbState> h(pl.n);
+	cudaMemcpyAsync(h.data(), pl.dst, sizeof(ProbState) * pl.n, cudaMemcpyDeviceToHost, s);
+	cudaStreamSynchronize(s);
+	for (int p = 0; p < pl.n; p++) pl.kt->active[p] = h[p].inner_active != 0;
+}
+
+void launch_vcycle_fused(const Plan &pl, cudaStream_t s)
+{
+	kt_refresh(pl, s);
+	for (int l = 0; l < pl.nfine_max; l++) {
+		if (!pl.nact[l]) continue;
+		KT_BEGIN(pl, s);
+		k_pre5<<<pl.nact[l], SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[l], l); ++*pl.nl;
+		KT_END(pl, s, "k_pre5", pl.kt->px(l) * BPX_PRE5);
+	}
+	{
+		KT_BEGIN(pl, s);
+		k_coarse5<<<pl.n, 1024, pl.coarse_smem, s>>>(pl.dp, pl.dst, pl.gl); ++*pl.nl;
+		KT_END(pl, s, "k_coarse5", pl.kt->cells() * BPC_COARSE5);
+	}
+	for (int l = pl.nfine_max - 1; l >= 0; l--) {
+		if (!pl.nact[l]) continue;
+		KT_BEGIN(pl, s);
+		k_post5<<<pl.nact[l], SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[l], l, pl.tbeg, pl.tcnt, pl.partial,
+				pl.gl); ++*pl.nl;
+		KT_END(pl, s, "k_post5", pl.kt->px(l) * BPX_POST5);
+	}
+}
+
+// Two fused PCG iterations (the search direction alternates between p and p2).
+void launch_iteration_fused(const Plan &pl, cudaStream_t s)
+{
+	const int nt = pl.nact[0];
+	for (int parity = 0; parity < 2; parity++) {
+		kt_refresh(pl, s);
+		{
+			KT_BEGIN(pl, s);
+			k_spmv5<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl,
+					parity); ++*pl.nl;
+			KT_END(pl, s, "k_spmv5", pl.kt->px(0) * BPX_SPMV5);
+		}
+		{
+			KT_BEGIN(pl, s);
+			k_xr<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl,
+					parity); ++*pl.nl;
+			KT_END(pl, s, "k_xr", pl.kt->px(0) * BPX_XR);
+		}
+		launch_vcycle_fused(pl, s);
+	}
+}
+
+// Signature of everything a solve graph bakes into its kernel parameters.
+std::string plan_signature(const simpois_ctx *ctx, const Plan &pl, int K, bool fused, const MgOptions &opt)
+{
+	std::string sig;
+	char buf[96];
+	snprintf(buf, sizeof buf, "%p/%d/%d/%d/%d/%d/%d/%d|", (void *)ctx->arena, pl.n, K, (int)fused, pl.nfine_max,
+			pl.nlev_max, pl.coarse_smem, opt.use_mg);
+	sig += buf;
+	snprintf(buf, sizeof buf, "%p/%p/%p/%p/%p/%p|", (void *)pl.dp, (void *)pl.dst, (void *)pl.gl, (void *)pl.tbeg,
+			(void *)pl.tcnt, (void *)pl.partial);
+	sig += buf;
+	for (int l = 0; l < pl.nlev_max; l++) {
+		snprintf(buf, sizeof buf, "%p:%d,", (void *)pl.act[l], pl.nact[l]);
+		sig += buf;
+	}
+	return sig;
+}
+
+// Build the whole converged solve as one graph with two nested device-side
+// WHILE loops: refinement steps (k_resid64, first V-cycle, the PCG loop, U +=
+// x) while a problem is still refining, and PCG iterations while a problem's
+// inner solve runs.  Both loops are bounded (gmax) besides the per-problem
+// caps the kernels enforce.  Returns cudaErrorNotSupported-like failures to
+// the caller, which then drives the loops from the host.
+template <int K>
+cudaError_t build_solve_graph(simpois_ctx *ctx, Plan &pl, const MgOptions &opt, bool fused)
+{
+	cudaStream_t cs = ctx->capture_stream;
+	const int nt = pl.nact[0];
+	cudaGraph_t G = nullptr;
+	cudaError_t e = cudaGraphCreate(&G, 0);
+	if (e != cudaSuccess) return e;
+	long long n0 = *pl.nl, n_outer = 0, n_inner = 0;
+	cudaGraphConditionalHandle ho, hi;
+	cudaGraphNodeParams po = {};
+	cudaGraphNode_t node_o, node_i;
+	cudaGraph_t body_o = nullptr, body_i = nullptr;
+	do {
+		if ((e = cudaGraphConditionalHandleCreate(&ho, G, 1, cudaGraphCondAssignDefault)) != cudaSuccess) break;
+		po.type = cudaGraphNodeTypeConditional;
+		po.conditional.handle = ho;
+		po.conditional.type = cudaGraphCondTypeWhile;
+		po.conditional.size = 1;
+		if ((e = cudaGraphAddNode(&node_o, G, nullptr, nullptr, 0, &po)) != cudaSuccess) break;
+		body_o = po.conditional.phGraph_out[0];
+		// refinement body
+		if ((e = cudaStreamBeginCaptureToGraph(cs, body_o, nullptr, nullptr, 0,
+				cudaStreamCaptureModeThreadLocal)) != cudaSuccess) break;
+		cudaError_t ce = cudaGraphConditionalHandleCreate(&hi, body_o, 0, cudaGraphCondAssignDefault);
+		long long c0 = *pl.nl;
+		k_resid64<K><<<nt, SP_THREADS, 0, cs>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl);
+		++*pl.nl;
+		if (fused) {
+			launch_vcycle_fused(pl, cs);
+		} else {
+			launch_precond<K>(pl, opt, cs);
+			k_rz<<<nt, SP_THREADS, 0, cs>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl); ++*pl.nl;
+		}
+		k_setcond<<<1, 32, 0, cs>>>(hi, pl.gl, 0, 1, 4 * INNER_MAX); ++*pl.nl;
+		cudaStreamCaptureStatus cst;
+		cudaGraph_t cg;
+		const cudaGraphNode_t *deps = nullptr;
+		size_t ndeps = 0;
+		if (ce == cudaSuccess) ce = cudaStreamGetCaptureInfo(cs, &cst, nullptr, &cg, &deps, nullptr, &ndeps);
+		cudaGraphNodeParams pi = {};
+		pi.type = cudaGraphNodeTypeConditional;
+		pi.conditional.handle = hi;
+		pi.conditional.type = cudaGraphCondTypeWhile;
+		pi.conditional.size = 1;
+		if (ce == cudaSuccess) ce = cudaGraphAddNode(&node_i, cg, deps, nullptr, ndeps, &pi);
+		if (ce == cudaSuccess) ce = cudaStreamUpdateCaptureDependencies(cs, &node_i, nullptr, 1,
+				cudaStreamSetCaptureDependencies);
+		k_uadd<<<nt, SP_THREADS, 0, cs>>>(pl.dp, pl.dst, pl.act[0]); ++*pl.nl;
+		k_setcond<<<1, 32, 0, cs>>>(ho, pl.gl, 1, 0, MAX_OUTER + 2); ++*pl.nl;
+		n_outer = *pl.nl - c0;
+		e = cudaStreamEndCapture(cs, &body_o);
+		if (ce != cudaSuccess) e = ce;
+		if (e != cudaSuccess) break;
+		body_i = pi.conditional.phGraph_out[0];
+		// PCG body
+		if ((e = cudaStreamBeginCaptureToGraph(cs, body_i, nullptr, nullptr, 0,
+				cudaStreamCaptureModeThreadLocal)) != cudaSuccess) break;
+		c0 = *pl.nl;
+		if (fused)
+			launch_iteration_fused(pl, cs);
+		else
+			launch_iteration<K>(pl, opt, cs);
+		k_setcond<<<1, 32, 0, cs>>>(hi, pl.gl, 0, 0, 4 * INNER_MAX); ++*pl.nl;
+		n_inner = *pl.nl - c0;
+		if ((e = cudaStreamEndCapture(cs, &body_i)) != cudaSuccess) break;
+		cudaGraphExec_t ex = nullptr;
+		if ((e = cudaGraphInstantiate(&ex, G, 0)) != cudaSuccess) break;
+		if (ctx->solve_exec) cudaGraphExecDestroy(ctx->solve_exec);
+		ctx->solve_exec = ex;
+		ctx->solve_nodes_outer = n_outer;
+		ctx->solve_nodes_inner = n_inner;
+	} while (0);
+	*pl.nl = n0;
+	cudaGraphDestroy(G);
+	if (e != cudaSuccess) cudaGetLastError();
+	return e;
+}
+
+// The converged solve as one graph launch and one synchronisation.
+template <int K>
+int run_device_loop(simpois_ctx *ctx, Plan &pl, const MgOptions &opt, bool fused, bool *done)
+{
+	*done = false;
+	const std::string sig = plan_signature(ctx, pl, K, fused, opt);
+	if (!ctx->solve_exec || ctx->solve_sig != sig) {
+		ctx->solve_sig.clear();
+		if (build_solve_graph<K>(ctx, pl, opt, fused) != cudaSuccess) return SIMPOIS_OK;  // host loop instead
+		ctx->solve_sig = sig;
+	}
+	cudaStream_t s = ctx->stream;
+	SP_CUDA(ctx, cudaGraphLaunch(ctx->solve_exec, s));
+	Globals *hg = (Globals *)ctx->pinned;
+	SP_CUDA(ctx, cudaMemcpyAsync(hg, pl.gl, sizeof(Globals), cudaMemcpyDeviceToHost, s));
+	SP_CUDA(ctx, cudaStreamSynchronize(s));
+	*pl.nl += ctx->solve_nodes_outer * hg->n_outer + ctx->solve_nodes_inner * hg->n_inner;
+	*done = true;
+	return SIMPOIS_OK;
 }
 
 template <int K>
@@ -839,13 +1608,25 @@ int run_kind(simpois_ctx *ctx, Plan &pl, const MgOptions &opt)
 	int *hcount = (int *)ctx->pinned;
 	const int nt = pl.nact[0];
 	if (nt == 0) return SIMPOIS_OK;
+	const bool fused = K == 0 && pl.fused && opt.use_mg;
+	if (opt.use_graph && !pl.kt && !verbose()) {
+		bool done = false;
+		int r = run_device_loop<K>(ctx, pl, opt, fused, &done);
+		if (r != SIMPOIS_OK || done) return r;
+	}
+	auto iteration = [&](cudaStream_t st) {
+		if (fused)
+			launch_iteration_fused(pl, st);
+		else
+			launch_iteration<K>(pl, opt, st);
+	};
 	cudaGraphExec_t gexec = nullptr;
-	long long per_iter = 0;   // kernel nodes of one captured iteration
-	if (opt.use_graph) {
+	long long per_iter = 0;   // kernel nodes of one captured graph
+	if (opt.use_graph && !pl.kt) {
 		cudaGraph_t graph;
 		long long before = *pl.nl;
 		SP_CUDA(ctx, cudaStreamBeginCapture(ctx->capture_stream, cudaStreamCaptureModeThreadLocal));
-		launch_iteration<K>(pl, opt, ctx->capture_stream);
+		iteration(ctx->capture_stream);
 		SP_CUDA(ctx, cudaStreamEndCapture(ctx->capture_stream, &graph));
 		per_iter = *pl.nl - before;
 		*pl.nl = before;
@@ -855,13 +1636,35 @@ int run_kind(simpois_ctx *ctx, Plan &pl, const MgOptions &opt)
 	}
 	int rc = SIMPOIS_OK;
 	for (int outer = 0; outer <= MAX_OUTER; outer++) {
-		k_resid64<K><<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl,
-				outer == 0); ++*pl.nl;
-		launch_precond<K>(pl, opt, s);
-		k_rz<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl); ++*pl.nl;
+		if (pl.kt) {   // the refinement step runs for every problem not yet converged
+			std::vector<ProbState> h(pl.n);
+			cudaMemcpyAsync(h.data(), pl.dst, sizeof(ProbState) * pl.n, cudaMemcpyDeviceToHost, s);
+			cudaStreamSynchronize(s);
+			for (int p = 0; p < pl.n; p++) pl.kt->active[p] = h[p].outer_active != 0;
+		}
+		{
+			KT_BEGIN(pl, s);
+			k_resid64<K><<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial,
+					pl.gl); ++*pl.nl;
+			KT_END(pl, s, "k_resid64", pl.kt->px(0) * BPX_RESID64);
+		}
+		if (fused) {
+			launch_vcycle_fused(pl, s);
+		} else {
+			launch_precond<K>(pl, opt, s);
+			k_rz<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl); ++*pl.nl;
+		}
 		cudaError_t e = cudaMemcpyAsync(hcount, &pl.gl->inner_count, sizeof(int), cudaMemcpyDeviceToHost, s);
 		if (e == cudaSuccess) e = cudaStreamSynchronize(s);
 		if (e != cudaSuccess) { rc = ctx_fail(ctx, SIMPOIS_ECUDA, "refinement: %s", cudaGetErrorString(e)); break; }
+		if (verbose()) {
+			std::vector<ProbState> h(pl.n);
+			cudaMemcpy(h.data(), pl.dst, sizeof(ProbState) * pl.n, cudaMemcpyDeviceToHost);
+			for (int p = 0; p < pl.n && p < 8; p++)
+				fprintf(stderr, "simpois: problem %d refinement %d: rel %.3e, PCG iterations %d, "
+						"last inner |r|^2 ratio %.3e, status %d\n", p, h[p].outer, h[p].rel,
+						h[p].total_iter, h[p].tau2 > 0 ? h[p].rr / (h[p].tau2) : 0.0, h[p].status);
+		}
 		if (*hcount == 0) break;
 		int chunk = 4;
 		for (int guard = 0; guard < 4 * INNER_MAX; guard++) {
@@ -870,7 +1673,7 @@ int run_kind(simpois_ctx *ctx, Plan &pl, const MgOptions &opt)
 					e = cudaGraphLaunch(gexec, s);
 					*pl.nl += per_iter;
 				} else
-					launch_iteration<K>(pl, opt, s), e = cudaGetLastError();
+					iteration(s), e = cudaGetLastError();
 				if (e != cudaSuccess) break;
 			}
 			if (e == cudaSuccess)
@@ -881,10 +1684,39 @@ int run_kind(simpois_ctx *ctx, Plan &pl, const MgOptions &opt)
 			chunk = 2;
 		}
 		if (e != cudaSuccess) { rc = ctx_fail(ctx, SIMPOIS_ECUDA, "inner solve: %s", cudaGetErrorString(e)); break; }
-		k_uadd<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0]); ++*pl.nl;
+		if (pl.kt) {   // U += x runs for every problem still in the refinement
+			std::vector<ProbState> h(pl.n);
+			cudaMemcpyAsync(h.data(), pl.dst, sizeof(ProbState) * pl.n, cudaMemcpyDeviceToHost, s);
+			cudaStreamSynchronize(s);
+			for (int p = 0; p < pl.n; p++) pl.kt->active[p] = h[p].outer_active != 0;
+		}
+		{
+			KT_BEGIN(pl, s);
+			k_uadd<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0]); ++*pl.nl;
+			KT_END(pl, s, "k_uadd", pl.kt->px(0) * BPX_UADD);
+		}
 	}
 	if (gexec) cudaGraphExecDestroy(gexec);
 	return rc;
+}
+
+// Fold the timer's records into the context's per-kernel totals.
+void kt_collect(simpois_ctx *ctx, KTimer &kt)
+{
+	cudaStreamSynchronize(ctx->stream);
+	for (const auto &r : kt.recs) {
+		float ms = 0;
+		cudaEventElapsedTime(&ms, r.a, r.b);
+		bool found = false;
+		for (auto &k : ctx->kstats)
+			if (k.name == r.name) {
+				k.launches++;
+				k.ms += ms;
+				k.bytes += r.bytes;
+				found = true;
+			}
+		if (!found) ctx->kstats.push_back({r.name, 1, (double)ms, r.bytes});
+	}
 }
 
 }  // namespace
@@ -899,8 +1731,8 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	pl.hp.resize(n);
 	int kinds = 0;
 	Layout Lo;
-	std::vector<size_t> off_mask[MAXLEV], off_b[MAXLEV], off_z[MAXLEV];
-	std::vector<size_t> off_U(n), off_x(n), off_p(n), off_q(n);
+	std::vector<size_t> off_mask[MAXLEV], off_b[MAXLEV], off_z[MAXLEV], off_z2[MAXLEV];
+	std::vector<size_t> off_U(n), off_x(n), off_p(n), off_q(n), off_p2(n);
 	std::vector<std::vector<int4>> lists(MAXLEV);
 	for (int k = 0; k < n; k++) {
 		const MgProblem &q = probs[k];
@@ -922,6 +1754,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 			off_mask[l].push_back(Lo.take(px));
 			off_b[l].push_back(Lo.take(px * 4));
 			off_z[l].push_back(Lo.take(px * 4));
+			off_z2[l].push_back(Lo.take(px * 4));
 			for (int ty = 0; ty < ntiles(lh[l]); ty++)
 				for (int tx = 0; tx < ntiles(lw[l]); tx++) lists[l].push_back(make_int4(k, tx, ty, 0));
 		}
@@ -929,15 +1762,30 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 			off_mask[l].push_back(0);
 			off_b[l].push_back(0);
 			off_z[l].push_back(0);
+			off_z2[l].push_back(0);
 		}
+		// fused path: the tile kernels cover the levels wider than coarse_max()
+		d.nfine = 0;
+		while (d.nfine < nl - 1 && std::max(lw[d.nfine], lh[d.nfine]) > coarse_max()) d.nfine++;
+		pl.nfine_max = std::max(pl.nfine_max, d.nfine);
+		pl.coarse_smem = std::max(pl.coarse_smem, coarse_layout(lw, lh, d.nfine, nl).bytes);
 		size_t px = (size_t)q.w * q.h;
 		off_U[k] = Lo.take(px * 8);
 		off_x[k] = Lo.take(px * 4);
 		off_p[k] = Lo.take(px * 4);
 		off_q[k] = Lo.take(px * 4);
+		off_p2[k] = Lo.take(px * 4);
 	}
 	if (kinds == 3) return ctx_fail(ctx, SIMPOIS_EINVAL, "a batch mixes 5-point and 13-point problems");
 	const int K = kinds == 2 ? 1 : 0;
+	pl.fused = K == 0 && opt.fused;
+	if (pl.fused) {
+		cudaError_t e = cudaFuncSetAttribute(k_coarse5, cudaFuncAttributeMaxDynamicSharedMemorySize,
+				pl.coarse_smem);
+		if (e != cudaSuccess)
+			return ctx_fail(ctx, SIMPOIS_ECUDA, "coarse kernel shared memory (%d B): %s", pl.coarse_smem,
+					cudaGetErrorString(e));
+	}
 	size_t o_dp = Lo.take(sizeof(ProbDev) * n);
 	size_t o_st = Lo.take(sizeof(ProbState) * n);
 	size_t o_gl = Lo.take(sizeof(Globals));
@@ -983,10 +1831,12 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 		d.x = (float *)(A + off_x[k]);
 		d.p = (float *)(A + off_p[k]);
 		d.q = (float *)(A + off_q[k]);
+		d.p2 = (float *)(A + off_p2[k]);
 		for (int l = 0; l < d.nlev; l++) {
 			d.lv[l].mask = (uint8_t *)(A + off_mask[l][k]);
 			d.lv[l].b = (float *)(A + off_b[l][k]);
 			d.lv[l].z = (float *)(A + off_z[l][k]);
+			d.lv[l].z2 = (float *)(A + off_z2[l][k]);
 		}
 	}
 	pl.dp = (ProbDev *)(A + o_dp);
@@ -1051,14 +1901,36 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 		k_mask_down<<<pl.nall[l], SP_THREADS, 0, s>>>(pl.dp, pl.all[l], l, pl.flag[l]); ++*pl.nl;
 	}
 	k_compact<<<pl.nlev_max, 1024, 0, s>>>(pl.dall, pl.dflag, pl.dnall, pl.dact, pl.dnact, pl.tbeg, pl.tcnt); ++*pl.nl;
+	k_init_counts<<<1, 256, 0, s>>>(pl.dst, pl.tcnt, n, pl.gl); ++*pl.nl;
 	SP_LAUNCH_CHECK(ctx);
 	int *hn = (int *)ctx->pinned;
 	SP_CUDA(ctx, cudaMemcpyAsync(hn, pl.dnact, sizeof(int) * MAXLEV, cudaMemcpyDeviceToHost, s));
 	SP_CUDA(ctx, cudaStreamSynchronize(s));
 	for (int l = 0; l < pl.nlev_max; l++) pl.nact[l] = hn[l];
 
+	KTimer kt;
+	if (opt.ktimer) {
+		kt.ctx = ctx;
+		kt.n = n;
+		kt.active.assign(n, 1);
+		kt.tiles.assign((size_t)MAXLEV * n, 0);
+		kt.coarse_cells.assign(n, 0);
+		for (int l = 0; l < pl.nlev_max; l++) {
+			if (!pl.nact[l]) continue;
+			std::vector<int4> h(pl.nact[l]);
+			SP_CUDA(ctx, cudaMemcpyAsync(h.data(), pl.act[l], sizeof(int4) * h.size(), cudaMemcpyDeviceToHost, s));
+			SP_CUDA(ctx, cudaStreamSynchronize(s));
+			for (const int4 &t : h) kt.tiles[(size_t)l * n + t.x]++;
+		}
+		for (int k = 0; k < n; k++) {
+			const LevelDev &c = pl.hp[k].lv[pl.hp[k].nfine];
+			kt.coarse_cells[k] = c.w * c.h;
+		}
+		pl.kt = &kt;
+	}
 	rc = K == 0 ? run_kind<0>(ctx, pl, opt) : run_kind<1>(ctx, pl, opt);
 	if (rc) return rc;
+	if (pl.kt) kt_collect(ctx, kt);
 
 	if (opt.mode == MG_ADJOINT) {
 		k_adjoint_scatter<<<pl.nall[0], SP_THREADS, 0, s>>>(pl.dp, pl.all[0], pl.gout, pl.gin, pl.gdat); ++*pl.nl;

@@ -30,6 +30,8 @@ struct MgOptions {
 	int max_iter = 500;    // PCG iterations per problem, all refinements
 	int use_mg = 1;        // multigrid preconditioner (0: plain CG)
 	int use_graph = 1;     // capture the PCG iteration in a CUDA graph
+	int fused = 1;         // 5-point: fused V-cycle kernels (0: one launch per sweep)
+	int ktimer = 0;        // time every main-loop launch with CUDA events (no graph)
 	int out_resid = 0;     // FP64 residual of the float output
 	int mode = MG_FILL;
 	// MG_ADJOINT only: grad_out per problem (device), results

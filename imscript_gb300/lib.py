@@ -13,7 +13,7 @@ import threading
 from . import _build
 
 OK, EINVAL, ENOMEM, NOT_CONVERGED, BREAKDOWN, ECUDA, ENODEV, SINGULAR = range(8)
-FLAG_NO_MG, FLAG_NO_GRAPH, FLAG_OUT_RESID = 0x1, 0x2, 0x4
+FLAG_NO_MG, FLAG_NO_GRAPH, FLAG_OUT_RESID, FLAG_UNFUSED, FLAG_KTIMER = 0x1, 0x2, 0x4, 0x8, 0x10
 
 STATUS_NAMES = {OK: "ok", EINVAL: "einval", ENOMEM: "enomem", NOT_CONVERGED: "not_converged",
                 BREAKDOWN: "breakdown", ECUDA: "ecuda", ENODEV: "enodev", SINGULAR: "singular"}
@@ -67,7 +67,8 @@ EXPORTS = [
     "simpois_strerror", "simpois_last_error", "simpois_solve", "simpois_solve_device",
     "simpois_solve_batch", "simpois_residual_device", "simpois_residual_device_noalloc",
     "simpois_adjoint_device",
-    "simpois_launch_count", "simpois_reset_launch_count",
+    "simpois_launch_count", "simpois_reset_launch_count", "simpois_kernel_stats",
+    "simpois_reset_kernel_stats",
     "poisson_solver_separable", "poisson_rec",
 ]
 
@@ -117,6 +118,10 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
         L.simpois_launch_count.restype = ctypes.c_longlong
         L.simpois_reset_launch_count.argtypes = [vp]
         L.simpois_reset_launch_count.restype = None
+        L.simpois_kernel_stats.argtypes = [vp]
+        L.simpois_kernel_stats.restype = ctypes.c_char_p
+        L.simpois_reset_kernel_stats.argtypes = [vp]
+        L.simpois_reset_kernel_stats.restype = None
         L.poisson_solver_separable.argtypes = [vp, vp, vp, ip, ip, ip, fp, ip, ip, fp]
         L.poisson_solver_separable.restype = None
         L.poisson_rec.argtypes = [vp, vp, vp, ip, ip, fp, ip, ip, ip]
@@ -160,6 +165,13 @@ class Context:
 
     def reset_launches(self):
         self._lib.simpois_reset_launch_count(self.handle)
+
+    def kernel_stats(self) -> dict:
+        import json
+        return json.loads(self._lib.simpois_kernel_stats(self.handle).decode())
+
+    def reset_kernel_stats(self):
+        self._lib.simpois_reset_kernel_stats(self.handle)
 
     def last_error(self) -> str:
         return self._lib.simpois_last_error(self.handle).decode()

@@ -70,6 +70,14 @@ typedef struct {
 #define SIMPOIS_FLAG_NO_GRAPH    0x2
 /* compute rel_residual_out (the FP64 residual of the stored float output) */
 #define SIMPOIS_FLAG_OUT_RESID   0x4
+/* converged schedule, 5-point operator: run the multigrid cycle with one
+ * kernel launch per colour sweep instead of the fused tile kernels (same
+ * arithmetic; for testing and comparison) */
+#define SIMPOIS_FLAG_UNFUSED     0x8
+/* converged schedule: time every launch of the main-loop kernels with a pair
+ * of CUDA events on the context's stream (launches are issued eagerly, not
+ * from a CUDA graph); see simpois_kernel_stats */
+#define SIMPOIS_FLAG_KTIMER      0x10
 
 /* Per-channel result record. */
 typedef struct {
@@ -164,6 +172,15 @@ int simpois_adjoint_device(simpois_ctx *ctx, const float *grad_out,
  * and a reset. */
 long long simpois_launch_count(const simpois_ctx *ctx);
 void simpois_reset_launch_count(simpois_ctx *ctx);
+
+/* Instrumentation (no counterpart in the reference): per-kernel totals of the
+ * solves run with SIMPOIS_FLAG_KTIMER, as a JSON object
+ *   {"<kernel>": {"launches": n, "ms": t, "bytes": b}, ...}
+ * where ms sums the CUDA-event durations of the launches and bytes sums their
+ * algorithmic bytes (reads plus writes per active tile pixel).  The string
+ * lives until the next call on the context. */
+const char *simpois_kernel_stats(simpois_ctx *ctx);
+void simpois_reset_kernel_stats(simpois_ctx *ctx);
 
 /* Drop-in replacements with the reference's signatures.  They run on device
  * 0 through a process-wide context and, like the reference, return nothing;

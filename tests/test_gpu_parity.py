@@ -154,6 +154,51 @@ def test_batched_equals_plain_bit_exact(sp):
             k += 1
 
 
+@pytest.mark.parametrize("h,w,pd", [(300, 260, 2), (129, 517, 1)])
+def test_fused_cycle_equals_per_sweep_kernels(sp, h, w, pd):
+    """The fused tile kernels compute what the one-launch-per-sweep kernels
+    compute, bit for bit (images wider than the shared-memory coarse levels)."""
+    from imscript_gb300 import lib, synth
+    rng = np.random.default_rng(h + w)
+    g = np.stack([synth.gaussian_field(rng, h, w, 8) for _ in range(pd)])
+    m = synth.disk_mask(rng, h, w, 0.3, rmin=3, rmax=25)
+    g[:, m] = np.nan
+    f = np.stack([synth.guidance(synth.gaussian_field(rng, h, w, 8))[2] for _ in range(pd)])
+    a, ra = sp.solve(_cuda(g), _cuda(f), rtol=1e-6)
+    b, rb = sp.solve(_cuda(g), _cuda(f), rtol=1e-6, flags=lib.FLAG_UNFUSED)
+    assert [r["iterations"] for r in ra] == [r["iterations"] for r in rb]
+    assert torch.equal(a.view(torch.int32), b.view(torch.int32))
+
+
+def test_kernel_timer_replay_is_identical(sp):
+    """SIMPOIS_FLAG_KTIMER issues the same kernels eagerly with CUDA events
+    around them: same bits as the graph-launched solve, and per-kernel stats."""
+    from imscript_gb300 import lib, synth
+    inst = synth.config1(seed=3, size=300, channels=2)
+    g, f = _cuda(inst.g), _cuda(inst.f)
+    ctx = sp.context(0, torch.cuda.current_stream().cuda_stream)
+    ctx.reset_kernel_stats()
+    a, ra = sp.solve(g, f, rtol=1e-6)
+    b, rb = sp.solve(g, f, rtol=1e-6, flags=lib.FLAG_KTIMER)
+    assert torch.equal(a.view(torch.int32), b.view(torch.int32))
+    st = ctx.kernel_stats()
+    for name in ("k_pre5", "k_post5", "k_coarse5", "k_spmv5", "k_xr", "k_resid64"):
+        assert st[name]["launches"] > 0 and st[name]["ms"] > 0 and st[name]["bytes"] > 0, name
+
+
+def test_fused_small_problems_close_to_per_sweep(sp):
+    """Images no wider than the shared-memory coarse levels: same answer
+    (only the order of one FP64 sum differs)."""
+    from imscript_gb300 import lib
+    rng = np.random.default_rng(4)
+    g, f = _random_case(rng, 100, 120, 0.3, 10, True, 0)
+    a, ra = sp.solve(_cuda(g), _cuda(f), rtol=1e-6)
+    b, rb = sp.solve(_cuda(g), _cuda(f), rtol=1e-6, flags=lib.FLAG_UNFUSED)
+    assert ra[0]["rel_residual"] <= 1e-6 and rb[0]["rel_residual"] <= 1e-6
+    a, b = a.cpu().numpy(), b.cpu().numpy()
+    assert np.abs(a - b).max() <= 1e-5 * np.abs(b).max()
+
+
 def test_all_known_and_all_unknown(sp, oracle_mod):
     rng = np.random.default_rng(1)
     g = rng.standard_normal((1, 20, 30)).astype(np.float32)
