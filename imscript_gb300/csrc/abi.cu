@@ -539,6 +539,26 @@ void poisson_solver_separable(float *out, float *in, float *dat, int w, int h, i
 		memcpy(out, in, sizeof(float) * (size_t)w * h * pd);
 }
 
+void poisson_recursive(float *u, float *g, float *f, int w, int h, float tstep, int niter, int scale)
+{
+	std::lock_guard<std::mutex> lock(g_dropin_mu);
+	int rc = SIMPOIS_OK;
+	if (!g_dropin_ctx) rc = simpois_create(&g_dropin_ctx, 0, nullptr);
+	if (rc == SIMPOIS_OK) {
+		simpois_params p;
+		simpois_default_params(&p);   // this variant reads no smart parameter
+		p.tstep = tstep;
+		p.niter = niter;
+		p.scale = scale;
+		p.flags = SIMPOIS_FLAG_MINI;
+		rc = simpois_solve(g_dropin_ctx, u, g, f, w, h, 1, &p, nullptr);
+	}
+	if (rc != SIMPOIS_OK) {
+		fprintf(stderr, "simpois: %s\n", simpois_strerror(rc));
+		if (u && g && u != g && w > 0 && h > 0) memcpy(u, g, sizeof(float) * (size_t)w * h);
+	}
+}
+
 void poisson_rec(float *u, float *g, float *f, int w, int h, float tstep, int niter, int scale, int cgit)
 {
 	int rc = dropin_solve(u, g, f, w, h, 1, tstep, niter, scale, cgit);

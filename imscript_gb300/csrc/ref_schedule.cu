@@ -110,9 +110,10 @@ __global__ void k_restrict(float *__restrict__ out, int ow, int oh,
 }
 
 // init = bilinear prolongation of the coarse solution (simpois.c:225-239), or
-// 0 at the coarsest level; then u = finite(g) ? g : init (simpois.c:159-160).
+// the nearest-neighbour one of ftr/minisimpois.c:117-124 when `nearest`, or 0
+// at the coarsest level; then u = finite(g) ? g : init (simpois.c:159-160).
 __global__ void k_prolong_init(float *__restrict__ u, const float *__restrict__ g,
-		int ow, int oh, const float *__restrict__ uc, int iw, int ih)
+		int ow, int oh, const float *__restrict__ uc, int iw, int ih, int nearest)
 {
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -120,7 +121,9 @@ __global__ void k_prolong_init(float *__restrict__ u, const float *__restrict__ 
 	if (i >= ow || j >= oh) return;
 	size_t k = (size_t)ow * oh * l + (size_t)ow * j + i;
 	float init = 0.f;
-	if (uc) {
+	if (uc && nearest) {
+		init = fetchc(uc + (size_t)iw * ih * l, iw, ih, i / 2, j / 2);
+	} else if (uc) {
 		const float *src = uc + (size_t)iw * ih * l;
 		float p = __double2float_rn(((double)i - 0.5) / 2);
 		float q = __double2float_rn(((double)j - 0.5) / 2);
@@ -146,7 +149,8 @@ __global__ void k_prolong_init(float *__restrict__ u, const float *__restrict__ 
 
 // One colour class of a Gauss-Seidel sweep, in place (simpois.c:109-118):
 // u[p] += tstep * (op(u)[p] - f[p]) for the NaN pixels p of g in the class.
-// op: 0 = lap_finite, 1 = lap_lap, 2 = lap_lap_lap.
+// op: 0 = lap_finite, 1 = lap_lap, 2 = lap_lap_lap, 3 = lap5 (the plain
+// clamped Laplacian of ftr/minisimpois.c:17-41).
 __global__ void k_gs_class(float *__restrict__ u, const float *__restrict__ g,
 		const float *__restrict__ f, int w, int h, float tstep, int op,
 		int ncol, int cj, int colour)
@@ -161,7 +165,8 @@ __global__ void k_gs_class(float *__restrict__ u, const float *__restrict__ g,
 	if (!isnan(g[off + ij])) return;
 	float *ul = u + off;
 	float lv = op == 0 ? lap_finite(ul, w, h, i, j)
-		: op == 1 ? lap_lap(ul, w, h, i, j) : lap_lap_lap(ul, w, h, i, j);
+		: op == 1 ? lap_lap(ul, w, h, i, j)
+		: op == 2 ? lap_lap_lap(ul, w, h, i, j) : lap5(ul, w, h, i, j);
 	float d = f ? f[off + ij] : 0.f;
 	ul[ij] = __fadd_rn(ul[ij], __fmul_rn(tstep, __fsub_rn(lv, d)));
 }
@@ -600,7 +605,12 @@ int ref_solve(simpois_ctx *ctx, float *out, const float *in, const float *dat, i
 	// operator of the sweeps (simpois.c:96-106)
 	float t = prm->tstep;
 	int op = 0, ncol = 2, cj = 1;
-	if (t < 0) {
+	// the ftr/minisimpois.c variant: plain Laplacian whatever the sign of t,
+	// nearest-neighbour prolongation, no CG branch
+	const bool mini = (prm->flags & SIMPOIS_FLAG_MINI) != 0;
+	if (mini) {
+		op = 3;
+	} else if (t < 0) {
 		op = 1; ncol = 5; cj = 3;
 		if (t < -1000) {
 			t += 1000;
@@ -616,14 +626,15 @@ int ref_solve(simpois_ctx *ctx, float *out, const float *in, const float *dat, i
 		RefLevel &c = lv[k];
 		dim3 G(nblk(c.w, 32), nblk(c.h, 8), pd);
 		k_prolong_init<<<G, B2, 0, s>>>(c.u, c.g, c.w, c.h, k + 1 < nl ? lv[k + 1].u : nullptr,
-				k + 1 < nl ? lv[k + 1].w : 0, k + 1 < nl ? lv[k + 1].h : 0); ctx->launches++;
+				k + 1 < nl ? lv[k + 1].w : 0, k + 1 < nl ? lv[k + 1].h : 0, mini); ctx->launches++;
 		int niter = prm->niter, cgit = prm->cgit;
-		if (prm->ponlit != 0 && prm->ponlit != (double)c.w) niter = cgit = 0;
+		if (!mini && prm->ponlit != 0 && prm->ponlit != (double)c.w) niter = cgit = 0;
 		for (int it = 0; it < niter; it++)
 			for (int col = 0; col < ncol; col++) {
 				k_gs_class<<<G, B2, 0, s>>>(c.u, c.g, c.f, c.w, c.h, t, op, ncol, cj, col); ctx->launches++;
 			}
 		SP_LAUNCH_CHECK(ctx);
+		if (mini) continue;
 		bool poisson = cgit && prm->tstep > 0;
 		int maxit = cgit;
 		// float cg_maxit = maxit == -1 ? nmask : maxit; a non-positive cap runs

@@ -14,6 +14,7 @@ from . import _build
 
 OK, EINVAL, ENOMEM, NOT_CONVERGED, BREAKDOWN, ECUDA, ENODEV, SINGULAR = range(8)
 FLAG_NO_MG, FLAG_NO_GRAPH, FLAG_OUT_RESID, FLAG_UNFUSED, FLAG_KTIMER = 0x1, 0x2, 0x4, 0x8, 0x10
+FLAG_MINI = 0x20
 
 STATUS_NAMES = {OK: "ok", EINVAL: "einval", ENOMEM: "enomem", NOT_CONVERGED: "not_converged",
                 BREAKDOWN: "breakdown", ECUDA: "ecuda", ENODEV: "enodev", SINGULAR: "singular"}
@@ -69,7 +70,7 @@ EXPORTS = [
     "simpois_adjoint_device",
     "simpois_launch_count", "simpois_reset_launch_count", "simpois_kernel_stats",
     "simpois_reset_kernel_stats",
-    "poisson_solver_separable", "poisson_rec",
+    "poisson_solver_separable", "poisson_rec", "poisson_recursive",
 ]
 
 _lib = None
@@ -126,6 +127,8 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
         L.poisson_solver_separable.restype = None
         L.poisson_rec.argtypes = [vp, vp, vp, ip, ip, fp, ip, ip, ip]
         L.poisson_rec.restype = None
+        L.poisson_recursive.argtypes = [vp, vp, vp, ip, ip, fp, ip, ip]
+        L.poisson_recursive.restype = None
         _lib = L
         return L
 

@@ -78,6 +78,10 @@ typedef struct {
  * of CUDA events on the context's stream (launches are issued eagerly, not
  * from a CUDA graph); see simpois_kernel_stats */
 #define SIMPOIS_FLAG_KTIMER      0x10
+/* reference schedule: the GS-only variant the ftr viewers use
+ * (ftr/minisimpois.c:127-162): the plain clamped Laplacian for every tstep,
+ * nearest-neighbour prolongation, no CG branch */
+#define SIMPOIS_FLAG_MINI        0x20
 
 /* Per-channel result record. */
 typedef struct {
@@ -193,6 +197,12 @@ void poisson_solver_separable(float *out, float *in, float *dat, int w, int h,
 		int pd, float tstep, int niter, int scale, float cgrad);
 void poisson_rec(float *u, float *g, float *f, int w, int h, float tstep,
 		int niter, int scale, int cgit);
+
+/* Drop-in for poisson_recursive of the ftr viewers (ftr/minisimpois.c:127-149,
+ * called in place by ftr/vnav.c:855,893): one channel, the GS-only pyramid of
+ * SIMPOIS_FLAG_MINI; u may alias g. */
+void poisson_recursive(float *u, float *g, float *f, int w, int h, float tstep,
+		int niter, int scale);
 
 #ifdef __cplusplus
 }

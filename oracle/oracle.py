@@ -31,6 +31,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle_simpois.so")
 REF_BIN = os.path.join(HERE, "_ref", "simpois")
+MINI_BIN = os.path.join(HERE, "_ref", "minisimpois")
 
 ORDER = {"raster": 0, "colour": 1}
 
@@ -85,6 +86,8 @@ def lib() -> ctypes.CDLL:
                                           ctypes.c_int, op, ctypes.POINTER(ctypes.c_double)]
         L.oracle_cg_extension.restype = ctypes.c_int
         L.oracle_apply_mask.argtypes = [fp, fp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.oracle_poisson_recursive.argtypes = [fp, fp, fp, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                               ctypes.c_int, ctypes.c_int, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -121,6 +124,18 @@ def poisson_solver_separable(inp, dat=None, tstep=0.25, niter=10, scale=99, cgra
     lib().oracle_poisson_solver_separable(_fptr(out), _fptr(g), _fptr(f), w, h, pd,
                                           float(tstep), int(niter), int(scale), float(cgrad),
                                           ctypes.byref(o))
+    return out
+
+
+def poisson_recursive(inp, dat=None, tstep=0.45, niter=10, scale=99, order="raster"):
+    """Restatement of ftr/minisimpois.c:127-162 (GS only) on planar input."""
+    g = _planar(inp, "inp")
+    pd, h, w = g.shape
+    f = None if dat is None else _planar(dat, "dat")
+    out = np.empty_like(g)
+    for l in range(pd):
+        lib().oracle_poisson_recursive(_fptr(out[l]), _fptr(g[l]), None if f is None else _fptr(f[l]),
+                                       w, h, float(tstep), int(niter), int(scale), ORDER[order])
     return out
 
 
@@ -203,12 +218,13 @@ def from_hwc(a):
 
 
 def run_reference(inp=None, dat=None, mask=None, args=(), env=None, timeout=600,
-                  input_via_stdin=False):
+                  input_via_stdin=False, binary=None):
     """Run the reference binary on planar inputs; returns the planar output."""
-    if not have_reference():
-        raise FileNotFoundError(REF_BIN)
+    binary = binary or REF_BIN
+    if not os.path.isfile(binary):
+        raise FileNotFoundError(binary)
     with tempfile.TemporaryDirectory() as td:
-        cmd = [REF_BIN]
+        cmd = [binary]
         stdin = None
         if inp is not None:
             p = os.path.join(td, "in.npy")

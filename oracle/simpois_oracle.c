@@ -384,6 +384,67 @@ static void cg_extension(float *out, cg_op A, const float *in, const float *dat,
 	free(bd); free(sol); free(x0); free(idx); free(inv); free(b);
 }
 
+/* ---- the GS-only variant of ftr/minisimpois.c ------------------------------
+ * poisson_recursive (ftr/minisimpois.c:127-149): the same octave pyramid, with
+ * the plain clamped Laplacian for every tstep (ftr/minisimpois.c:17-41), the
+ * nearest-neighbour prolongation (ftr/minisimpois.c:117-124), fs *= 3 and no
+ * CG branch.  In place (u == g) works: g is read before u is written.        */
+
+static void gs_sweep_plain(float *u, const float *f, int w, int h, const int *omega, int n_omega,
+		float tstep, int order)
+{
+	for (int c = 0; c < (order == ORACLE_ORDER_RASTER ? 1 : 2); c++)
+		for (int p = 0; p < n_omega; p++) {
+			int ij = omega[p];
+			int i = ij % w, j = ij / w;
+			if (order != ORACLE_ORDER_RASTER && ((i + j) & 1) != c) continue;
+			float l = lap5(u, w, h, i, j);
+			float d = f ? f[ij] : 0;
+			u[ij] = u[ij] + tstep * (l - d);
+		}
+}
+
+static void prolong_nearest(float *out, int ow, int oh, const float *in, int iw, int ih)
+{
+	for (int j = 0; j < oh; j++)
+	for (int i = 0; i < ow; i++)
+		out[ow * j + i] = fetch(in, iw, ih, i / 2, j / 2);
+}
+
+static void mini_level(float *u, const float *g, const float *f, int w, int h, float tstep,
+		int niter, int scale, int order)
+{
+	float *init = ora_alloc(sizeof(float) * (size_t)w * h);
+	for (int k = 0; k < w * h; k++) init[k] = 0;
+	if (scale > 1 && (w > 1 || h > 1)) {
+		int ws = ceil(w / 2.0);
+		int hs = ceil(h / 2.0);
+		float *gs = ora_alloc(sizeof(float) * (size_t)ws * hs);
+		float *fs = f ? ora_alloc(sizeof(float) * (size_t)ws * hs) : NULL;
+		float *us = ora_alloc(sizeof(float) * (size_t)ws * hs);
+		restrict2(gs, ws, hs, g, w, h);
+		restrict2(fs, ws, hs, f, w, h);
+		if (f) for (int k = 0; k < ws * hs; k++) fs[k] *= 3;
+		mini_level(us, gs, fs, ws, hs, tstep, niter, scale - 1, order);
+		prolong_nearest(init, w, h, us, ws, hs);
+		free(gs); free(fs); free(us);
+	}
+	int n;
+	int *omega = nan_list(&n, g, w, h);
+	for (int k = 0; k < w * h; k++)
+		u[k] = isfinite(g[k]) ? g[k] : init[k];
+	for (int it = 0; it < niter; it++)
+		gs_sweep_plain(u, f, w, h, omega, n, tstep, order);
+	free(omega);
+	free(init);
+}
+
+void oracle_poisson_recursive(float *u, const float *g, const float *f, int w, int h,
+		float tstep, int niter, int scale, int order)
+{
+	mini_level(u, g, f, w, h, tstep, niter, scale, order);
+}
+
 /* ---- recursion and channel loop (simpois.c:247-302) ----------------------- */
 
 static void rec_level(float *u, const float *g, const float *f, int w, int h,

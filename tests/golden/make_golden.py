@@ -211,6 +211,19 @@ def io_cases():
     return len(res)
 
 
+def mini_cases(rng):
+    """The GS-only copy of the ftr viewers (ftr/minisimpois.c) from its own main."""
+    k = 0
+    for (pd, h, w) in [(1, 13, 17), (2, 20, 9), (1, 1, 25), (1, 24, 24)]:
+        for a in (["-t", "0.25"], ["-t", "0.45", "-n", "25", "-s", "3"], ["-t", "0.2", "-n", "4", "-s", "1"]):
+            g = noisy(rng, pd, h, w, 0.35)
+            f = (rng.standard_normal(g.shape) * 0.05).astype(np.float32) if k % 2 else None
+            out = O.run_reference(g, f, args=a, binary=O.MINI_BIN)
+            save(f"mini_{k:03d}", g, f, args=a, out=out)
+            k += 1
+    return k
+
+
 def main():
     if not O.have_reference():
         O.build(reference=True)
@@ -219,8 +232,9 @@ def main():
     n2 = conv_cases(rng)
     n3 = cli_cases()
     n4 = io_cases()
-    print(f"wrote {n1} pin cases, {n2} converged cases, {n3} CLI cases and {n4} I/O cases "
-          f"into {OUT}")
+    n5 = mini_cases(np.random.default_rng(4242))
+    print(f"wrote {n1} pin cases, {n2} converged cases, {n3} CLI cases, {n4} I/O cases and "
+          f"{n5} minisimpois cases into {OUT}")
 
 
 if __name__ == "__main__":

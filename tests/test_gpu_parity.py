@@ -238,3 +238,30 @@ def test_dropin_symbol_matches_oracle(sp, oracle_mod):
                                ctypes.c_float(0.25), 25, 99, ctypes.c_float(0))
     want = oracle_mod.poisson_solver_separable(g, None, niter=25, order="colour")
     assert np.array_equal(_bits(out), _bits(want))
+
+
+@pytest.mark.parametrize("path", cases("mini_"), ids=lambda p: p.rsplit("/", 1)[-1][:-4])
+def test_minisimpois_variant_matches_colour_oracle(sp, oracle_mod, path):
+    """The ftr viewers' GS-only pyramid (SIMPOIS_FLAG_MINI), bit for bit."""
+    from imscript_gb300 import lib
+    from test_oracle_golden import _mini_kw
+    d = load(path)
+    kw = _mini_kw(d["args"])
+    want = oracle_mod.poisson_recursive(d["g"], d["f"], order="colour", **kw)
+    got, _ = sp.poisson_solver_separable(_cuda(d["g"]), None if d["f"] is None else _cuda(d["f"]),
+                                         kw["tstep"], kw["niter"], kw["scale"], 0, flags=lib.FLAG_MINI)
+    assert np.array_equal(_bits(got.cpu().numpy()), _bits(want))
+
+
+def test_poisson_recursive_dropin_in_place(sp, oracle_mod):
+    """poisson_recursive(strip, strip, 0, w, h, 0.25, 10, 99) as ftr/vnav.c:855 calls it."""
+    import ctypes
+    from imscript_gb300 import lib
+    rng = np.random.default_rng(12)
+    g = rng.standard_normal((40, 33)).astype(np.float32)
+    g[rng.random((40, 33)) < 0.3] = np.nan
+    want = oracle_mod.poisson_recursive(g, None, 0.25, 10, 99, order="colour")[0]
+    strip = g.copy()
+    lib.load().poisson_recursive(strip.ctypes.data, strip.ctypes.data, None, 33, 40,
+                                 ctypes.c_float(0.25), 10, 99)
+    assert np.array_equal(_bits(strip), _bits(want))

@@ -58,3 +58,18 @@ def test_live_reference_matches_oracle_random(oracle_mod):
         ref = oracle_mod.run_reference(g, args=args)
         out = oracle_mod.poisson_solver_separable(g, **{k2: v for k2, v in parse_args(args, {}).items()})
         assert np.array_equal(ref.view(np.uint32), out.view(np.uint32))
+
+
+def _mini_kw(args):
+    opt = {"t": "0.45", "n": "10", "s": "99"}
+    for k in range(0, len(args), 2):
+        opt[args[k][1:]] = args[k + 1]
+    return dict(tstep=float(np.float32(float(opt["t"]))), niter=int(float(opt["n"])),
+                scale=int(float(opt["s"])))
+
+
+@pytest.mark.parametrize("path", cases("mini_"), ids=lambda p: p.rsplit("/", 1)[-1][:-4])
+def test_oracle_reproduces_minisimpois_bit_exact(oracle_mod, path):
+    d = load(path)
+    out = oracle_mod.poisson_recursive(d["g"], d["f"], order="raster", **_mini_kw(d["args"]))
+    assert np.array_equal(out.view(np.uint32), d["out"].view(np.uint32))
