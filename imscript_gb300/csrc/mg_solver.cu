@@ -49,7 +49,8 @@ constexpr int COARSE_SWEEPS = 10;   // symmetric sweeps on the coarsest level
 constexpr int NU5 = 2;              // pre- and post-smoothing sweeps, 5-point
 constexpr int NU13 = 4;             // pre- and post-smoothing sweeps, 13-point
 constexpr int MAX_OUTER = 8;        // FP64 refinement steps
-constexpr int INNER_MAX = 60;       // PCG iterations per refinement step
+constexpr int INNER_MAX = 60;       // PCG iterations per refinement step (5-point)
+constexpr int INNER_MAX13 = 600;    // the same for the FP64 13-point PCG
 constexpr double TAU_MIN = 2e-6;    // FP32 inner solve: smallest relative decrease
 
 struct LevelDev {
@@ -73,6 +74,7 @@ struct ProbDev {
 	double *U;           // FP64 solution image (g or 0 at the known pixels)
 	float *x, *p, *q;    // level-0 PCG vectors
 	float *p2;           // fused path: second search-direction buffer
+	double *r64, *p64, *q64;   // 13-point: FP64 Krylov vectors (else null)
 	double rtol;
 	LevelDev lv[MAXLEV];
 };
@@ -370,8 +372,12 @@ __global__ void k_resid64(const ProbDev *__restrict__ P, ProbState *st, const in
 			if (L.mask[k]) {
 				double s = pr.rhs ? (double)pr.rhs_sign * (double)pr.rhs[k] : 0.0;
 				double rk = s - apply64<K>(pr.U, L.mask, pr.w, pr.h, i, j, false);
-				L.b[k] = (float)rk;
-				pr.x[k] = 0.f;
+				if (pr.r64) {
+					pr.r64[k] = rk;     // the FP64 PCG starts from this residual
+				} else {
+					L.b[k] = (float)rk;
+					pr.x[k] = 0.f;
+				}
 				rr += rk * rk;
 				if (first) {
 					double bk = s - apply64<K>(pr.U, L.mask, pr.w, pr.h, i, j, true);
@@ -399,7 +405,8 @@ __global__ void k_resid64(const ProbDev *__restrict__ P, ProbState *st, const in
 			s.outer += 1;
 			s.iter = 0;
 			s.inner_active = 1;
-			double tau = fmax(0.3 * pr.rtol / rel, TAU_MIN);
+			// an FP32 inner solve stalls near TAU_MIN; the FP64 one goes to rtol
+			double tau = pr.r64 ? 0.5 * pr.rtol / rel : fmax(0.3 * pr.rtol / rel, TAU_MIN);
 			s.tau2 = tau * tau * tot[0];
 			s.rho = 0;
 			s.beta = 0;
@@ -890,7 +897,7 @@ __global__ void __launch_bounds__(SP_THREADS) k_pre5(const ProbDev *__restrict__
 // PCG scalars beta, rho (the last tile of the problem to finish).
 __global__ void __launch_bounds__(SP_THREADS) k_post5(const ProbDev *__restrict__ P, ProbState *st,
 		const int4 *__restrict__ tl, int l, const int *__restrict__ tbeg, const int *__restrict__ tcnt,
-		double *partial, Globals *gl)
+		double *partial, Globals *gl, int pcg)
 {
 	__shared__ float sb[FN], sz[FN];
 	__shared__ uint8_t sm[FN];
@@ -940,7 +947,7 @@ __global__ void __launch_bounds__(SP_THREADS) k_post5(const ProbDev *__restrict_
 			if (sm[rc]) rz += (double)sb[rc] * (double)sz[rc];
 		}
 	}
-	if (l != 0) return;
+	if (l != 0 || !pcg) return;
 	double tot[2];
 	if (problem_sum1(rz, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
 		ProbState &s = st[prob];
@@ -1000,7 +1007,8 @@ __device__ __forceinline__ void smem_sweep5(float *z, const float *b, const uint
 // kernels, with the coarsest level (<= 4 x 4) getting COARSE_SWEEPS symmetric
 // sweeps.  Reads b of level nfine, writes z2 of level nfine.  When nfine == 0
 // (a problem no larger than coarse_max()) it also forms r.z and the PCG scalars.
-__global__ void __launch_bounds__(1024) k_coarse5(const ProbDev *__restrict__ P, ProbState *st, Globals *gl)
+__global__ void __launch_bounds__(1024) k_coarse5(const ProbDev *__restrict__ P, ProbState *st, Globals *gl,
+		int pcg)
 {
 	extern __shared__ __align__(16) unsigned char smem[];
 	__shared__ double sh[32];
@@ -1089,7 +1097,7 @@ __global__ void __launch_bounds__(1024) k_coarse5(const ProbDev *__restrict__ P,
 		pr.lv[c0].z2[c] = m[c] ? z[c] : 0.f;
 		if (m[c]) rz += (double)b[c] * (double)z[c];
 	}
-	if (c0 != 0) return;
+	if (c0 != 0 || !pcg) return;
 	rz = block_sum<1024>(rz, sh);
 	if (threadIdx.x == 0) {
 		ProbState &s = st[prob];
@@ -1163,6 +1171,165 @@ __global__ void __launch_bounds__(SP_THREADS) k_spmv5(const ProbDev *__restrict_
 			atomicSub(&gl->inner_count, 1);
 		} else {
 			s.alpha = a;
+		}
+	}
+}
+
+// ------------------------------------------------------------------ 13-point PCG in FP64
+//
+// The biharmonic system needs FP64 Krylov vectors: for a hole d pixels wide
+// the smoothest mode has eigenvalue ~(pi/d)^4 (1e-10 for d = 1024), far below
+// the FP32 rounding of the 13-point sum (~64 * 6e-8), so an FP32 A p cannot
+// see the components that converge last.  The preconditioner stays in FP32:
+// away from the image border the masked 13-point operator is L^2 + B B^T, with
+// L the masked 5-point -Laplacian and B B^T >= 0 the coupling through known
+// pixels, so two symmetric 5-point V-cycles (V V ~ L^-2) precondition it;
+// the coarse grids resolve the smooth modes that FP32 cannot see on the fine
+// one.
+
+#define TILE_LOOP_UNKNOWN(pr, t, body)                                      \
+	{                                                                   \
+		const int i_ = tile_i(t);                                   \
+		for (int r_ = 0; r_ < SP_ROWS; r_++) {                      \
+			const int j_ = tile_j(t, r_);                       \
+			if (i_ < (pr).w && j_ < (pr).h) {                   \
+				const size_t k = (size_t)j_ * (pr).w + i_;  \
+				if ((pr).lv[0].mask[k]) { body }            \
+			}                                                   \
+		}                                                           \
+	}
+
+// b0 = (float) r64: the first V-cycle's right-hand side
+__global__ void k_cast_r(const ProbDev *__restrict__ P, const ProbState *__restrict__ st, const int4 *__restrict__ tl)
+{
+	const int4 t = tl[blockIdx.x];
+	if (!st[t.x].inner_active) return;
+	const ProbDev &pr = P[t.x];
+	TILE_LOOP_UNKNOWN(pr, t, pr.lv[0].b[k] = (float)pr.r64[k];)
+}
+
+// b0 = z2_0: the second V-cycle's right-hand side
+__global__ void k_z2_to_b(const ProbDev *__restrict__ P, const ProbState *__restrict__ st, const int4 *__restrict__ tl)
+{
+	const int4 t = tl[blockIdx.x];
+	if (!st[t.x].inner_active) return;
+	const ProbDev &pr = P[t.x];
+	TILE_LOOP_UNKNOWN(pr, t, pr.lv[0].b[k] = pr.lv[0].z2[k];)
+}
+
+// rho = r64 . z; beta = rho / rho_old (0 on the first iteration)
+__global__ void k_rz64(const ProbDev *__restrict__ P, ProbState *st, const int4 *__restrict__ tl,
+		const int *__restrict__ tbeg, const int *__restrict__ tcnt, double *partial, Globals *gl)
+{
+	__shared__ double sh[32];
+	const int4 t = tl[blockIdx.x];
+	const int prob = t.x;
+	if (!st[prob].inner_active) return;
+	const ProbDev &pr = P[prob];
+	double rz = 0;
+	TILE_LOOP_UNKNOWN(pr, t, rz += pr.r64[k] * (double)pr.lv[0].z2[k];)
+	double tot[2];
+	if (problem_sum1(rz, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
+		ProbState &s = st[prob];
+		if (!(tot[0] > 0) || !isfinite(tot[0])) {
+			if (tot[0] != 0) s.status = SIMPOIS_BREAKDOWN;
+			s.inner_active = 0;
+			atomicSub(&gl->inner_count, 1);
+		} else {
+			s.beta = s.rho > 0 ? tot[0] / s.rho : 0.0;
+			s.rho = tot[0];
+		}
+	}
+}
+
+// p64 = z + beta p64
+__global__ void k_pupd64(const ProbDev *__restrict__ P, const ProbState *__restrict__ st, const int4 *__restrict__ tl)
+{
+	const int4 t = tl[blockIdx.x];
+	if (!st[t.x].inner_active) return;
+	const ProbDev &pr = P[t.x];
+	const double beta = st[t.x].beta;
+	TILE_LOOP_UNKNOWN(pr, t, {
+		const double z = (double)pr.lv[0].z2[k];
+		pr.p64[k] = beta != 0 ? z + beta * pr.p64[k] : z;
+	})
+}
+
+// q64 = A p64 with the 13-point clamped operator in FP64; alpha = rho / (p.q)
+__global__ void k_spmv64(const ProbDev *__restrict__ P, ProbState *st, const int4 *__restrict__ tl,
+		const int *__restrict__ tbeg, const int *__restrict__ tcnt, double *partial, Globals *gl)
+{
+	__shared__ double sh[32];
+	const int4 t = tl[blockIdx.x];
+	const int prob = t.x;
+	if (!st[prob].inner_active) return;
+	const ProbDev &pr = P[prob];
+	const uint8_t *m = pr.lv[0].mask;
+	const int w = pr.w, h = pr.h;
+	double pq = 0;
+	const int i = tile_i(t);
+	for (int r = 0; r < SP_ROWS; r++) {
+		const int j = tile_j(t, r);
+		if (i >= w || j >= h) continue;
+		const size_t k = (size_t)j * w + i;
+		if (!m[k]) continue;
+		double diag = 20.0, off = 0.0;
+#pragma unroll
+		for (int s2 = 0; s2 < 12; s2++) {
+			const int qi = clampi(i + c_di13[s2], w), qj = clampi(j + c_dj13[s2], h);
+			if (qi == i && qj == j) {
+				diag += c_cf13[s2];
+			} else {
+				const size_t q = (size_t)qj * w + qi;
+				if (m[q]) off += (double)c_cf13[s2] * pr.p64[q];
+			}
+		}
+		const double pk = pr.p64[k];
+		const double qk = diag * pk + off;
+		pr.q64[k] = qk;
+		pq += pk * qk;
+	}
+	double tot[2];
+	if (problem_sum1(pq, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
+		ProbState &s = st[prob];
+		const double a = s.rho / tot[0];
+		if (!(tot[0] > 0) || !isfinite(a)) {
+			s.status = SIMPOIS_BREAKDOWN;
+			s.inner_active = 0;
+			s.alpha = 0;
+			atomicSub(&gl->inner_count, 1);
+		} else {
+			s.alpha = a;
+		}
+	}
+}
+
+// U += alpha p64 (the FP64 solution itself); r64 -= alpha q64; r.r; stop test
+__global__ void k_xr64(const ProbDev *__restrict__ P, ProbState *st, const int4 *__restrict__ tl,
+		const int *__restrict__ tbeg, const int *__restrict__ tcnt, double *partial, Globals *gl)
+{
+	__shared__ double sh[32];
+	const int4 t = tl[blockIdx.x];
+	const int prob = t.x;
+	if (!st[prob].inner_active) return;
+	const ProbDev &pr = P[prob];
+	const double a = st[prob].alpha;
+	double rr = 0;
+	TILE_LOOP_UNKNOWN(pr, t, {
+		pr.U[k] += a * pr.p64[k];
+		const double rk = pr.r64[k] - a * pr.q64[k];
+		pr.r64[k] = rk;
+		rr += rk * rk;
+	})
+	double tot[2];
+	if (problem_sum1(rr, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
+		ProbState &s = st[prob];
+		s.rr = tot[0];
+		s.iter += 1;
+		s.total_iter += 1;
+		if (tot[0] <= s.tau2 || s.iter >= INNER_MAX13 || s.total_iter >= s.max_iter) {
+			s.inner_active = 0;
+			atomicSub(&gl->inner_count, 1);
 		}
 	}
 }
@@ -1432,7 +1599,9 @@ void kt_refresh(const Plan &pl, cudaStream_t s)
 	for (int p = 0; p < pl.n; p++) pl.kt->active[p] = h[p].inner_active != 0;
 }
 
-void launch_vcycle_fused(const Plan &pl, cudaStream_t s)
+// pcg = 0: the cycle is half of the biharmonic preconditioner and leaves the
+// 5-point PCG scalars alone.
+void launch_vcycle_fused(const Plan &pl, cudaStream_t s, int pcg = 1)
 {
 	kt_refresh(pl, s);
 	for (int l = 0; l < pl.nfine_max; l++) {
@@ -1443,16 +1612,44 @@ void launch_vcycle_fused(const Plan &pl, cudaStream_t s)
 	}
 	{
 		KT_BEGIN(pl, s);
-		k_coarse5<<<pl.n, 1024, pl.coarse_smem, s>>>(pl.dp, pl.dst, pl.gl); ++*pl.nl;
+		k_coarse5<<<pl.n, 1024, pl.coarse_smem, s>>>(pl.dp, pl.dst, pl.gl, pcg); ++*pl.nl;
 		KT_END(pl, s, "k_coarse5", pl.kt->cells() * BPC_COARSE5);
 	}
 	for (int l = pl.nfine_max - 1; l >= 0; l--) {
 		if (!pl.nact[l]) continue;
 		KT_BEGIN(pl, s);
 		k_post5<<<pl.nact[l], SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[l], l, pl.tbeg, pl.tcnt, pl.partial,
-				pl.gl); ++*pl.nl;
+				pl.gl, pcg); ++*pl.nl;
 		KT_END(pl, s, "k_post5", pl.kt->px(l) * BPX_POST5);
 	}
+}
+
+// Biharmonic preconditioner: z = V(V(r)) with V the fused 5-point V-cycle,
+// then rho = r . z and beta.
+void launch_precond_bih(const Plan &pl, cudaStream_t s)
+{
+	const int nt = pl.nact[0];
+	k_cast_r<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0]); ++*pl.nl;
+	launch_vcycle_fused(pl, s, 0);
+	k_z2_to_b<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0]); ++*pl.nl;
+	launch_vcycle_fused(pl, s, 0);
+	k_rz64<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl); ++*pl.nl;
+}
+
+// One FP64 biharmonic PCG iteration.
+void launch_iteration_bih(const Plan &pl, cudaStream_t s)
+{
+	const int nt = pl.nact[0];
+	kt_refresh(pl, s);
+	k_pupd64<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0]); ++*pl.nl;
+	{
+		KT_BEGIN(pl, s);
+		k_spmv64<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl);
+		++*pl.nl;
+		KT_END(pl, s, "k_spmv64", pl.kt->px(0) * (1 + 8 + 8));
+	}
+	k_xr64<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl); ++*pl.nl;
+	launch_precond_bih(pl, s);
 }
 
 // Two fused PCG iterations (the search direction alternates between p and p2).
@@ -1477,8 +1674,10 @@ void launch_iteration_fused(const Plan &pl, cudaStream_t s)
 	}
 }
 
+enum { MODE_PLAIN = 0, MODE_FUSED5 = 1, MODE_BIH64 = 2 };
+
 // Signature of everything a solve graph bakes into its kernel parameters.
-std::string plan_signature(const simpois_ctx *ctx, const Plan &pl, int K, bool fused, const MgOptions &opt)
+std::string plan_signature(const simpois_ctx *ctx, const Plan &pl, int K, int fused, const MgOptions &opt)
 {
 	std::string sig;
 	char buf[96];
@@ -1502,7 +1701,7 @@ std::string plan_signature(const simpois_ctx *ctx, const Plan &pl, int K, bool f
 // caps the kernels enforce.  Returns cudaErrorNotSupported-like failures to
 // the caller, which then drives the loops from the host.
 template <int K>
-cudaError_t build_solve_graph(simpois_ctx *ctx, Plan &pl, const MgOptions &opt, bool fused)
+cudaError_t build_solve_graph(simpois_ctx *ctx, Plan &pl, const MgOptions &opt, int mode)
 {
 	cudaStream_t cs = ctx->capture_stream;
 	const int nt = pl.nact[0];
@@ -1529,13 +1728,16 @@ cudaError_t build_solve_graph(simpois_ctx *ctx, Plan &pl, const MgOptions &opt, 
 		long long c0 = *pl.nl;
 		k_resid64<K><<<nt, SP_THREADS, 0, cs>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl);
 		++*pl.nl;
-		if (fused) {
+		if (mode == MODE_FUSED5) {
 			launch_vcycle_fused(pl, cs);
+		} else if (mode == MODE_BIH64) {
+			launch_precond_bih(pl, cs);
 		} else {
 			launch_precond<K>(pl, opt, cs);
 			k_rz<<<nt, SP_THREADS, 0, cs>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl); ++*pl.nl;
 		}
-		k_setcond<<<1, 32, 0, cs>>>(hi, pl.gl, 0, 1, 4 * INNER_MAX); ++*pl.nl;
+		const int gmax_inner = mode == MODE_BIH64 ? INNER_MAX13 + 4 : 4 * INNER_MAX;
+		k_setcond<<<1, 32, 0, cs>>>(hi, pl.gl, 0, 1, gmax_inner); ++*pl.nl;
 		cudaStreamCaptureStatus cst;
 		cudaGraph_t cg;
 		const cudaGraphNode_t *deps = nullptr;
@@ -1549,7 +1751,9 @@ cudaError_t build_solve_graph(simpois_ctx *ctx, Plan &pl, const MgOptions &opt, 
 		if (ce == cudaSuccess) ce = cudaGraphAddNode(&node_i, cg, deps, nullptr, ndeps, &pi);
 		if (ce == cudaSuccess) ce = cudaStreamUpdateCaptureDependencies(cs, &node_i, nullptr, 1,
 				cudaStreamSetCaptureDependencies);
-		k_uadd<<<nt, SP_THREADS, 0, cs>>>(pl.dp, pl.dst, pl.act[0]); ++*pl.nl;
+		if (mode != MODE_BIH64) {   // the FP64 biharmonic PCG updates U itself
+			k_uadd<<<nt, SP_THREADS, 0, cs>>>(pl.dp, pl.dst, pl.act[0]); ++*pl.nl;
+		}
 		k_setcond<<<1, 32, 0, cs>>>(ho, pl.gl, 1, 0, MAX_OUTER + 2); ++*pl.nl;
 		n_outer = *pl.nl - c0;
 		e = cudaStreamEndCapture(cs, &body_o);
@@ -1560,11 +1764,13 @@ cudaError_t build_solve_graph(simpois_ctx *ctx, Plan &pl, const MgOptions &opt, 
 		if ((e = cudaStreamBeginCaptureToGraph(cs, body_i, nullptr, nullptr, 0,
 				cudaStreamCaptureModeThreadLocal)) != cudaSuccess) break;
 		c0 = *pl.nl;
-		if (fused)
+		if (mode == MODE_FUSED5)
 			launch_iteration_fused(pl, cs);
+		else if (mode == MODE_BIH64)
+			launch_iteration_bih(pl, cs);
 		else
 			launch_iteration<K>(pl, opt, cs);
-		k_setcond<<<1, 32, 0, cs>>>(hi, pl.gl, 0, 0, 4 * INNER_MAX); ++*pl.nl;
+		k_setcond<<<1, 32, 0, cs>>>(hi, pl.gl, 0, 0, gmax_inner); ++*pl.nl;
 		n_inner = *pl.nl - c0;
 		if ((e = cudaStreamEndCapture(cs, &body_i)) != cudaSuccess) break;
 		cudaGraphExec_t ex = nullptr;
@@ -1582,13 +1788,13 @@ cudaError_t build_solve_graph(simpois_ctx *ctx, Plan &pl, const MgOptions &opt, 
 
 // The converged solve as one graph launch and one synchronisation.
 template <int K>
-int run_device_loop(simpois_ctx *ctx, Plan &pl, const MgOptions &opt, bool fused, bool *done)
+int run_device_loop(simpois_ctx *ctx, Plan &pl, const MgOptions &opt, int mode, bool *done)
 {
 	*done = false;
-	const std::string sig = plan_signature(ctx, pl, K, fused, opt);
+	const std::string sig = plan_signature(ctx, pl, K, mode, opt);
 	if (!ctx->solve_exec || ctx->solve_sig != sig) {
 		ctx->solve_sig.clear();
-		if (build_solve_graph<K>(ctx, pl, opt, fused) != cudaSuccess) return SIMPOIS_OK;  // host loop instead
+		if (build_solve_graph<K>(ctx, pl, opt, mode) != cudaSuccess) return SIMPOIS_OK;  // host loop instead
 		ctx->solve_sig = sig;
 	}
 	cudaStream_t s = ctx->stream;
@@ -1608,15 +1814,20 @@ int run_kind(simpois_ctx *ctx, Plan &pl, const MgOptions &opt)
 	int *hcount = (int *)ctx->pinned;
 	const int nt = pl.nact[0];
 	if (nt == 0) return SIMPOIS_OK;
-	const bool fused = K == 0 && pl.fused && opt.use_mg;
+	// MODE_FUSED5: 5-point, fused V-cycle; MODE_BIH64: 13-point FP64 PCG with
+	// the squared 5-point V-cycle; MODE_PLAIN: per-sweep kernels (or no MG)
+	const int mode = !opt.use_mg || !pl.fused ? MODE_PLAIN : (K == 0 ? MODE_FUSED5 : MODE_BIH64);
+	const bool fused = mode == MODE_FUSED5;
 	if (opt.use_graph && !pl.kt && !verbose()) {
 		bool done = false;
-		int r = run_device_loop<K>(ctx, pl, opt, fused, &done);
+		int r = run_device_loop<K>(ctx, pl, opt, mode, &done);
 		if (r != SIMPOIS_OK || done) return r;
 	}
 	auto iteration = [&](cudaStream_t st) {
 		if (fused)
 			launch_iteration_fused(pl, st);
+		else if (mode == MODE_BIH64)
+			launch_iteration_bih(pl, st);
 		else
 			launch_iteration<K>(pl, opt, st);
 	};
@@ -1650,6 +1861,8 @@ int run_kind(simpois_ctx *ctx, Plan &pl, const MgOptions &opt)
 		}
 		if (fused) {
 			launch_vcycle_fused(pl, s);
+		} else if (mode == MODE_BIH64) {
+			launch_precond_bih(pl, s);
 		} else {
 			launch_precond<K>(pl, opt, s);
 			k_rz<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl); ++*pl.nl;
@@ -1667,7 +1880,7 @@ int run_kind(simpois_ctx *ctx, Plan &pl, const MgOptions &opt)
 		}
 		if (*hcount == 0) break;
 		int chunk = 4;
-		for (int guard = 0; guard < 4 * INNER_MAX; guard++) {
+		for (int guard = 0; guard < 4 * INNER_MAX13; guard++) {
 			for (int c = 0; c < chunk; c++) {
 				if (gexec) {
 					e = cudaGraphLaunch(gexec, s);
@@ -1690,7 +1903,7 @@ int run_kind(simpois_ctx *ctx, Plan &pl, const MgOptions &opt)
 			cudaStreamSynchronize(s);
 			for (int p = 0; p < pl.n; p++) pl.kt->active[p] = h[p].outer_active != 0;
 		}
-		{
+		if (mode != MODE_BIH64) {
 			KT_BEGIN(pl, s);
 			k_uadd<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0]); ++*pl.nl;
 			KT_END(pl, s, "k_uadd", pl.kt->px(0) * BPX_UADD);
@@ -1733,6 +1946,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	Layout Lo;
 	std::vector<size_t> off_mask[MAXLEV], off_b[MAXLEV], off_z[MAXLEV], off_z2[MAXLEV];
 	std::vector<size_t> off_U(n), off_x(n), off_p(n), off_q(n), off_p2(n);
+	std::vector<size_t> off_r64(n, 0), off_p64(n, 0), off_q64(n, 0);
 	std::vector<std::vector<int4>> lists(MAXLEV);
 	for (int k = 0; k < n; k++) {
 		const MgProblem &q = probs[k];
@@ -1775,10 +1989,15 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 		off_p[k] = Lo.take(px * 4);
 		off_q[k] = Lo.take(px * 4);
 		off_p2[k] = Lo.take(px * 4);
+		if (q.kind == 1 && opt.fused && opt.use_mg) {   // FP64 Krylov vectors of the biharmonic PCG
+			off_r64[k] = Lo.take(px * 8);
+			off_p64[k] = Lo.take(px * 8);
+			off_q64[k] = Lo.take(px * 8);
+		}
 	}
 	if (kinds == 3) return ctx_fail(ctx, SIMPOIS_EINVAL, "a batch mixes 5-point and 13-point problems");
 	const int K = kinds == 2 ? 1 : 0;
-	pl.fused = K == 0 && opt.fused;
+	pl.fused = opt.fused;   // 13-point problems use the 5-point cycle as preconditioner
 	if (pl.fused) {
 		cudaError_t e = cudaFuncSetAttribute(k_coarse5, cudaFuncAttributeMaxDynamicSharedMemorySize,
 				pl.coarse_smem);
@@ -1832,6 +2051,9 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 		d.p = (float *)(A + off_p[k]);
 		d.q = (float *)(A + off_q[k]);
 		d.p2 = (float *)(A + off_p2[k]);
+		d.r64 = off_r64[k] ? (double *)(A + off_r64[k]) : nullptr;
+		d.p64 = off_p64[k] ? (double *)(A + off_p64[k]) : nullptr;
+		d.q64 = off_q64[k] ? (double *)(A + off_q64[k]) : nullptr;
 		for (int l = 0; l < d.nlev; l++) {
 			d.lv[l].mask = (uint8_t *)(A + off_mask[l][k]);
 			d.lv[l].b = (float *)(A + off_b[l][k]);
