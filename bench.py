@@ -179,6 +179,50 @@ def cpu_baseline(insts, budget_s=20.0):
                       f"to FP64 relative residual 1e-6, one crop per thread; {dt:.1f} s"}
 
 
+# ------------------------------------------------------------------ differentiation
+
+def run_diff(args):
+    """32 x 1024^2 guided Poisson fills: forward (converged fill) and backward
+    (adjoint solve + scatter) through the torch.autograd.Function, timed with
+    CUDA events; reports forward filled Mpx/s and the bwd/fwd time ratio."""
+    import torch
+    from imscript_gb300 import autograd as ag, synth
+    n = 32 if args.size == 0 else max(1, args.size)
+    insts, targets, guid = synth.config4(seed=0, n=n)
+    dev = torch.device("cuda", 0)
+    base = torch.stack([torch.from_numpy(np.nan_to_num(i.g[0], nan=0.0)) for i in insts]).to(dev)
+    mask = torch.stack([torch.from_numpy(np.isnan(i.g[0])) for i in insts]).to(dev)
+    gx = torch.stack([torch.from_numpy(x) for x, _ in guid]).to(dev)
+    gy = torch.stack([torch.from_numpy(y) for _, y in guid]).to(dev)
+    tgt = torch.stack([torch.from_numpy(t) for t in targets]).to(dev)
+    unknowns = int(mask.sum().item())
+    stream = torch.cuda.current_stream(dev)
+    fwd_ms, bwd_ms = [], []
+    for it in range(args.warmup + args.steps):
+        img = base.clone().requires_grad_(True)
+        Gx = gx.clone().requires_grad_(True)
+        Gy = gy.clone().requires_grad_(True)
+        g = torch.where(mask, torch.full_like(img, float("nan")), img)
+        f = ag.divergence(Gx, Gy)
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        torch.cuda.synchronize()
+        e0.record(stream)
+        u = ag.fill(g, f, rtol=1e-6)
+        e1.record(stream)
+        loss = 0.5 * ((u - tgt) ** 2).mean()
+        loss.backward()
+        e2.record(stream)
+        torch.cuda.synchronize()
+        if it >= args.warmup:
+            fwd_ms.append(e0.elapsed_time(e1))
+            bwd_ms.append(e1.elapsed_time(e2))
+    f_ms, b_ms = sum(fwd_ms) / len(fwd_ms), sum(bwd_ms) / len(bwd_ms)
+    print(json.dumps({"workload": f"differentiation {n}x1024x1024 guided Poisson (MSE loss)",
+                      "forward_ms": f_ms, "backward_ms": b_ms, "bwd_fwd_ratio": b_ms / f_ms,
+                      "forward_filled_mpx_s": unknowns / (f_ms / 1e3) / 1e6,
+                      "unknown_samples": unknowns, "steps": args.steps, "warmup": args.warmup}))
+
+
 # ------------------------------------------------------------------ GPU arm
 
 def run_ours(args):
@@ -195,7 +239,16 @@ def run_ours(args):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
 
-    insts, wname = make_workload(args.workload, rank)
+    from imscript_gb300 import dist as sdist
+    if args.shard and world > 1:
+        # one batch partitioned across the ranks (strong scaling), no collective
+        # on the data path
+        insts, wname = make_workload(args.workload, 0)
+        insts = sdist.shard(insts, [i.unknowns for i in insts], rank, world)
+        wname += f" sharded over {world} ranks"
+    else:
+        # every rank solves its own seeded copy of the workload (weak scaling)
+        insts, wname = make_workload(args.workload, rank)
     unknowns = sum(i.unknowns for i in insts)
     gs = [torch.from_numpy(i.g).to(dev) for i in insts]
     fs = [None if i.f is None else torch.from_numpy(i.f).to(dev) for i in insts]
@@ -250,11 +303,9 @@ def run_ours(args):
     launches = ctx.launches()
     bad = [r for r in reps if r["status"] not in (splib.OK,)]
     worst = max(r["rel_residual"] for r in reps)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = unknowns * world * args.steps / (ms / 1e3) / 1e6
+    ms = sdist.max_over_ranks(ms, device=dev)
+    total_unknowns = sdist.sum_over_ranks(unknowns, device=dev)
+    value = total_unknowns * args.steps / (ms / 1e3) / 1e6
     if args.quick:
         if rank == 0:
             print(json.dumps({"value": value, "ms_per_step": ms / args.steps, "gpu_launches": launches,
@@ -333,13 +384,13 @@ def run_ours(args):
         "warmup": args.warmup,
         "ms_per_step": ms / args.steps,
         "higher_is_better": True,
-        "scaling": "weak",
+        "scaling": "strong" if (args.shard and world > 1) else "weak",
         "vs_baseline": None,
         "dtype": "f32 (FP64 refinement and reductions)",
         "data": "synthetic (seeded; shapes and distributions of the benchmark workload)",
         "config": {"workload": wname, "unknown_samples_per_step": unknowns, "rtol": rtol,
                    "l2": "flushed between timed steps (512 MiB write)",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+                   "parallelism": ("shards" if args.shard else "replicas") if world > 1 else "single GPU"},
         "plain": {"value": round(value_plain, 3), "unit": "filled Mpx/s",
                   "ms_per_step": ms_plain / args.steps,
                   "batched_over_plain": round(value / world / value_plain, 3)},
@@ -399,11 +450,16 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="c1")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--size", type=int, default=0, help="c4: number of images (default 32)")
+    ap.add_argument("--shard", action="store_true",
+                    help="N>1: partition one batch across the ranks instead of one copy per rank")
     ap.add_argument("--quick", action="store_true",
                     help="batched solves only, short JSON (for profiling runs)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "c4":
+        run_diff(args)
     else:
         run_ours(args)
 

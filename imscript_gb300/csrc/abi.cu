@@ -159,7 +159,10 @@ int run_converged(simpois_ctx *ctx, const simpois_image *im, int n, const simpoi
 	MgOptions opt;
 	opt.max_iter = p->max_iter > 0 ? p->max_iter : 500;
 	opt.use_mg = !(p->flags & SIMPOIS_FLAG_NO_MG);
-	opt.use_graph = !(p->flags & SIMPOIS_FLAG_NO_GRAPH);
+	// SIMPOIS_NO_GRAPH=1 issues every kernel eagerly (profilers cannot see
+	// into graphs with conditional nodes); the kernels and results are the same
+	const char *ng = getenv("SIMPOIS_NO_GRAPH");
+	opt.use_graph = !(p->flags & SIMPOIS_FLAG_NO_GRAPH) && !(ng && atoi(ng) > 0);
 	opt.out_resid = (p->flags & SIMPOIS_FLAG_OUT_RESID) != 0;
 	opt.fused = !(p->flags & SIMPOIS_FLAG_UNFUSED);
 	opt.ktimer = (p->flags & SIMPOIS_FLAG_KTIMER) != 0;
