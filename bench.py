@@ -307,9 +307,15 @@ def run_ours(args):
     total_unknowns = sdist.sum_over_ranks(unknowns, device=dev)
     value = total_unknowns * args.steps / (ms / 1e3) / 1e6
     if args.quick:
+        line = {"value": value, "ms_per_step": ms / args.steps, "gpu_launches": launches,
+                "iterations": [r["iterations"] for r in reps], "max_rel": worst}
+        if args.with_plain:
+            step_plain()
+            ms_p, _ = timed(step_plain, args.steps)
+            line["plain_value"] = unknowns * args.steps / (ms_p / 1e3) / 1e6
+            line["batched_over_plain"] = value / line["plain_value"]
         if rank == 0:
-            print(json.dumps({"value": value, "ms_per_step": ms / args.steps, "gpu_launches": launches,
-                              "iterations": [r["iterations"] for r in reps], "max_rel": worst}))
+            print(json.dumps(line))
         return
 
     # kernel roofline: one more step of the same workload on the same stream,
@@ -453,6 +459,7 @@ def main():
     ap.add_argument("--size", type=int, default=0, help="c4: number of images (default 32)")
     ap.add_argument("--shard", action="store_true",
                     help="N>1: partition one batch across the ranks instead of one copy per rank")
+    ap.add_argument("--with-plain", action="store_true", help="--quick: also time one image per call")
     ap.add_argument("--quick", action="store_true",
                     help="batched solves only, short JSON (for profiling runs)")
     args = ap.parse_args()

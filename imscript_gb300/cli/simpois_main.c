@@ -202,4 +202,8 @@ int main_simpois(int argc, char *argv[])
 	return wr ? 1 : 0;
 }
 
+/* the im multi-tool compiles every tool with HIDE_ALL_MAINS and dispatches
+ * to main_simpois itself (src/im.c, src/all_mains.inc) */
+#ifndef HIDE_ALL_MAINS
 int main(int c, char **v) { return main_simpois(c, v); }
+#endif
