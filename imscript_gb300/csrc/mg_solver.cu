@@ -23,7 +23,7 @@
 //     so the cycle is a symmetric operator when A is;
 //   * restriction sums the children's residuals (times 2 for the 13-point
 //     operator), prolongation injects the coarse correction into the unknown
-//     children; the coarsest level (<= 4 x 4) gets 10 symmetric sweeps.
+//     children; the coarsest level (<= 4 x 4) gets 4 symmetric sweeps.
 //
 // Batching.  All problems of a call share every launch: each level keeps one
 // list of 32 x 32 tiles that contain unknowns, over all problems.  Every
@@ -45,13 +45,13 @@ namespace {
 
 constexpr int MAXLEV = 16;
 constexpr int COARSE_MAX = 4;       // coarsest level: max(w, h) <= 4
-constexpr int COARSE_SWEEPS = 10;   // symmetric sweeps on the coarsest level
+constexpr int COARSE_SWEEPS = 4;    // symmetric sweeps on the coarsest level (<= 4 x 4)
 constexpr int NU5 = 2;              // pre- and post-smoothing sweeps, 5-point
 constexpr int NU13 = 4;             // pre- and post-smoothing sweeps, 13-point
 constexpr int MAX_OUTER = 8;        // FP64 refinement steps
 constexpr int INNER_MAX = 60;       // PCG iterations per refinement step (5-point)
 constexpr int INNER_MAX13 = 600;    // the same for the FP64 13-point PCG
-constexpr double TAU_MIN = 2e-6;    // FP32 inner solve: smallest relative decrease
+constexpr double TAU_MIN = 5e-7;    // FP32 inner solve: smallest relative decrease (measured: one refinement step fewer than 2e-6 on 2048^2 x 3)
 
 struct LevelDev {
 	int w, h;
@@ -75,6 +75,7 @@ struct ProbDev {
 	float *x, *p, *q;    // level-0 PCG vectors
 	float *p2;           // fused path: second search-direction buffer
 	double *r64, *p64, *q64;   // 13-point: FP64 Krylov vectors (else null)
+	double tau_min;            // FP32 inner solve: smallest relative decrease
 	double rtol;
 	LevelDev lv[MAXLEV];
 };
@@ -363,33 +364,46 @@ __global__ void k_resid64(const ProbDev *__restrict__ P, ProbState *st, const in
 	const bool first = st[prob].outer == 0;
 	const ProbDev &pr = P[prob];
 	const LevelDev &L = pr.lv[0];
-	int i = tile_i(t);
-	double rr = 0, bb = 0;
+	const int i = tile_i(t), w = pr.w, h = pr.h;
+	double rr = 0;
+	// U is 0 at every unknown until the first refinement step adds to it, so
+	// there b = rhs - A_UK g_K is exactly this residual: ||b|| = ||r||.
+#pragma unroll
 	for (int r = 0; r < SP_ROWS; r++) {
-		int j = tile_j(t, r);
-		if (i < pr.w && j < pr.h) {
-			size_t k = (size_t)j * pr.w + i;
-			if (L.mask[k]) {
-				double s = pr.rhs ? (double)pr.rhs_sign * (double)pr.rhs[k] : 0.0;
-				double rk = s - apply64<K>(pr.U, L.mask, pr.w, pr.h, i, j, false);
-				if (pr.r64) {
-					pr.r64[k] = rk;     // the FP64 PCG starts from this residual
-				} else {
-					L.b[k] = (float)rk;
-					pr.x[k] = 0.f;
-				}
-				rr += rk * rk;
-				if (first) {
-					double bk = s - apply64<K>(pr.U, L.mask, pr.w, pr.h, i, j, true);
-					bb += bk * bk;
-				}
+		const int j = tile_j(t, r);
+		const bool in = i < w && j < h;
+		const size_t k = in ? (size_t)j * w + i : 0;
+		const uint8_t m = in ? L.mask[k] : 0;
+		double rk = 0;
+		if (K == 0) {
+			// the five loads do not depend on the mask: all in flight together
+			const int ie = i + 1 < w ? i + 1 : i, iw = i > 0 ? i - 1 : i;
+			const int js = j + 1 < h ? j + 1 : j, jn = j > 0 ? j - 1 : j;
+			const double uc = in ? pr.U[k] : 0.0;
+			const double ue = in ? pr.U[(size_t)j * w + ie] : 0.0;
+			const double us = in ? pr.U[(size_t)js * w + i] : 0.0;
+			const double uw = in ? pr.U[(size_t)j * w + iw] : 0.0;
+			const double un = in ? pr.U[(size_t)jn * w + i] : 0.0;
+			const double s = (in && pr.rhs) ? (double)pr.rhs_sign * (double)pr.rhs[k] : 0.0;
+			rk = s - (4.0 * uc - ue - us - uw - un);
+		} else if (m) {
+			const double s = pr.rhs ? (double)pr.rhs_sign * (double)pr.rhs[k] : 0.0;
+			rk = s - apply64<K>(pr.U, L.mask, w, h, i, j, false);
+		}
+		if (m) {
+			if (pr.r64) {
+				pr.r64[k] = rk;     // the FP64 PCG starts from this residual
+			} else {
+				L.b[k] = (float)rk;
+				pr.x[k] = 0.f;
 			}
+			rr += rk * rk;
 		}
 	}
 	double tot[2];
-	if (problem_sum2(rr, bb, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
+	if (problem_sum1(rr, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
 		ProbState &s = st[prob];
-		if (first) s.bnorm2 = tot[1];
+		if (first) s.bnorm2 = tot[0];
 		if (first && s.nknown == 0) s.status = SIMPOIS_SINGULAR;
 		double rel = s.bnorm2 > 0 ? sqrt(tot[0] / s.bnorm2) : 0.0;
 		if (first) s.rel_first = rel;
@@ -406,7 +420,7 @@ __global__ void k_resid64(const ProbDev *__restrict__ P, ProbState *st, const in
 			s.iter = 0;
 			s.inner_active = 1;
 			// an FP32 inner solve stalls near TAU_MIN; the FP64 one goes to rtol
-			double tau = pr.r64 ? 0.5 * pr.rtol / rel : fmax(0.3 * pr.rtol / rel, TAU_MIN);
+			double tau = pr.r64 ? 0.5 * pr.rtol / rel : fmax(0.3 * pr.rtol / rel, pr.tau_min);
 			s.tau2 = tau * tau * tot[0];
 			s.rho = 0;
 			s.beta = 0;
@@ -777,6 +791,18 @@ constexpr int FN = FR * FR;
 // Levels with max(w, h) <= coarse_max() run in k_coarse5, one block per
 // problem.  Default 64 (measured best on 2048^2 x 3 against 32 and 128);
 // SIMPOIS_COARSE_MAX (8..128) overrides it.
+// FP32 inner solves stop at this relative decrease at the latest (the FP32
+// recurrence drifts below it); SIMPOIS_TAU_MIN overrides it for tuning.
+double tau_min()
+{
+	static double v = [] {
+		const char *e = getenv("SIMPOIS_TAU_MIN");
+		double x = e ? atof(e) : TAU_MIN;
+		return x > 0 ? x : TAU_MIN;
+	}();
+	return v;
+}
+
 // SIMPOIS_VERBOSE=1: print each refinement step's residual to stderr
 bool verbose()
 {
@@ -823,20 +849,106 @@ __device__ __forceinline__ float az5_cell(const float *z, const uint8_t *m, int 
 	return diag * z[c] + off;
 }
 
+// Per-cell code of a shared region cell: bit 0 unknown; bits 1-4 the E, W, S,
+// N neighbour is in the image, unknown and inside the region; bits 5-7 the
+// number of clamped sides (the 5-point diagonal is 4 minus it).
+__device__ __forceinline__ uint8_t region_code(const uint8_t *sm, int c, int rx, int ry, int gi, int gj, int w,
+		int h)
+{
+	if (!sm[c]) return 0;
+	int code = 1, nd = 0;
+	if (gi + 1 < w) { if (rx + 1 < FR && sm[c + 1]) code |= 2; } else nd++;
+	if (gi > 0)     { if (rx > 0 && sm[c - 1]) code |= 4; } else nd++;
+	if (gj + 1 < h) { if (ry + 1 < FR && sm[c + FR]) code |= 8; } else nd++;
+	if (gj > 0)     { if (ry > 0 && sm[c - FR]) code |= 16; } else nd++;
+	return (uint8_t)(code | (nd << 5));
+}
+
+// The off-diagonal sum of split<0> from a cell code (same operations, same
+// order: E, W, S, N).
+__device__ __forceinline__ float off_code(const float *z, int c, int R, int code)
+{
+	float off = 0.f;
+	if (code & 2) off -= z[c + 1];
+	if (code & 4) off -= z[c - 1];
+	if (code & 8) off -= z[c + R];
+	if (code & 16) off -= z[c - R];
+	return off;
+}
+
+__device__ __forceinline__ float diag_code(int code) { return 4.f - (float)(code >> 5); }
+
+// The colour cells of the 40x40 region a thread owns: for colour col, cell
+// q = tid + 256 k (k < 4, q < 800) of the compacted class, packed as
+// (region index) | (ring << 11); ring = distance to the region's edge.
+__device__ __forceinline__ void own_cells(int x0, int y0, int cells[2][4])
+{
+#pragma unroll
+	for (int col = 0; col < 2; col++)
+#pragma unroll
+		for (int k = 0; k < 4; k++) {
+			const int q = threadIdx.x + SP_THREADS * k;
+			if (q >= FN / 2) { cells[col][k] = -1; continue; }
+			const int ry = q / (FR / 2);
+			const int rx = 2 * (q - ry * (FR / 2)) + ((col ^ (x0 + y0 + ry)) & 1);
+			const int ring = min(min(rx, ry), min(FR - 1 - rx, FR - 1 - ry));
+			cells[col][k] = (ry * FR + rx) | (ring << 11);
+		}
+}
+
+// Half-sweep of colour col over the cells with ring >= lo.
+__device__ __forceinline__ void sweep_cells(float *sz, const float *sb, const uint8_t *sc, const int cells[2][4],
+		int col, int lo)
+{
+#pragma unroll
+	for (int k = 0; k < 4; k++) {
+		const int e = cells[col][k];
+		if (e < 0 || (e >> 11) < lo) continue;
+		const int c = e & 2047;
+		const int code = sc[c];
+		if (!(code & 1)) continue;
+		const float off = off_code(sz, c, FR, code);
+		sz[c] = gs_div(sb[c] - off, diag_code(code));
+	}
+}
+
 // Pre-smoothing from z = 0 (NU5 forward red-black sweeps), residual, and its
 // restriction (sum over the children) into b of level l+1.  Writes z of level
 // l (the pre-smoothed correction).
 __global__ void __launch_bounds__(SP_THREADS) k_pre5(const ProbDev *__restrict__ P, const ProbState *__restrict__ st,
 		const int4 *__restrict__ tl, int l)
 {
-	__shared__ float sb[FN], sz[FN];
-	__shared__ uint8_t sm[FN];
+	__shared__ __align__(16) float sb[FN], sz[FN];
+	__shared__ __align__(16) uint8_t sm[FN], sc[FN];
 	const int4 t = tl[blockIdx.x];
 	const ProbDev &pr = P[t.x];
 	if (!st[t.x].inner_active || l >= pr.nfine) return;
 	const LevelDev L = pr.lv[l];
 	const int x0 = t.y * SP_TILE - FH, y0 = t.z * SP_TILE - FH;
 	// every load depends only on the coordinates, so all are in flight at once
+	if ((L.w & 3) == 0) {
+		// groups of 4 cells of a row (aligned, wholly inside or outside)
+#pragma unroll
+		for (int it = 0; it < (FN / 4 + SP_THREADS - 1) / SP_THREADS; it++) {
+			const int f = threadIdx.x + it * SP_THREADS;
+			if (f < FN / 4) {
+				const int ry = f / (FR / 4), rx = 4 * (f - ry * (FR / 4)), gi = x0 + rx, gj = y0 + ry;
+				const bool in = gi >= 0 && gi < L.w && gj >= 0 && gj < L.h;
+				const size_t k = in ? (size_t)gj * L.w + gi : 0;
+				uchar4 m = make_uchar4(0, 0, 0, 0);
+				float4 bv = make_float4(0.f, 0.f, 0.f, 0.f);
+				if (in) {
+					m = *(const uchar4 *)(L.mask + k);
+					bv = *(const float4 *)(L.b + k);
+				}
+				const int c = ry * FR + rx;
+				*(uchar4 *)(sm + c) = m;
+				*(float4 *)(sb + c) = make_float4(m.x ? bv.x : 0.f, m.y ? bv.y : 0.f, m.z ? bv.z : 0.f,
+						m.w ? bv.w : 0.f);
+				*(float4 *)(sz + c) = make_float4(0.f, 0.f, 0.f, 0.f);
+			}
+		}
+	} else
 #pragma unroll
 	for (int it = 0; it < (FN + SP_THREADS - 1) / SP_THREADS; it++) {
 		const int c = threadIdx.x + it * SP_THREADS;
@@ -851,23 +963,22 @@ __global__ void __launch_bounds__(SP_THREADS) k_pre5(const ProbDev *__restrict__
 			sz[c] = 0.f;
 		}
 	}
+	int cells[2][4];
+	own_cells(x0, y0, cells);
 	__syncthreads();
-	// half-sweep s updates colour s&1 on the region [s, FR-s)^2; at s = 0 the
-	// neighbours are all 0, so the outermost ring needs no outside value
-	for (int s = 0; s < 2 * NU5; s++) {
-		const int colour = s & 1, lo = s, hi = FR - s;
-		for (int q = threadIdx.x; q < FN / 2; q += SP_THREADS) {
-			const int ry = q / (FR / 2);
-			const int rx = 2 * (q - ry * (FR / 2)) + ((colour ^ (x0 + y0 + ry)) & 1);
-			const int c = ry * FR + rx, gi = x0 + rx, gj = y0 + ry;
-			if (rx < lo || rx >= hi || ry < lo || ry >= hi || !sm[c]) continue;
-			if (s == 0) {
-				float diag = 4.f - (gi + 1 >= L.w) - (gi <= 0) - (gj + 1 >= L.h) - (gj <= 0);
-				sz[c] = gs_div(sb[c] - 0.f, diag);
-			} else {
-				gs5_cell(sz, sb, sm, c, FR, gi, gj, L.w, L.h);
-			}
+#pragma unroll
+	for (int it = 0; it < (FN + SP_THREADS - 1) / SP_THREADS; it++) {
+		const int c = threadIdx.x + it * SP_THREADS;
+		if (c < FN) {
+			const int ry = c / FR, rx = c - ry * FR;
+			sc[c] = region_code(sm, c, rx, ry, x0 + rx, y0 + ry, L.w, L.h);
 		}
+	}
+	__syncthreads();
+	// half-sweep s updates colour s&1 on the cells of ring >= s; at s = 0 every
+	// neighbour is 0, so the outermost ring needs no outside value
+	for (int s = 0; s < 2 * NU5; s++) {
+		sweep_cells(sz, sb, sc, cells, s & 1, s);
 		__syncthreads();
 	}
 	// write the pre-smoothed correction of the tile
@@ -885,7 +996,8 @@ __global__ void __launch_bounds__(SP_THREADS) k_pre5(const ProbDev *__restrict__
 				const int fi = 2 * ci + aa, fj = 2 * cj + bb;
 				if (fi < L.w && fj < L.h) {
 					const int c = (fj - y0) * FR + (fi - x0);
-					acc += sb[c] - az5_cell(sz, sm, c, FR, fi, fj, L.w, L.h);
+					const int code = sc[c];
+					acc += sb[c] - (diag_code(code) * sz[c] + off_code(sz, c, FR, code));
 				}
 			}
 		C.b[(size_t)cj * C.w + ci] = 1.f * acc;
@@ -899,8 +1011,8 @@ __global__ void __launch_bounds__(SP_THREADS) k_post5(const ProbDev *__restrict_
 		const int4 *__restrict__ tl, int l, const int *__restrict__ tbeg, const int *__restrict__ tcnt,
 		double *partial, Globals *gl, int pcg)
 {
-	__shared__ float sb[FN], sz[FN];
-	__shared__ uint8_t sm[FN];
+	__shared__ __align__(16) float sb[FN], sz[FN];
+	__shared__ __align__(16) uint8_t sm[FN], sc[FN];
 	__shared__ double sh[32];
 	const int4 t = tl[blockIdx.x];
 	const int prob = t.x;
@@ -908,6 +1020,39 @@ __global__ void __launch_bounds__(SP_THREADS) k_post5(const ProbDev *__restrict_
 	if (!st[prob].inner_active || l >= pr.nfine) return;
 	const LevelDev L = pr.lv[l], C = pr.lv[l + 1];
 	const int x0 = t.y * SP_TILE - FH, y0 = t.z * SP_TILE - FH;
+	if ((L.w & 3) == 0) {
+		// groups of 4 cells of a row: with w % 4 == 0 (and x0 % 4 == 0) a group
+		// is wholly inside or outside the image and every access is aligned
+#pragma unroll
+		for (int it = 0; it < (FN / 4 + SP_THREADS - 1) / SP_THREADS; it++) {
+			const int f = threadIdx.x + it * SP_THREADS;
+			if (f < FN / 4) {
+				const int ry = f / (FR / 4), rx = 4 * (f - ry * (FR / 4)), gi = x0 + rx, gj = y0 + ry;
+				const bool in = gi >= 0 && gi < L.w && gj >= 0 && gj < L.h;
+				const size_t k = in ? (size_t)gj * L.w + gi : 0;
+				const size_t kc = in ? (size_t)(gj >> 1) * C.w + (gi >> 1) : 0;
+				uchar4 m = make_uchar4(0, 0, 0, 0);
+				float4 bv = make_float4(0.f, 0.f, 0.f, 0.f), zv = bv;
+				float2 cz = make_float2(0.f, 0.f);
+				uint8_t cm0 = 0, cm1 = 0;
+				if (in) {
+					m = *(const uchar4 *)(L.mask + k);
+					bv = *(const float4 *)(L.b + k);
+					zv = *(const float4 *)(L.z + k);
+					cz = *(const float2 *)(C.z2 + kc);
+					cm0 = C.mask[kc];
+					cm1 = C.mask[kc + 1];
+				}
+				const int c = ry * FR + rx;
+				*(uchar4 *)(sm + c) = m;
+				*(float4 *)(sb + c) = make_float4(m.x ? bv.x : 0.f, m.y ? bv.y : 0.f, m.z ? bv.z : 0.f,
+						m.w ? bv.w : 0.f);
+				*(float4 *)(sz + c) = make_float4(m.x ? (cm0 ? zv.x + cz.x : zv.x) : 0.f,
+						m.y ? (cm0 ? zv.y + cz.x : zv.y) : 0.f, m.z ? (cm1 ? zv.z + cz.y : zv.z) : 0.f,
+						m.w ? (cm1 ? zv.w + cz.y : zv.w) : 0.f);
+			}
+		}
+	} else
 #pragma unroll
 	for (int it = 0; it < (FN + SP_THREADS - 1) / SP_THREADS; it++) {
 		const int c = threadIdx.x + it * SP_THREADS;
@@ -926,16 +1071,21 @@ __global__ void __launch_bounds__(SP_THREADS) k_post5(const ProbDev *__restrict_
 			sz[c] = m ? (cm ? zv + cz : zv) : 0.f;
 		}
 	}
+	int cells[2][4];
+	own_cells(x0, y0, cells);
 	__syncthreads();
-	for (int s = 0; s < 2 * NU5; s++) {
-		const int colour = 1 - (s & 1), lo = s + 1, hi = FR - s - 1;
-		for (int q = threadIdx.x; q < FN / 2; q += SP_THREADS) {
-			const int ry = q / (FR / 2);
-			const int rx = 2 * (q - ry * (FR / 2)) + ((colour ^ (x0 + y0 + ry)) & 1);
-			const int c = ry * FR + rx, gi = x0 + rx, gj = y0 + ry;
-			if (rx < lo || rx >= hi || ry < lo || ry >= hi || !sm[c]) continue;
-			gs5_cell(sz, sb, sm, c, FR, gi, gj, L.w, L.h);
+#pragma unroll
+	for (int it = 0; it < (FN + SP_THREADS - 1) / SP_THREADS; it++) {
+		const int c = threadIdx.x + it * SP_THREADS;
+		if (c < FN) {
+			const int ry = c / FR, rx = c - ry * FR;
+			sc[c] = region_code(sm, c, rx, ry, x0 + rx, y0 + ry, L.w, L.h);
 		}
+	}
+	__syncthreads();
+	// half-sweep s updates colour 1 - (s&1) on the cells of ring >= s + 1
+	for (int s = 0; s < 2 * NU5; s++) {
+		sweep_cells(sz, sb, sc, cells, 1 - (s & 1), s + 1);
 		__syncthreads();
 	}
 	double rz = 0;
@@ -1002,12 +1152,87 @@ __device__ __forceinline__ void smem_sweep5(float *z, const float *b, const uint
 	__syncthreads();
 }
 
+// The same half-sweep done by one warp (levels of at most 256 cells).
+__device__ __forceinline__ void warp_sweep5(float *z, const float *b, const uint8_t *m, int w, int h, int colour)
+{
+	const int lane = threadIdx.x & 31, hw = (w + 1) >> 1;
+	if (w <= 16) {
+		// 8 half-columns x 4 rows of lanes: no division in the loop
+		const int i = 2 * (lane & 7);
+		for (int j = lane >> 3; j < h; j += 4) {
+			const int ic = i + ((colour ^ j) & 1);
+			const int c = j * w + ic;
+			if (ic < w && m[c]) gs5_cell(z, b, m, c, w, ic, j, w, h);
+		}
+	} else {
+		for (int q = lane; q < hw * h; q += 32) {
+			const int j = q / hw, i = 2 * (q - j * hw) + ((colour ^ j) & 1);
+			const int c = j * w + i;
+			if (i < w && m[c]) gs5_cell(z, b, m, c, w, i, j, w, h);
+		}
+	}
+	__syncwarp();
+}
+
+// Levels l0 .. L-1 of the cycle by warp 0 alone (all of them hold at most 256
+// cells): the same sweeps, restriction and injection as the block-wide code,
+// synchronised with __syncwarp instead of block barriers.
+__device__ void warp_vcycle5(float *const *Z, float *const *B, const uint8_t *const *M, const int *lw,
+		const int *lh, int l0, int L)
+{
+	const int lane = threadIdx.x & 31;
+	for (int l = l0; l + 1 < L; l++) {
+		for (int s = 0; s < NU5; s++) {
+			warp_sweep5(Z[l], B[l], M[l], lw[l], lh[l], 0);
+			warp_sweep5(Z[l], B[l], M[l], lw[l], lh[l], 1);
+		}
+		const int wc = lw[l + 1], hc = lh[l + 1];
+		for (int c = lane; c < wc * hc; c += 32) {
+			const int cj = c / wc, ci = c - cj * wc;
+			if (!M[l + 1][c]) continue;
+			float acc = 0.f;
+			for (int bb = 0; bb < 2; bb++)
+				for (int aa = 0; aa < 2; aa++) {
+					const int fi = 2 * ci + aa, fj = 2 * cj + bb;
+					if (fi < lw[l] && fj < lh[l]) {
+						const int f = fj * lw[l] + fi;
+						acc += B[l][f] - az5_cell(Z[l], M[l], f, lw[l], fi, fj, lw[l], lh[l]);
+					}
+				}
+			B[l + 1][c] = 1.f * acc;
+		}
+		__syncwarp();
+	}
+	{
+		const int l = L - 1;
+		for (int s = 0; s < COARSE_SWEEPS; s++) {
+			warp_sweep5(Z[l], B[l], M[l], lw[l], lh[l], 0);
+			warp_sweep5(Z[l], B[l], M[l], lw[l], lh[l], 1);
+			warp_sweep5(Z[l], B[l], M[l], lw[l], lh[l], 1);
+			warp_sweep5(Z[l], B[l], M[l], lw[l], lh[l], 0);
+		}
+	}
+	for (int l = L - 2; l >= l0; l--) {
+		const int wc = lw[l + 1];
+		for (int c = lane; c < lw[l] * lh[l]; c += 32) {
+			const int j = c / lw[l], i = c - j * lw[l];
+			const int kc = (j >> 1) * wc + (i >> 1);
+			if (M[l][c] && M[l + 1][kc]) Z[l][c] += Z[l + 1][kc];
+		}
+		__syncwarp();
+		for (int s = 0; s < NU5; s++) {
+			warp_sweep5(Z[l], B[l], M[l], lw[l], lh[l], 1);
+			warp_sweep5(Z[l], B[l], M[l], lw[l], lh[l], 0);
+		}
+	}
+}
+
 // The V-cycle below level nfine of every problem, one block per problem, all
 // in shared memory: the same sweeps, restriction and injection as the tile
 // kernels, with the coarsest level (<= 4 x 4) getting COARSE_SWEEPS symmetric
 // sweeps.  Reads b of level nfine, writes z2 of level nfine.  When nfine == 0
 // (a problem no larger than coarse_max()) it also forms r.z and the PCG scalars.
-__global__ void __launch_bounds__(1024) k_coarse5(const ProbDev *__restrict__ P, ProbState *st, Globals *gl,
+__global__ void __launch_bounds__(1024, 1) k_coarse5(const ProbDev *__restrict__ P, ProbState *st, Globals *gl,
 		int pcg)
 {
 	extern __shared__ __align__(16) unsigned char smem[];
@@ -1034,8 +1259,11 @@ __global__ void __launch_bounds__(1024) k_coarse5(const ProbDev *__restrict__ P,
 		}
 	}
 	__syncthreads();
-	// down
-	for (int l = c0; l + 1 < L; l++) {
+	// levels ls.. hold at most 256 cells: warp 0 runs them alone
+	int ls = c0;
+	while (ls < L - 1 && lw[ls] * lh[ls] > 256) ls++;
+	// down (block-wide levels)
+	for (int l = c0; l < ls; l++) {
 		float *z = Zs(l), *b = Bs(l);
 		const uint8_t *m = Ms(l);
 		for (int s = 0; s < NU5; s++) {
@@ -1061,19 +1289,15 @@ __global__ void __launch_bounds__(1024) k_coarse5(const ProbDev *__restrict__ P,
 		}
 		__syncthreads();
 	}
-	{   // coarsest
-		const int l = L - 1;
-		float *z = Zs(l), *b = Bs(l);
-		const uint8_t *m = Ms(l);
-		for (int s = 0; s < COARSE_SWEEPS; s++) {
-			smem_sweep5(z, b, m, lw[l], lh[l], 0);
-			smem_sweep5(z, b, m, lw[l], lh[l], 1);
-			smem_sweep5(z, b, m, lw[l], lh[l], 1);
-			smem_sweep5(z, b, m, lw[l], lh[l], 0);
-		}
+	if (threadIdx.x < 32) {
+		float *Z[MAXLEV], *B[MAXLEV];
+		const uint8_t *M[MAXLEV];
+		for (int l = ls; l < L; l++) { Z[l] = Zs(l); B[l] = Bs(l); M[l] = Ms(l); }
+		warp_vcycle5(Z, B, M, lw, lh, ls, L);
 	}
-	// up
-	for (int l = L - 2; l >= c0; l--) {
+	__syncthreads();
+	// up (block-wide levels)
+	for (int l = ls - 1; l >= c0; l--) {
 		float *z = Zs(l), *b = Bs(l);
 		const uint8_t *m = Ms(l);
 		const float *zc = Zs(l + 1);
@@ -1959,6 +2183,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 		d.w = q.w;
 		d.h = q.h;
 		d.rtol = q.rtol;
+		d.tau_min = tau_min();
 		kinds |= 1 << q.kind;
 		pl.nlev_max = std::max(pl.nlev_max, nl);
 		for (int l = 0; l < nl; l++) {
