@@ -295,6 +295,13 @@ def run_ours(args):
         ms = sum(a.elapsed_time(b) for a, b in evs)
         return ms, reps
 
+    # untimed: the autotuner times the fused V-cycle's hand-over sizes on this
+    # workload and the timed solves reuse its choice (the same output bits
+    # whichever size it picks)
+    coarse_max = None
+    if not args.no_autotune:
+        _, _, coarse_max = simpois.autotune(list(zip(gs, fs, [i.tstep for i in insts])), rtol=rtol,
+                                            outs=outs)
     for _ in range(args.warmup):
         step_batched()
     ctx.reset_launches()
@@ -308,7 +315,8 @@ def run_ours(args):
     value = total_unknowns * args.steps / (ms / 1e3) / 1e6
     if args.quick:
         line = {"value": value, "ms_per_step": ms / args.steps, "gpu_launches": launches,
-                "iterations": [r["iterations"] for r in reps], "max_rel": worst}
+                "iterations": [r["iterations"] for r in reps], "max_rel": worst,
+                "coarse_max": coarse_max}
         if args.with_plain:
             step_plain()
             ms_p, _ = timed(step_plain, args.steps)
@@ -396,6 +404,7 @@ def run_ours(args):
         "data": "synthetic (seeded; shapes and distributions of the benchmark workload)",
         "config": {"workload": wname, "unknown_samples_per_step": unknowns, "rtol": rtol,
                    "l2": "flushed between timed steps (512 MiB write)",
+                   "autotuned": {"coarse_max": coarse_max},
                    "parallelism": ("shards" if args.shard else "replicas") if world > 1 else "single GPU"},
         "plain": {"value": round(value_plain, 3), "unit": "filled Mpx/s",
                   "ms_per_step": ms_plain / args.steps,
@@ -456,6 +465,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="c1")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="skip the untimed autotuning solve (default hand-over size)")
     ap.add_argument("--size", type=int, default=0, help="c4: number of images (default 32)")
     ap.add_argument("--shard", action="store_true",
                     help="N>1: partition one batch across the ranks instead of one copy per rank")

@@ -6,6 +6,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "common.cuh"
@@ -132,8 +133,69 @@ int run_reference(simpois_ctx *ctx, float *out, const float *in, const float *da
 
 // Converged schedule over the channels of several images; the singular
 // channels (no known pixel) are redone with the reference schedule.
+// Key of the tuning table: operator, V-cycle variant and every channel's shape.
+std::string tune_key(const std::vector<MgProblem> &sub, int kind, const MgOptions &opt)
+{
+	std::string key = std::to_string(kind) + (opt.fused ? "f" : "u") + (opt.use_mg ? "m" : "c");
+	char buf[32];
+	for (const MgProblem &q : sub) {
+		snprintf(buf, sizeof buf, "|%dx%d", q.w, q.h);
+		key += buf;
+	}
+	return key;
+}
+
+// Solve the batch once per distinct hand-over size among the default, 32, 64
+// and 128 (sizes that put the same levels in the same kernels are tried
+// once): one untimed solve that captures the solve graph, then the best of
+// two timed ones (CUDA events on the context's stream around the whole call).
+// Every candidate writes the same bits, so the batch is left solved.
+int tune_and_solve(simpois_ctx *ctx, const std::vector<MgProblem> &sub, MgOptions opt, simpois_report *r,
+		int *chosen)
+{
+	const int cands[] = {mg_default_coarse_max(), 32, 64, 128};
+	std::vector<std::vector<int>> seen;
+	cudaEvent_t a, b;
+	SP_CUDA(ctx, cudaEventCreate(&a));
+	if (cudaEventCreate(&b) != cudaSuccess) {
+		cudaEventDestroy(a);
+		return ctx_fail(ctx, SIMPOIS_ECUDA, "cudaEventCreate");
+	}
+	float best_ms = 0;
+	int best = 0, rc = SIMPOIS_OK;
+	for (int c : cands) {
+		std::vector<int> nf;
+		for (const MgProblem &q : sub) nf.push_back(mg_handover_level(q.w, q.h, c));
+		if (std::find(seen.begin(), seen.end(), nf) != seen.end()) continue;
+		seen.push_back(nf);
+		opt.coarse_max = c;
+		rc = mg_solve(ctx, sub.data(), (int)sub.size(), opt, r);
+		if (rc) break;
+		float t = 0;
+		for (int k = 0; k < 2 && !rc; k++) {
+			float ms = 0;
+			cudaEventRecord(a, ctx->stream);
+			rc = mg_solve(ctx, sub.data(), (int)sub.size(), opt, r);
+			cudaEventRecord(b, ctx->stream);
+			if (cudaEventSynchronize(b) != cudaSuccess || cudaEventElapsedTime(&ms, a, b) != cudaSuccess)
+				rc = ctx_fail(ctx, SIMPOIS_ECUDA, "autotuner timing: %s", cudaGetErrorString(cudaGetLastError()));
+			t = k == 0 ? ms : std::min(t, ms);
+		}
+		if (rc) break;
+		if (best == 0 || t < best_ms) {
+			best_ms = t;
+			best = c;
+		}
+	}
+	cudaEventDestroy(a);
+	cudaEventDestroy(b);
+	if (rc) return rc;
+	*chosen = best;
+	return SIMPOIS_OK;
+}
+
 int run_converged(simpois_ctx *ctx, const simpois_image *im, int n, const simpois_params *p,
-		simpois_report *rep)
+		simpois_report *rep, int tune = 0, int *tuned_cm = nullptr)
 {
 	std::vector<MgProblem> probs;
 	std::vector<int> img_of;
@@ -178,8 +240,27 @@ int run_converged(simpois_ctx *ctx, const simpois_image *im, int n, const simpoi
 			}
 		if (sub.empty()) continue;
 		std::vector<simpois_report> r(sub.size());
-		rc = mg_solve(ctx, sub.data(), (int)sub.size(), opt, r.data());
-		if (rc) return rc;
+		MgOptions o = opt;
+		const std::string key = tune_key(sub, kind, opt);
+		const bool tunable = o.fused && o.use_mg && !o.ktimer;
+		if (ctx->coarse_max_fixed > 0) {
+			o.coarse_max = ctx->coarse_max_fixed;
+		} else if (tune && tunable) {
+			int best = 0;
+			rc = tune_and_solve(ctx, sub, o, r.data(), &best);
+			if (rc) return rc;
+			ctx->tuned[key] = best;
+			o.coarse_max = best;
+		} else {
+			auto it = ctx->tuned.find(key);
+			if (it != ctx->tuned.end()) o.coarse_max = it->second;
+		}
+		if (!(tune && tunable && ctx->coarse_max_fixed <= 0)) {
+			rc = mg_solve(ctx, sub.data(), (int)sub.size(), o, r.data());
+			if (rc) return rc;
+		}
+		if (tuned_cm && (kind == 0 || tuned_cm[0] == 0))
+			tuned_cm[0] = o.coarse_max > 0 ? o.coarse_max : mg_default_coarse_max();
 		for (size_t q = 0; q < sub.size(); q++) rep[where[q]] = r[q];
 	}
 	// singular channels: the reference schedule, as the reference would run them
@@ -346,8 +427,8 @@ int simpois_solve(simpois_ctx *ctx, float *out, const float *in, const float *da
 	return st;
 }
 
-int simpois_solve_batch(simpois_ctx *ctx, const simpois_image *images, int n, const simpois_params *params,
-		simpois_report *reports)
+static int solve_batch(simpois_ctx *ctx, const simpois_image *images, int n, const simpois_params *params,
+		simpois_report *reports, int tune, int *coarse_max)
 {
 	if (!ctx || (!images && n > 0) || n < 0) return ctx_fail(ctx, SIMPOIS_EINVAL, "bad batch");
 	simpois_params p;
@@ -384,7 +465,7 @@ int simpois_solve_batch(simpois_ctx *ctx, const simpois_image *images, int n, co
 		int nch = 0;
 		for (auto &im : conv) nch += im.pd;
 		std::vector<simpois_report> r(nch);
-		rc = run_converged(ctx, conv.data(), (int)conv.size(), &p, r.data());
+		rc = run_converged(ctx, conv.data(), (int)conv.size(), &p, r.data(), tune, coarse_max);
 		if (rc) return rc;
 		int q = 0;
 		for (size_t k = 0; k < conv.size(); k++)
@@ -395,6 +476,30 @@ int simpois_solve_batch(simpois_ctx *ctx, const simpois_image *images, int n, co
 	for (int l = 0; l < total; l++) st = worst(st, rep[l].status == SIMPOIS_SINGULAR ? SIMPOIS_OK : rep[l].status);
 	if (reports) memcpy(reports, rep.data(), sizeof(simpois_report) * total);
 	return st;
+}
+
+int simpois_solve_batch(simpois_ctx *ctx, const simpois_image *images, int n, const simpois_params *params,
+		simpois_report *reports)
+{
+	return solve_batch(ctx, images, n, params, reports, 0, nullptr);
+}
+
+int simpois_autotune(simpois_ctx *ctx, const simpois_image *images, int n, const simpois_params *params,
+		simpois_report *reports, int *coarse_max)
+{
+	int cm = 0;
+	const int st = solve_batch(ctx, images, n, params, reports, 1, &cm);
+	if (coarse_max) *coarse_max = cm;
+	return st;
+}
+
+int simpois_set_coarse_max(simpois_ctx *ctx, int coarse_max)
+{
+	if (!ctx) return SIMPOIS_EINVAL;
+	if (coarse_max != 0 && (coarse_max < 8 || coarse_max > 128))
+		return ctx_fail(ctx, SIMPOIS_EINVAL, "hand-over size %d outside 8..128", coarse_max);
+	ctx->coarse_max_fixed = coarse_max;
+	return SIMPOIS_OK;
 }
 
 int simpois_residual_device(simpois_ctx *ctx, const float *u, const float *in, const float *dat, int w, int h,
@@ -458,6 +563,11 @@ int simpois_adjoint_device(simpois_ctx *ctx, const float *grad_out, const float 
 	opt.use_graph = !(p.flags & SIMPOIS_FLAG_NO_GRAPH);
 	opt.fused = !(p.flags & SIMPOIS_FLAG_UNFUSED);
 	opt.mode = MG_ADJOINT;
+	opt.coarse_max = ctx->coarse_max_fixed;
+	if (opt.coarse_max <= 0) {   // the forward fill's tuned hand-over, if any
+		auto it = ctx->tuned.find(tune_key(probs, 0, opt));
+		if (it != ctx->tuned.end()) opt.coarse_max = it->second;
+	}
 	opt.grad_out = go.data();
 	opt.grad_in = gi.data();
 	opt.grad_dat = gd.data();

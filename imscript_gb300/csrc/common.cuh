@@ -7,6 +7,7 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <map>
 #include <string>
 #include <vector>
 
@@ -53,6 +54,11 @@ struct simpois_ctx {
 	cudaGraphExec_t solve_exec = nullptr;
 	std::string solve_sig;
 	long long solve_nodes_outer = 0, solve_nodes_inner = 0, solve_nodes_top = 0;
+
+	// fused V-cycle hand-over size: fixed by the caller (0: none), and the
+	// autotuner's choice per batch shape
+	int coarse_max_fixed = 0;
+	std::map<std::string, int> tuned;
 };
 
 // Record a message on the context and return the status.

@@ -82,6 +82,7 @@ struct ProbDev {
 
 struct ProbState {
 	double bnorm2, rho, alpha, beta, rr, tau2, rel, rel_first;
+	double cross;   // FP64 biharmonic PCG: r_new . z_old (flexible beta)
 	int iter, total_iter, outer, inner_active, outer_active, status;
 	unsigned int cnt;
 	int max_iter;
@@ -788,9 +789,6 @@ __global__ void k_coarsest(const ProbDev *__restrict__ P, const ProbState *__res
 constexpr int FH = 2 * NU5;           // halo: one pixel per half-sweep
 constexpr int FR = SP_TILE + 2 * FH;  // side of the shared region (40)
 constexpr int FN = FR * FR;
-// Levels with max(w, h) <= coarse_max() run in k_coarse5, one block per
-// problem.  Default 64 (measured best on 2048^2 x 3 against 32 and 128);
-// SIMPOIS_COARSE_MAX (8..128) overrides it.
 // FP32 inner solves stop at this relative decrease at the latest (the FP32
 // recurrence drifts below it); SIMPOIS_TAU_MIN overrides it for tuning.
 double tau_min()
@@ -813,14 +811,34 @@ bool verbose()
 	return v;
 }
 
-int coarse_max()
+// Hand-over size of the fused V-cycle: levels with max(w, h) <= it run in
+// k_coarse5 (one block per problem), wider levels in the tile kernels.
+// Level 0 of a problem of at most SMALL_MAX x SMALL_MAX always runs in
+// k_coarse5 and level 0 of a larger problem always in the tile kernels, so
+// the hand-over size (8..128) moves work between kernels but changes no bit
+// of a result (both compute the same sweeps, restrictions and injections).
+// Default 64; SIMPOIS_COARSE_MAX overrides the default.
+constexpr int SMALL_MAX = 64;
+
+int clamp_coarse_max(int x) { return x < 8 ? 8 : (x > 128 ? 128 : x); }
+
+int default_coarse_max()
 {
 	static int v = [] {
 		const char *e = getenv("SIMPOIS_COARSE_MAX");
-		int x = e ? atoi(e) : 64;
-		return x < 8 ? 8 : (x > 128 ? 128 : x);
+		return clamp_coarse_max(e ? atoi(e) : 64);
 	}();
 	return v;
+}
+
+// Levels of a problem that run in the tile kernels (the level nfine and the
+// coarser ones run in k_coarse5).
+int handover_level(const int *lw, const int *lh, int nl, int cmax)
+{
+	if (std::max(lw[0], lh[0]) <= SMALL_MAX) return 0;
+	int nf = 1;
+	while (nf < nl - 1 && std::max(lw[nf], lh[nf]) > cmax) nf++;
+	return nf;
 }
 
 // 5-point Gauss-Seidel update of region cell c (region side R), in place:
@@ -1231,7 +1249,7 @@ __device__ void warp_vcycle5(float *const *Z, float *const *B, const uint8_t *co
 // in shared memory: the same sweeps, restriction and injection as the tile
 // kernels, with the coarsest level (<= 4 x 4) getting COARSE_SWEEPS symmetric
 // sweeps.  Reads b of level nfine, writes z2 of level nfine.  When nfine == 0
-// (a problem no larger than coarse_max()) it also forms r.z and the PCG scalars.
+// (a problem of at most SMALL_MAX x SMALL_MAX) it also forms r.z and the PCG scalars.
 __global__ void __launch_bounds__(1024, 1) k_coarse5(const ProbDev *__restrict__ P, ProbState *st, Globals *gl,
 		int pcg)
 {
@@ -1460,7 +1478,11 @@ __global__ void k_rz64(const ProbDev *__restrict__ P, ProbState *st, const int4 
 			s.inner_active = 0;
 			atomicSub(&gl->inner_count, 1);
 		} else {
-			s.beta = s.rho > 0 ? tot[0] / s.rho : 0.0;
+			// flexible (Polak-Ribiere) beta = r_new . (z_new - z_old) / rho_old:
+			// the FP32 preconditioner is only approximately symmetric, and this
+			// form keeps the FP64 recurrence converging where the classical
+			// r.z / rho_old stalls (small images with holes at the border)
+			s.beta = s.rho > 0 ? (tot[0] - s.cross) / s.rho : 0.0;
 			s.rho = tot[0];
 		}
 	}
@@ -1538,17 +1560,19 @@ __global__ void k_xr64(const ProbDev *__restrict__ P, ProbState *st, const int4 
 	if (!st[prob].inner_active) return;
 	const ProbDev &pr = P[prob];
 	const double a = st[prob].alpha;
-	double rr = 0;
+	double rr = 0, cross = 0;
 	TILE_LOOP_UNKNOWN(pr, t, {
 		pr.U[k] += a * pr.p64[k];
 		const double rk = pr.r64[k] - a * pr.q64[k];
 		pr.r64[k] = rk;
 		rr += rk * rk;
+		cross += rk * (double)pr.lv[0].z2[k];   // z2 still holds the previous z
 	})
 	double tot[2];
-	if (problem_sum1(rr, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
+	if (problem_sum2(rr, cross, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
 		ProbState &s = st[prob];
 		s.rr = tot[0];
+		s.cross = tot[1];
 		s.iter += 1;
 		s.total_iter += 1;
 		if (tot[0] <= s.tau2 || s.iter >= INNER_MAX13 || s.total_iter >= s.max_iter) {
@@ -2158,6 +2182,15 @@ void kt_collect(simpois_ctx *ctx, KTimer &kt)
 
 }  // namespace
 
+int mg_handover_level(int w, int h, int coarse_max)
+{
+	int lw[MAXLEV], lh[MAXLEV];
+	const int nl = level_dims(w, h, lw, lh);
+	return handover_level(lw, lh, nl, coarse_max > 0 ? clamp_coarse_max(coarse_max) : default_coarse_max());
+}
+
+int mg_default_coarse_max() { return default_coarse_max(); }
+
 int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &opt, simpois_report *rep)
 {
 	if (n <= 0) return SIMPOIS_OK;
@@ -2172,6 +2205,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	std::vector<size_t> off_U(n), off_x(n), off_p(n), off_q(n), off_p2(n);
 	std::vector<size_t> off_r64(n, 0), off_p64(n, 0), off_q64(n, 0);
 	std::vector<std::vector<int4>> lists(MAXLEV);
+	const int cmax = opt.coarse_max > 0 ? clamp_coarse_max(opt.coarse_max) : default_coarse_max();
 	for (int k = 0; k < n; k++) {
 		const MgProblem &q = probs[k];
 		int lw[MAXLEV], lh[MAXLEV];
@@ -2203,9 +2237,8 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 			off_z[l].push_back(0);
 			off_z2[l].push_back(0);
 		}
-		// fused path: the tile kernels cover the levels wider than coarse_max()
-		d.nfine = 0;
-		while (d.nfine < nl - 1 && std::max(lw[d.nfine], lh[d.nfine]) > coarse_max()) d.nfine++;
+		// fused path: the tile kernels cover the levels above the hand-over
+		d.nfine = handover_level(lw, lh, nl, cmax);
 		pl.nfine_max = std::max(pl.nfine_max, d.nfine);
 		pl.coarse_smem = std::max(pl.coarse_smem, coarse_layout(lw, lh, d.nfine, nl).bytes);
 		size_t px = (size_t)q.w * q.h;

@@ -33,6 +33,7 @@ struct MgOptions {
 	int fused = 1;         // 5-point: fused V-cycle kernels (0: one launch per sweep)
 	int ktimer = 0;        // time every main-loop launch with CUDA events (no graph)
 	int out_resid = 0;     // FP64 residual of the float output
+	int coarse_max = 0;    // fused V-cycle hand-over size (0: the default)
 	int mode = MG_FILL;
 	// MG_ADJOINT only: grad_out per problem (device), results
 	const float *const *grad_out = nullptr;
@@ -43,6 +44,13 @@ struct MgOptions {
 // Batched converged solve of n problems; rep receives n records.
 int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &opt,
 		simpois_report *rep);
+
+// Number of levels of a w x h problem that the fused V-cycle runs in the tile
+// kernels for hand-over size coarse_max (0: the default).
+int mg_handover_level(int w, int h, int coarse_max);
+
+// The hand-over size used when a solve names none (64, or SIMPOIS_COARSE_MAX).
+int mg_default_coarse_max();
 
 // FP64 relative residual of a float output for n problems (kind per problem).
 int mg_residual(simpois_ctx *ctx, const MgProblem *probs, const float *const *u, int n,

@@ -67,7 +67,7 @@ EXPORTS = [
     "simpois_default_params", "simpois_params_from_env", "simpois_create", "simpois_destroy",
     "simpois_strerror", "simpois_last_error", "simpois_solve", "simpois_solve_device",
     "simpois_solve_batch", "simpois_residual_device", "simpois_residual_device_noalloc",
-    "simpois_adjoint_device",
+    "simpois_adjoint_device", "simpois_autotune", "simpois_set_coarse_max",
     "simpois_launch_count", "simpois_reset_launch_count", "simpois_kernel_stats",
     "simpois_reset_kernel_stats",
     "poisson_solver_separable", "poisson_rec", "poisson_recursive",
@@ -115,6 +115,8 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
                                               ctypes.POINTER(ctypes.c_double)]
         L.simpois_residual_device_noalloc.argtypes = L.simpois_residual_device.argtypes
         L.simpois_adjoint_device.argtypes = [vp, vp, vp, ip, ip, ip, vp, vp, P, R]
+        L.simpois_autotune.argtypes = [vp, ctypes.POINTER(Image), ip, P, R, ctypes.POINTER(ip)]
+        L.simpois_set_coarse_max.argtypes = [vp, ip]
         L.simpois_launch_count.argtypes = [vp]
         L.simpois_launch_count.restype = ctypes.c_longlong
         L.simpois_reset_launch_count.argtypes = [vp]
@@ -175,6 +177,10 @@ class Context:
 
     def reset_kernel_stats(self):
         self._lib.simpois_reset_kernel_stats(self.handle)
+
+    def set_coarse_max(self, coarse_max: int):
+        """Fix the fused V-cycle's hand-over size (8..128; 0: tuned or default)."""
+        self.check(self._lib.simpois_set_coarse_max(self.handle, int(coarse_max)))
 
     def last_error(self) -> str:
         return self._lib.simpois_last_error(self.handle).decode()

@@ -116,6 +116,20 @@ def solve_batch(images, *, rtol=1e-6, tstep=0.25, max_iter=0, flags=0, allow=(_l
     ``images`` is a list of ``g`` tensors or of ``(g, f)`` / ``(g, f, tstep)``
     tuples.  Returns (outputs, reports) with one report per channel.
     """
+    outs, reps, _ = _batch(images, rtol, tstep, max_iter, flags, allow, outs, False)
+    return outs, reps
+
+
+def autotune(images, *, rtol=1e-6, tstep=0.25, max_iter=0, flags=0, allow=(_lib.OK,), outs=None):
+    """``solve_batch`` that also times the fused V-cycle's hand-over sizes and
+    keeps the fastest for later batches of the same shapes on this context.
+
+    Returns (outputs, reports, coarse_max); the outputs are the same bits
+    whichever hand-over is chosen."""
+    return _batch(images, rtol, tstep, max_iter, flags, allow, outs, True)
+
+
+def _batch(images, rtol, tstep, max_iter, flags, allow, outs, tune):
     import torch
     items = []
     for k, it in enumerate(images):
@@ -130,7 +144,7 @@ def solve_batch(images, *, rtol=1e-6, tstep=0.25, max_iter=0, flags=0, allow=(_l
             raise ValueError(f"image {k}: data term must match the image")
         items.append((g, f, t))
     if not items:
-        return [], []
+        return [], [], None
     dev = items[0][0].device
     outs = [torch.empty_like(g) for g, _, _ in items] if outs is None else outs
     arr = (_lib.Image * len(items))()
@@ -144,9 +158,15 @@ def solve_batch(images, *, rtol=1e-6, tstep=0.25, max_iter=0, flags=0, allow=(_l
     prm = _lib.default_params(rtol=float(rtol), max_iter=int(max_iter), flags=int(flags),
                               tstep=float(tstep))
     ctx = context(dev.index or 0, _torch_stream(items[0][0]))
-    rc = _lib.load().simpois_solve_batch(ctx.handle, arr, len(items), ctypes.byref(prm), reps)
+    if tune:
+        cm = ctypes.c_int(0)
+        rc = _lib.load().simpois_autotune(ctx.handle, arr, len(items), ctypes.byref(prm), reps,
+                                          ctypes.byref(cm))
+    else:
+        cm = None
+        rc = _lib.load().simpois_solve_batch(ctx.handle, arr, len(items), ctypes.byref(prm), reps)
     ctx.check(rc, allow)
-    return outs, [r.as_dict() for r in reps]
+    return outs, [r.as_dict() for r in reps], (cm.value if cm is not None else None)
 
 
 def residual(u, g, f=None, kind=0):

@@ -171,6 +171,23 @@ int simpois_adjoint_device(simpois_ctx *ctx, const float *grad_out,
 		float *grad_dat, const simpois_params *params,
 		simpois_report *reports);
 
+/* Autotuner (no counterpart in the reference, which has no launch-shape
+ * knobs).  The converged 5-point V-cycle runs the levels wider than a
+ * hand-over size in 32 x 32 tile kernels and the rest in one shared-memory
+ * block per channel; the hand-over size (8..128) moves work between the two
+ * kernels but changes no bit of any result.
+ * simpois_autotune solves the batch like simpois_solve_batch while timing
+ * every distinct hand-over among 32, 64 and 128 (plus the default), keeps the
+ * fastest for batches of the same channel shapes and operators on this
+ * context (later solves of such batches use it), and writes it to
+ * *coarse_max (may be NULL; the value of the 5-point channels when the batch
+ * mixes operators).  simpois_set_coarse_max fixes the hand-over for every
+ * later solve on the context (0 restores tuned-or-default). */
+int simpois_autotune(simpois_ctx *ctx, const simpois_image *images, int n,
+		const simpois_params *params, simpois_report *reports,
+		int *coarse_max);
+int simpois_set_coarse_max(simpois_ctx *ctx, int coarse_max);
+
 /* Instrumentation (no counterpart in the reference): the number of kernel
  * launches this context has issued (a graph replay counts its kernel nodes),
  * and a reset. */
