@@ -126,5 +126,74 @@ __device__ __forceinline__ double block_sum(double v, double *sh)
 	return r;
 }
 
+// ---------------------------------------------------------------- float-float sums
+// A sum carried as hi + lo in two floats (about 48 significant bits) on the
+// FP32 units.  FP64 arithmetic issues at about 1/70 of the FP32 rate on this
+// GPU (and a float-to-double conversion costs as much), so the per-pixel
+// terms of the FP32 PCG's dot products are accumulated this way and only the
+// per-warp sums are converted to double for the rest of the reduction.
+struct FF {
+	float hi, lo;
+};
+
+// a + b exactly as hi + lo (TwoSum)
+__device__ __forceinline__ FF ff_two_sum(float a, float b)
+{
+	const float s = __fadd_rn(a, b);
+	const float bb = __fsub_rn(s, a);
+	FF r;
+	r.hi = s;
+	r.lo = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+	return r;
+}
+
+// hi + lo with |lo| folded below half an ulp of hi (Fast2Sum)
+__device__ __forceinline__ FF ff_norm(float hi, float lo)
+{
+	FF r;
+	r.hi = __fadd_rn(hi, lo);
+	r.lo = __fsub_rn(lo, __fsub_rn(r.hi, hi));
+	return r;
+}
+
+// acc += a * b: the product split exactly by an FMA, added by TwoSum
+__device__ __forceinline__ void ff_add_prod(FF &acc, float a, float b)
+{
+	const float p = __fmul_rn(a, b);
+	const float e = __fmaf_rn(a, b, -p);
+	const FF s = ff_two_sum(acc.hi, p);
+	acc = ff_norm(s.hi, __fadd_rn(__fadd_rn(acc.lo, e), s.lo));
+}
+
+__device__ __forceinline__ FF ff_add(FF a, FF b)
+{
+	const FF s = ff_two_sum(a.hi, b.hi);
+	return ff_norm(s.hi, __fadd_rn(__fadd_rn(a.lo, b.lo), s.lo));
+}
+
+// Block sum of float-float values (thread 0 gets the result): float-float
+// across each warp, the warps' sums in double.
+template <int NT>
+__device__ __forceinline__ double block_sum_ff(FF v, double *sh)
+{
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) {
+		FF w;
+		w.hi = __shfl_down_sync(0xffffffffu, v.hi, o);
+		w.lo = __shfl_down_sync(0xffffffffu, v.lo, o);
+		v = ff_add(v, w);
+	}
+	if (lane == 0) sh[warp] = (double)v.hi + (double)v.lo;
+	__syncthreads();
+	double r = 0;
+	if (threadIdx.x == 0) {
+#pragma unroll
+		for (int k = 0; k < NT / 32; k++) r += sh[k];
+	}
+	__syncthreads();
+	return r;
+}
+
 // Clamp-to-edge index (the Neumann extension of simpois.c:25-32).
 __device__ __forceinline__ int clampi(int v, int n) { return v < 0 ? 0 : (v >= n ? n - 1 : v); }

@@ -56,6 +56,7 @@ constexpr double TAU_MIN = 5e-7;    // FP32 inner solve: smallest relative decre
 struct LevelDev {
 	int w, h;
 	uint8_t *mask;   // 1 = unknown
+	uint8_t *code;   // 5-point cell code (cell_code), levels below the coarsest
 	float *b;        // right-hand side (level 0: the PCG residual r)
 	float *z;        // correction (level 0: the preconditioned residual);
 	                 // fused path: the pre-smoothed correction
@@ -74,6 +75,8 @@ struct ProbDev {
 	double *U;           // FP64 solution image (g or 0 at the known pixels)
 	float *x, *p, *q;    // level-0 PCG vectors
 	float *p2;           // fused path: second search-direction buffer
+	float *b_alt;        // fused path: the other level-0 residual buffer (k_pre5
+	                     // writes the updated r there, then swaps it with lv[0].b)
 	double *r64, *p64, *q64;   // 13-point: FP64 Krylov vectors (else null)
 	double tau_min;            // FP32 inner solve: smallest relative decrease
 	double rtol;
@@ -84,6 +87,7 @@ struct ProbState {
 	double bnorm2, rho, alpha, beta, rr, tau2, rel, rel_first;
 	double cross;   // FP64 biharmonic PCG: r_new . z_old (flexible beta)
 	int iter, total_iter, outer, inner_active, outer_active, status;
+	int pending;    // fused 5-point PCG: alpha is set, x and r await their update
 	unsigned int cnt;
 	int max_iter;
 	int nknown, nunknown;   // pixel counts of the channel
@@ -207,12 +211,11 @@ __device__ bool problem_sum2(double v0, double v1, int prob, const int *__restri
 	return true;
 }
 
-// problem_sum2 for a single value (one block reduction instead of two).
-__device__ bool problem_sum1(double v0, int prob, const int *__restrict__ tbeg, const int *__restrict__ tcnt,
+// problem_sum2 for a single value whose block sum s0 thread 0 holds.
+__device__ bool problem_sum1_block(double s0, int prob, const int *__restrict__ tbeg, const int *__restrict__ tcnt,
 		double *partial, ProbState *st, double *tot, double *sh)
 {
 	__shared__ bool am_last;
-	double s0 = block_sum<SP_THREADS>(v0, sh);
 	if (threadIdx.x == 0) {
 		partial[2 * blockIdx.x] = s0;
 		__threadfence();
@@ -232,6 +235,19 @@ __device__ bool problem_sum1(double v0, int prob, const int *__restrict__ tbeg, 
 		st[prob].cnt = 0;
 	}
 	return true;
+}
+
+__device__ bool problem_sum1(double v0, int prob, const int *__restrict__ tbeg, const int *__restrict__ tcnt,
+		double *partial, ProbState *st, double *tot, double *sh)
+{
+	return problem_sum1_block(block_sum<SP_THREADS>(v0, sh), prob, tbeg, tcnt, partial, st, tot, sh);
+}
+
+// problem_sum1 of float-float per-thread terms (the FP32 PCG's dot products)
+__device__ bool problem_sum1_ff(FF v0, int prob, const int *__restrict__ tbeg, const int *__restrict__ tcnt,
+		double *partial, ProbState *st, double *tot, double *sh)
+{
+	return problem_sum1_block(block_sum_ff<SP_THREADS>(v0, sh), prob, tbeg, tcnt, partial, st, tot, sh);
 }
 
 // ------------------------------------------------------------------ setup kernels
@@ -277,7 +293,23 @@ __global__ void k_setup0(const ProbDev *__restrict__ P, ProbState *st, const int
 	}
 }
 
-// Level l >= 1 over all tiles: unknown iff every existing child is unknown.
+// Cell code of a 5-point cell: bit 0 unknown; bits 1-4 the E, W, S, N
+// neighbour is in the image and unknown; bits 5-7 the number of clamped sides
+// (the diagonal is 4 minus it).  0 for a known cell.
+__device__ __forceinline__ uint8_t cell_code(const uint8_t *m, int i, int j, int w, int h)
+{
+	const size_t k = (size_t)j * w + i;
+	if (!m[k]) return 0;
+	int code = 1, nd = 0;
+	if (i + 1 < w) { if (m[k + 1]) code |= 2; } else nd++;
+	if (i > 0)     { if (m[k - 1]) code |= 4; } else nd++;
+	if (j + 1 < h) { if (m[k + w]) code |= 8; } else nd++;
+	if (j > 0)     { if (m[k - w]) code |= 16; } else nd++;
+	return (uint8_t)(code | (nd << 5));
+}
+
+// Level l >= 1 over all tiles: unknown iff every existing child is unknown;
+// also the cell codes of level l-1.
 __global__ void k_mask_down(const ProbDev *__restrict__ P, const int4 *__restrict__ all, int l, int *__restrict__ flag)
 {
 	__shared__ int any;
@@ -304,6 +336,11 @@ __global__ void k_mask_down(const ProbDev *__restrict__ P, const int4 *__restric
 	if (__any_sync(0xffffffffu, mine) && (threadIdx.x & 31) == 0) atomicOr(&any, 1);
 	__syncthreads();
 	if (threadIdx.x == 0) flag[blockIdx.x] = any;
+	// the mask of level l-1 is complete: its cell codes under this tile
+	for (int q = threadIdx.x; q < 4 * SP_TILE * SP_TILE; q += SP_THREADS) {
+		const int fi = 2 * SP_TILE * t.y + (q & (2 * SP_TILE - 1)), fj = 2 * SP_TILE * t.z + q / (2 * SP_TILE);
+		if (fi < F.w && fj < F.h) F.code[(size_t)fj * F.w + fi] = cell_code(F.mask, fi, fj, F.w, F.h);
+	}
 }
 
 // One block per level: ordered compaction of the level's tile list by flag.
@@ -425,6 +462,7 @@ __global__ void k_resid64(const ProbDev *__restrict__ P, ProbState *st, const in
 			s.tau2 = tau * tau * tot[0];
 			s.rho = 0;
 			s.beta = 0;
+			s.pending = 0;
 			atomicAdd(&gl->inner_count, 1);
 		}
 	}
@@ -519,7 +557,7 @@ __global__ void k_spmv(const ProbDev *__restrict__ P, ProbState *st, const int4 
 	const ProbDev &pr = P[prob];
 	const LevelDev &L = pr.lv[0];
 	int i = tile_i(t);
-	double pq = 0;
+	FF pq = {0.f, 0.f};
 	for (int r = 0; r < SP_ROWS; r++) {
 		int j = tile_j(t, r);
 		if (i < pr.w && j < pr.h) {
@@ -530,12 +568,12 @@ __global__ void k_spmv(const ProbDev *__restrict__ P, ProbState *st, const int4 
 				float pk = pr.p[k];
 				float qk = d * pk + o;
 				pr.q[k] = qk;
-				pq += (double)pk * (double)qk;
+				ff_add_prod(pq, pk, qk);
 			}
 		}
 	}
 	double tot[2];
-	if (problem_sum1(pq, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
+	if (problem_sum1_ff(pq, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
 		ProbState &s = st[prob];
 		double a = s.rho / tot[0];
 		if (!(tot[0] > 0) || !isfinite(a)) {
@@ -550,7 +588,7 @@ __global__ void k_spmv(const ProbDev *__restrict__ P, ProbState *st, const int4 
 }
 
 // x += alpha p; r -= alpha q; r.r; the inner stopping test
-__global__ void __launch_bounds__(SP_THREADS, 8) k_xr(const ProbDev *__restrict__ P, ProbState *st, const int4 *__restrict__ tl,
+__global__ void __launch_bounds__(SP_THREADS) k_xr(const ProbDev *__restrict__ P, ProbState *st, const int4 *__restrict__ tl,
 		const int *__restrict__ tbeg, const int *__restrict__ tcnt, double *partial, Globals *gl,
 		int use_p2)
 {
@@ -563,7 +601,7 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_xr(const ProbDev *__restrict_
 	const float a = (float)st[prob].alpha;
 	const float *pv = use_p2 ? pr.p2 : pr.p;
 	int i = tile_i(t);
-	double rr = 0;
+	FF rr = {0.f, 0.f};
 	// all loads of the four rows first (they depend only on coordinates)
 	uint8_t m[SP_ROWS];
 	float xv[SP_ROWS], pk[SP_ROWS], bk[SP_ROWS], qk[SP_ROWS];
@@ -582,14 +620,14 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_xr(const ProbDev *__restrict_
 #pragma unroll
 	for (int r = 0; r < SP_ROWS; r++) {
 		if (m[r]) {
-			pr.x[kk[r]] = xv[r] + a * pk[r];
-			const float rk = bk[r] - a * qk[r];
+			pr.x[kk[r]] = __fmaf_rn(a, pk[r], xv[r]);
+			const float rk = __fmaf_rn(-a, qk[r], bk[r]);
 			L.b[kk[r]] = rk;
-			rr += (double)rk * rk;
+			ff_add_prod(rr, rk, rk);
 		}
 	}
 	double tot[2];
-	if (problem_sum1(rr, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
+	if (problem_sum1_ff(rr, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
 		ProbState &s = st[prob];
 		s.rr = tot[0];
 		s.iter += 1;
@@ -612,16 +650,16 @@ __global__ void k_rz(const ProbDev *__restrict__ P, ProbState *st, const int4 *_
 	const ProbDev &pr = P[prob];
 	const LevelDev &L = pr.lv[0];
 	int i = tile_i(t);
-	double rz = 0;
+	FF rz = {0.f, 0.f};
 	for (int r = 0; r < SP_ROWS; r++) {
 		int j = tile_j(t, r);
 		if (i < pr.w && j < pr.h) {
 			size_t k = (size_t)j * pr.w + i;
-			if (L.mask[k]) rz += (double)L.b[k] * (double)L.z[k];
+			if (L.mask[k]) ff_add_prod(rz, L.b[k], L.z[k]);
 		}
 	}
 	double tot[2];
-	if (problem_sum1(rz, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
+	if (problem_sum1_ff(rz, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
 		ProbState &s = st[prob];
 		if (!(tot[0] > 0) || !isfinite(tot[0])) {
 			// r = 0 exactly, or a preconditioner that is not positive here
@@ -867,19 +905,26 @@ __device__ __forceinline__ float az5_cell(const float *z, const uint8_t *m, int 
 	return diag * z[c] + off;
 }
 
-// Per-cell code of a shared region cell: bit 0 unknown; bits 1-4 the E, W, S,
-// N neighbour is in the image, unknown and inside the region; bits 5-7 the
-// number of clamped sides (the 5-point diagonal is 4 minus it).
-__device__ __forceinline__ uint8_t region_code(const uint8_t *sm, int c, int rx, int ry, int gi, int gj, int w,
-		int h)
+// Region code of a shared region cell: the level's cell code (cell_code) with
+// the neighbour bits that point out of the region cleared (those cells are
+// not in shared memory).  For a group of 4 cells of a row (x the lowest byte)
+// and for one cell.
+__device__ __forceinline__ uint32_t region_codes4(uint32_t cd, int rx, int ry)
 {
-	if (!sm[c]) return 0;
-	int code = 1, nd = 0;
-	if (gi + 1 < w) { if (rx + 1 < FR && sm[c + 1]) code |= 2; } else nd++;
-	if (gi > 0)     { if (rx > 0 && sm[c - 1]) code |= 4; } else nd++;
-	if (gj + 1 < h) { if (ry + 1 < FR && sm[c + FR]) code |= 8; } else nd++;
-	if (gj > 0)     { if (ry > 0 && sm[c - FR]) code |= 16; } else nd++;
-	return (uint8_t)(code | (nd << 5));
+	if (rx == 0) cd &= ~0x00000004u;        // W of the first column
+	if (rx == FR - 4) cd &= ~0x02000000u;   // E of the last column
+	if (ry == 0) cd &= ~0x10101010u;        // N of the first row
+	if (ry == FR - 1) cd &= ~0x08080808u;   // S of the last row
+	return cd;
+}
+
+__device__ __forceinline__ uint8_t region_code1(uint8_t cd, int rx, int ry)
+{
+	if (rx == 0) cd &= ~4;
+	if (rx == FR - 1) cd &= ~2;
+	if (ry == 0) cd &= ~16;
+	if (ry == FR - 1) cd &= ~8;
+	return cd;
 }
 
 // The off-diagonal sum of split<0> from a cell code (same operations, same
@@ -933,15 +978,27 @@ __device__ __forceinline__ void sweep_cells(float *sz, const float *sb, const ui
 // Pre-smoothing from z = 0 (NU5 forward red-black sweeps), residual, and its
 // restriction (sum over the children) into b of level l+1.  Writes z of level
 // l (the pre-smoothed correction).
-__global__ void __launch_bounds__(SP_THREADS) k_pre5(const ProbDev *__restrict__ P, const ProbState *__restrict__ st,
-		const int4 *__restrict__ tl, int l)
+// At level 0 with a PCG step pending (alpha set by k_spmv5) it first takes
+// that step, as k_xr would: x += alpha p and r -= alpha q on the tile (the
+// new r goes to b_alt, which the problem's last tile then swaps with lv[0].b,
+// as neighbouring tiles still read the old r of this tile's cells), with r
+// recomputed on the whole region as the right-hand side of the sweeps, and
+// |r|^2 summed and tested as in k_xr (same operations, same order).
+__global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *st, const int4 *__restrict__ tl,
+		int l, const int *__restrict__ tbeg, const int *__restrict__ tcnt, double *partial, Globals *gl,
+		int use_p2)
 {
 	__shared__ __align__(16) float sb[FN], sz[FN];
-	__shared__ __align__(16) uint8_t sm[FN], sc[FN];
+	__shared__ __align__(16) uint8_t sc[FN];
+	__shared__ double sh[32];
 	const int4 t = tl[blockIdx.x];
-	const ProbDev &pr = P[t.x];
-	if (!st[t.x].inner_active || l >= pr.nfine) return;
-	const LevelDev L = pr.lv[l];
+	const int prob = t.x;
+	const ProbDev &pr = P[prob];
+	if (!st[prob].inner_active || l >= pr.nfine) return;
+	const LevelDev L = pr.lv[l], C = pr.lv[l + 1];
+	const bool upd = l == 0 && st[prob].pending;
+	const float a = upd ? (float)st[prob].alpha : 0.f;
+	const float *qv = pr.q;
 	const int x0 = t.y * SP_TILE - FH, y0 = t.z * SP_TILE - FH;
 	// every load depends only on the coordinates, so all are in flight at once
 	if ((L.w & 3) == 0) {
@@ -953,16 +1010,24 @@ __global__ void __launch_bounds__(SP_THREADS) k_pre5(const ProbDev *__restrict__
 				const int ry = f / (FR / 4), rx = 4 * (f - ry * (FR / 4)), gi = x0 + rx, gj = y0 + ry;
 				const bool in = gi >= 0 && gi < L.w && gj >= 0 && gj < L.h;
 				const size_t k = in ? (size_t)gj * L.w + gi : 0;
-				uchar4 m = make_uchar4(0, 0, 0, 0);
+				uint32_t cd = 0;
 				float4 bv = make_float4(0.f, 0.f, 0.f, 0.f);
 				if (in) {
-					m = *(const uchar4 *)(L.mask + k);
+					cd = *(const uint32_t *)(L.code + k);
 					bv = *(const float4 *)(L.b + k);
+					if (upd) {
+						const float4 qq = *(const float4 *)(qv + k);
+						bv.x = __fmaf_rn(-a, qq.x, bv.x);
+						bv.y = __fmaf_rn(-a, qq.y, bv.y);
+						bv.z = __fmaf_rn(-a, qq.z, bv.z);
+						bv.w = __fmaf_rn(-a, qq.w, bv.w);
+					}
 				}
+				cd = region_codes4(cd, rx, ry);
 				const int c = ry * FR + rx;
-				*(uchar4 *)(sm + c) = m;
-				*(float4 *)(sb + c) = make_float4(m.x ? bv.x : 0.f, m.y ? bv.y : 0.f, m.z ? bv.z : 0.f,
-						m.w ? bv.w : 0.f);
+				*(uint32_t *)(sc + c) = cd;
+				*(float4 *)(sb + c) = make_float4((cd & 1u) ? bv.x : 0.f, (cd & 0x100u) ? bv.y : 0.f,
+						(cd & 0x10000u) ? bv.z : 0.f, (cd & 0x1000000u) ? bv.w : 0.f);
 				*(float4 *)(sz + c) = make_float4(0.f, 0.f, 0.f, 0.f);
 			}
 		}
@@ -974,24 +1039,45 @@ __global__ void __launch_bounds__(SP_THREADS) k_pre5(const ProbDev *__restrict__
 			const int ry = c / FR, rx = c - ry * FR, gi = x0 + rx, gj = y0 + ry;
 			const bool in = gi >= 0 && gi < L.w && gj >= 0 && gj < L.h;
 			const size_t k = in ? (size_t)gj * L.w + gi : 0;
-			const uint8_t m = in ? L.mask[k] : 0;
-			const float bv = in ? L.b[k] : 0.f;
-			sm[c] = m;
-			sb[c] = m ? bv : 0.f;
+			const uint8_t cd = region_code1(in ? L.code[k] : 0, rx, ry);
+			float bv = in ? L.b[k] : 0.f;
+			if (upd && in) bv = __fmaf_rn(-a, qv[k], bv);
+			sc[c] = cd;
+			sb[c] = (cd & 1) ? bv : 0.f;
 			sz[c] = 0.f;
+		}
+	}
+	// the PCG step on the tile: the pixel -> thread map and the order of the
+	// |r|^2 terms are those of k_xr
+	FF rr = {0.f, 0.f};
+	if (upd) {
+		const float *pv = use_p2 ? pr.p2 : pr.p;
+		const int i = tile_i(t);
+		float xv[SP_ROWS], pk[SP_ROWS];
+		uint8_t mk[SP_ROWS];
+		int kk[SP_ROWS];
+#pragma unroll
+		for (int r = 0; r < SP_ROWS; r++) {
+			const int j = tile_j(t, r);
+			const bool in = i < L.w && j < L.h;
+			kk[r] = in ? j * L.w + i : 0;
+			mk[r] = in ? L.mask[kk[r]] : 0;
+			xv[r] = in ? pr.x[kk[r]] : 0.f;
+			pk[r] = in ? pv[kk[r]] : 0.f;
+		}
+		__syncthreads();   // sb holds the new r
+#pragma unroll
+		for (int r = 0; r < SP_ROWS; r++) {
+			if (mk[r]) {
+				pr.x[kk[r]] = __fmaf_rn(a, pk[r], xv[r]);
+				const float rk = sb[(tile_j(t, r) - y0) * FR + (i - x0)];
+				pr.b_alt[kk[r]] = rk;
+				ff_add_prod(rr, rk, rk);
+			}
 		}
 	}
 	int cells[2][4];
 	own_cells(x0, y0, cells);
-	__syncthreads();
-#pragma unroll
-	for (int it = 0; it < (FN + SP_THREADS - 1) / SP_THREADS; it++) {
-		const int c = threadIdx.x + it * SP_THREADS;
-		if (c < FN) {
-			const int ry = c / FR, rx = c - ry * FR;
-			sc[c] = region_code(sm, c, rx, ry, x0 + rx, y0 + ry, L.w, L.h);
-		}
-	}
 	__syncthreads();
 	// half-sweep s updates colour s&1 on the cells of ring >= s; at s = 0 every
 	// neighbour is 0, so the outermost ring needs no outside value
@@ -1005,7 +1091,6 @@ __global__ void __launch_bounds__(SP_THREADS) k_pre5(const ProbDev *__restrict__
 		if (gi < L.w && gj < L.h) L.z[(size_t)gj * L.w + gi] = sz[(ty + FH) * FR + tx + FH];
 	}
 	// restriction: one coarse cell per thread (16 x 16 per tile)
-	const LevelDev C = pr.lv[l + 1];
 	const int ci = t.y * (SP_TILE / 2) + (threadIdx.x & 15), cj = t.z * (SP_TILE / 2) + (threadIdx.x >> 4);
 	if (ci < C.w && cj < C.h && C.mask[(size_t)cj * C.w + ci]) {
 		float acc = 0.f;
@@ -1020,17 +1105,34 @@ __global__ void __launch_bounds__(SP_THREADS) k_pre5(const ProbDev *__restrict__
 			}
 		C.b[(size_t)cj * C.w + ci] = 1.f * acc;
 	}
+	if (!upd) return;
+	double tot[2];
+	if (problem_sum1_ff(rr, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
+		ProbState &s = st[prob];
+		s.rr = tot[0];
+		s.iter += 1;
+		s.total_iter += 1;
+		s.pending = 0;
+		ProbDev &w = P[prob];   // every tile of the problem is done with the old r
+		float *nb = w.b_alt;
+		w.b_alt = w.lv[0].b;
+		w.lv[0].b = nb;
+		if (tot[0] <= s.tau2 || s.iter >= INNER_MAX || s.total_iter >= s.max_iter) {
+			s.inner_active = 0;
+			atomicSub(&gl->inner_count, 1);
+		}
+	}
 }
 
 // Coarse correction (injection from z2 of level l+1) and post-smoothing
 // (NU5 backward sweeps); writes z2 of level l.  At level 0 also r.z and the
 // PCG scalars beta, rho (the last tile of the problem to finish).
-__global__ void __launch_bounds__(SP_THREADS) k_post5(const ProbDev *__restrict__ P, ProbState *st,
+__global__ void __launch_bounds__(SP_THREADS, 8) k_post5(const ProbDev *__restrict__ P, ProbState *st,
 		const int4 *__restrict__ tl, int l, const int *__restrict__ tbeg, const int *__restrict__ tcnt,
 		double *partial, Globals *gl, int pcg)
 {
 	__shared__ __align__(16) float sb[FN], sz[FN];
-	__shared__ __align__(16) uint8_t sm[FN], sc[FN];
+	__shared__ __align__(16) uint8_t sc[FN];
 	__shared__ double sh[32];
 	const int4 t = tl[blockIdx.x];
 	const int prob = t.x;
@@ -1049,25 +1151,27 @@ __global__ void __launch_bounds__(SP_THREADS) k_post5(const ProbDev *__restrict_
 				const bool in = gi >= 0 && gi < L.w && gj >= 0 && gj < L.h;
 				const size_t k = in ? (size_t)gj * L.w + gi : 0;
 				const size_t kc = in ? (size_t)(gj >> 1) * C.w + (gi >> 1) : 0;
-				uchar4 m = make_uchar4(0, 0, 0, 0);
+				uint32_t cd = 0;
 				float4 bv = make_float4(0.f, 0.f, 0.f, 0.f), zv = bv;
 				float2 cz = make_float2(0.f, 0.f);
 				uint8_t cm0 = 0, cm1 = 0;
 				if (in) {
-					m = *(const uchar4 *)(L.mask + k);
+					cd = *(const uint32_t *)(L.code + k);
 					bv = *(const float4 *)(L.b + k);
 					zv = *(const float4 *)(L.z + k);
 					cz = *(const float2 *)(C.z2 + kc);
 					cm0 = C.mask[kc];
 					cm1 = C.mask[kc + 1];
 				}
+				cd = region_codes4(cd, rx, ry);
 				const int c = ry * FR + rx;
-				*(uchar4 *)(sm + c) = m;
-				*(float4 *)(sb + c) = make_float4(m.x ? bv.x : 0.f, m.y ? bv.y : 0.f, m.z ? bv.z : 0.f,
-						m.w ? bv.w : 0.f);
-				*(float4 *)(sz + c) = make_float4(m.x ? (cm0 ? zv.x + cz.x : zv.x) : 0.f,
-						m.y ? (cm0 ? zv.y + cz.x : zv.y) : 0.f, m.z ? (cm1 ? zv.z + cz.y : zv.z) : 0.f,
-						m.w ? (cm1 ? zv.w + cz.y : zv.w) : 0.f);
+				*(uint32_t *)(sc + c) = cd;
+				const bool m0 = cd & 1u, m1 = cd & 0x100u, m2 = cd & 0x10000u, m3 = cd & 0x1000000u;
+				*(float4 *)(sb + c) = make_float4(m0 ? bv.x : 0.f, m1 ? bv.y : 0.f, m2 ? bv.z : 0.f,
+						m3 ? bv.w : 0.f);
+				*(float4 *)(sz + c) = make_float4(m0 ? (cm0 ? zv.x + cz.x : zv.x) : 0.f,
+						m1 ? (cm0 ? zv.y + cz.x : zv.y) : 0.f, m2 ? (cm1 ? zv.z + cz.y : zv.z) : 0.f,
+						m3 ? (cm1 ? zv.w + cz.y : zv.w) : 0.f);
 			}
 		}
 	} else
@@ -1079,12 +1183,13 @@ __global__ void __launch_bounds__(SP_THREADS) k_post5(const ProbDev *__restrict_
 			const bool in = gi >= 0 && gi < L.w && gj >= 0 && gj < L.h;
 			const size_t k = in ? (size_t)gj * L.w + gi : 0;
 			const size_t kc = in ? (size_t)(gj >> 1) * C.w + (gi >> 1) : 0;
-			const uint8_t m = in ? L.mask[k] : 0;
+			const uint8_t cd = region_code1(in ? L.code[k] : 0, rx, ry);
 			const float bv = in ? L.b[k] : 0.f;
 			const float zv = in ? L.z[k] : 0.f;
 			const uint8_t cm = in ? C.mask[kc] : 0;
 			const float cz = in ? C.z2[kc] : 0.f;
-			sm[c] = m;
+			const bool m = cd & 1;
+			sc[c] = cd;
 			sb[c] = m ? bv : 0.f;
 			sz[c] = m ? (cm ? zv + cz : zv) : 0.f;
 		}
@@ -1092,32 +1197,23 @@ __global__ void __launch_bounds__(SP_THREADS) k_post5(const ProbDev *__restrict_
 	int cells[2][4];
 	own_cells(x0, y0, cells);
 	__syncthreads();
-#pragma unroll
-	for (int it = 0; it < (FN + SP_THREADS - 1) / SP_THREADS; it++) {
-		const int c = threadIdx.x + it * SP_THREADS;
-		if (c < FN) {
-			const int ry = c / FR, rx = c - ry * FR;
-			sc[c] = region_code(sm, c, rx, ry, x0 + rx, y0 + ry, L.w, L.h);
-		}
-	}
-	__syncthreads();
 	// half-sweep s updates colour 1 - (s&1) on the cells of ring >= s + 1
 	for (int s = 0; s < 2 * NU5; s++) {
 		sweep_cells(sz, sb, sc, cells, 1 - (s & 1), s + 1);
 		__syncthreads();
 	}
-	double rz = 0;
+	FF rz = {0.f, 0.f};
 	for (int c = threadIdx.x; c < SP_TILE * SP_TILE; c += SP_THREADS) {
 		const int ty = c >> 5, tx = c & 31, gi = x0 + FH + tx, gj = y0 + FH + ty;
 		if (gi < L.w && gj < L.h) {
 			const int rc = (ty + FH) * FR + tx + FH;
 			L.z2[(size_t)gj * L.w + gi] = sz[rc];
-			if (sm[rc]) rz += (double)sb[rc] * (double)sz[rc];
+			if (sc[rc] & 1) ff_add_prod(rz, sb[rc], sz[rc]);
 		}
 	}
 	if (l != 0 || !pcg) return;
 	double tot[2];
-	if (problem_sum1(rz, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
+	if (problem_sum1_ff(rz, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
 		ProbState &s = st[prob];
 		if (!(tot[0] > 0) || !isfinite(tot[0])) {
 			if (tot[0] != 0) s.status = SIMPOIS_BREAKDOWN;
@@ -1249,99 +1345,151 @@ __device__ void warp_vcycle5(float *const *Z, float *const *B, const uint8_t *co
 // in shared memory: the same sweeps, restriction and injection as the tile
 // kernels, with the coarsest level (<= 4 x 4) getting COARSE_SWEEPS symmetric
 // sweeps.  Reads b of level nfine, writes z2 of level nfine.  When nfine == 0
-// (a problem of at most SMALL_MAX x SMALL_MAX) it also forms r.z and the PCG scalars.
+// (a problem of at most SMALL_MAX x SMALL_MAX) it also takes a pending PCG
+// step first (x += alpha p, r -= alpha q in place, |r|^2 and the convergence
+// test of k_xr, summed in another order) and forms r.z and the PCG scalars.
 __global__ void __launch_bounds__(1024, 1) k_coarse5(const ProbDev *__restrict__ P, ProbState *st, Globals *gl,
-		int pcg)
+		int pcg, int use_p2)
 {
 	extern __shared__ __align__(16) unsigned char smem[];
 	__shared__ double sh[32];
+	__shared__ int stopped;
+	// the level table in shared memory (no per-thread copies)
+	__shared__ int s_w[MAXLEV], s_h[MAXLEV], s_pre[MAXLEV + 1];
+	__shared__ float *s_Z[MAXLEV], *s_B[MAXLEV];
+	__shared__ uint8_t *s_M[MAXLEV];
+	__shared__ const uint8_t *s_gm[MAXLEV];
 	const int prob = blockIdx.x;
 	if (!st[prob].inner_active) return;
 	const ProbDev &pr = P[prob];
 	const int c0 = pr.nfine, L = pr.nlev;
-	int lw[MAXLEV], lh[MAXLEV];
-	for (int l = 0; l < L; l++) { lw[l] = pr.lv[l].w; lh[l] = pr.lv[l].h; }
-	const CoarseLayout cl = coarse_layout(lw, lh, c0, L);
-	auto Zs = [&](int l) { return (float *)(smem + cl.off_z[l]); };
-	auto Bs = [&](int l) { return (float *)(smem + cl.off_b[l]); };
-	auto Ms = [&](int l) { return (uint8_t *)(smem + cl.off_m[l]); };
-	for (int l = c0; l < L; l++) {
-		const uint8_t *gm = pr.lv[l].mask;
-		uint8_t *m = Ms(l);
-		float *z = Zs(l), *b = Bs(l);
-		for (int c = threadIdx.x; c < lw[l] * lh[l]; c += blockDim.x) {
-			const uint8_t mv = gm[c];
-			m[c] = mv;
-			z[c] = 0.f;
-			if (l == c0) b[c] = mv ? pr.lv[l].b[c] : 0.f;
+	const bool upd = c0 == 0 && pcg && st[prob].pending;
+	const float a = upd ? (float)st[prob].alpha : 0.f;
+	const float *pv = use_p2 ? pr.p2 : pr.p;
+	FF rr = {0.f, 0.f};
+	if (threadIdx.x < L) {
+		s_w[threadIdx.x] = pr.lv[threadIdx.x].w;
+		s_h[threadIdx.x] = pr.lv[threadIdx.x].h;
+		s_gm[threadIdx.x] = pr.lv[threadIdx.x].mask;
+	}
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		const CoarseLayout cl = coarse_layout(s_w, s_h, c0, L);
+		int pre = 0;
+		for (int l = c0; l < L; l++) {
+			s_Z[l] = (float *)(smem + cl.off_z[l]);
+			s_B[l] = (float *)(smem + cl.off_b[l]);
+			s_M[l] = (uint8_t *)(smem + cl.off_m[l]);
+			s_pre[l] = pre;
+			pre += s_w[l] * s_h[l];
+		}
+		s_pre[L] = pre;
+		stopped = 0;
+	}
+	__syncthreads();
+	// every level's mask (and b of level c0) in one flat loop: the loads of
+	// successive iterations do not depend on each other
+	const int total = s_pre[L];
+	const float *gb = pr.lv[c0].b;
+#pragma unroll 4
+	for (int q = threadIdx.x; q < total; q += blockDim.x) {
+		int l = c0;
+		while (q >= s_pre[l + 1]) l++;
+		const int c = q - s_pre[l];
+		const uint8_t mv = s_gm[l][c];
+		s_M[l][c] = mv;
+		s_Z[l][c] = 0.f;
+		if (l == c0) {
+			float bv = mv ? gb[c] : 0.f;
+			if (upd && mv) {
+				pr.x[c] = __fmaf_rn(a, pv[c], pr.x[c]);
+				bv = __fmaf_rn(-a, pr.q[c], bv);
+				pr.lv[0].b[c] = bv;
+				ff_add_prod(rr, bv, bv);
+			}
+			s_B[l][c] = bv;
+		}
+	}
+	if (upd) {
+		const double rrs = block_sum_ff<1024>(rr, sh);
+		if (threadIdx.x == 0) {
+			ProbState &s = st[prob];
+			s.rr = rrs;
+			s.iter += 1;
+			s.total_iter += 1;
+			s.pending = 0;
+			if (rrs <= s.tau2 || s.iter >= INNER_MAX || s.total_iter >= s.max_iter) {
+				s.inner_active = 0;
+				atomicSub(&gl->inner_count, 1);
+				stopped = 1;
+			}
 		}
 	}
 	__syncthreads();
-	// levels ls.. hold at most 256 cells: warp 0 runs them alone
+	// levels ls.. hold at most 64 cells: warp 0 runs them alone
 	int ls = c0;
-	while (ls < L - 1 && lw[ls] * lh[ls] > 256) ls++;
+	while (ls < L - 1 && s_w[ls] * s_h[ls] > 64) ls++;
+	const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
 	// down (block-wide levels)
 	for (int l = c0; l < ls; l++) {
-		float *z = Zs(l), *b = Bs(l);
-		const uint8_t *m = Ms(l);
+		float *z = s_Z[l], *b = s_B[l];
+		const uint8_t *m = s_M[l];
+		const int w = s_w[l], h = s_h[l];
 		for (int s = 0; s < NU5; s++) {
-			smem_sweep5(z, b, m, lw[l], lh[l], 0);
-			smem_sweep5(z, b, m, lw[l], lh[l], 1);
+			smem_sweep5(z, b, m, w, h, 0);
+			smem_sweep5(z, b, m, w, h, 1);
 		}
-		float *bc = Bs(l + 1);
-		const uint8_t *mc = Ms(l + 1);
-		const int wc = lw[l + 1], hc = lh[l + 1];
-		for (int c = threadIdx.x; c < wc * hc; c += blockDim.x) {
-			const int cj = c / wc, ci = c - cj * wc;
-			if (!mc[c]) continue;
-			float acc = 0.f;
-			for (int bb = 0; bb < 2; bb++)
-				for (int aa = 0; aa < 2; aa++) {
-					const int fi = 2 * ci + aa, fj = 2 * cj + bb;
-					if (fi < lw[l] && fj < lh[l]) {
-						const int f = fj * lw[l] + fi;
-						acc += b[f] - az5_cell(z, m, f, lw[l], fi, fj, lw[l], lh[l]);
+		float *bc = s_B[l + 1];
+		const uint8_t *mc = s_M[l + 1];
+		const int wc = s_w[l + 1], hc = s_h[l + 1];
+		for (int cj = ty; cj < hc; cj += 32)
+			for (int ci = tx; ci < wc; ci += 32) {
+				const int c = cj * wc + ci;
+				if (!mc[c]) continue;
+				float acc = 0.f;
+				for (int bb = 0; bb < 2; bb++)
+					for (int aa = 0; aa < 2; aa++) {
+						const int fi = 2 * ci + aa, fj = 2 * cj + bb;
+						if (fi < w && fj < h) {
+							const int f = fj * w + fi;
+							acc += b[f] - az5_cell(z, m, f, w, fi, fj, w, h);
+						}
 					}
-				}
-			bc[c] = 1.f * acc;
-		}
+				bc[c] = 1.f * acc;
+			}
 		__syncthreads();
 	}
-	if (threadIdx.x < 32) {
-		float *Z[MAXLEV], *B[MAXLEV];
-		const uint8_t *M[MAXLEV];
-		for (int l = ls; l < L; l++) { Z[l] = Zs(l); B[l] = Bs(l); M[l] = Ms(l); }
-		warp_vcycle5(Z, B, M, lw, lh, ls, L);
-	}
+	if (threadIdx.x < 32) warp_vcycle5(s_Z, s_B, s_M, s_w, s_h, ls, L);
 	__syncthreads();
 	// up (block-wide levels)
 	for (int l = ls - 1; l >= c0; l--) {
-		float *z = Zs(l), *b = Bs(l);
-		const uint8_t *m = Ms(l);
-		const float *zc = Zs(l + 1);
-		const uint8_t *mc = Ms(l + 1);
-		const int wc = lw[l + 1];
-		for (int c = threadIdx.x; c < lw[l] * lh[l]; c += blockDim.x) {
-			const int j = c / lw[l], i = c - j * lw[l];
-			const int kc = (j >> 1) * wc + (i >> 1);
-			if (m[c] && mc[kc]) z[c] += zc[kc];
-		}
+		float *z = s_Z[l], *b = s_B[l];
+		const uint8_t *m = s_M[l];
+		const float *zc = s_Z[l + 1];
+		const uint8_t *mc = s_M[l + 1];
+		const int w = s_w[l], h = s_h[l], wc = s_w[l + 1];
+		for (int j = ty; j < h; j += 32)
+			for (int i = tx; i < w; i += 32) {
+				const int c = j * w + i, kc = (j >> 1) * wc + (i >> 1);
+				if (m[c] && mc[kc]) z[c] += zc[kc];
+			}
 		__syncthreads();
 		for (int s = 0; s < NU5; s++) {
-			smem_sweep5(z, b, m, lw[l], lh[l], 1);
-			smem_sweep5(z, b, m, lw[l], lh[l], 0);
+			smem_sweep5(z, b, m, w, h, 1);
+			smem_sweep5(z, b, m, w, h, 0);
 		}
 	}
-	const float *z = Zs(c0), *b = Bs(c0);
-	const uint8_t *m = Ms(c0);
-	double rz = 0;
-	for (int c = threadIdx.x; c < lw[c0] * lh[c0]; c += blockDim.x) {
-		pr.lv[c0].z2[c] = m[c] ? z[c] : 0.f;
-		if (m[c]) rz += (double)b[c] * (double)z[c];
+	const float *z = s_Z[c0], *b = s_B[c0];
+	const uint8_t *m = s_M[c0];
+	float *gz2 = pr.lv[c0].z2;
+	FF rzf = {0.f, 0.f};
+	for (int c = threadIdx.x; c < s_w[c0] * s_h[c0]; c += blockDim.x) {
+		gz2[c] = m[c] ? z[c] : 0.f;
+		if (m[c]) ff_add_prod(rzf, b[c], z[c]);
 	}
 	if (c0 != 0 || !pcg) return;
-	rz = block_sum<1024>(rz, sh);
-	if (threadIdx.x == 0) {
+	const double rz = block_sum_ff<1024>(rzf, sh);
+	if (threadIdx.x == 0 && !stopped) {
 		ProbState &s = st[prob];
 		if (!(rz > 0) || !isfinite(rz)) {
 			if (rz != 0) s.status = SIMPOIS_BREAKDOWN;
@@ -1357,13 +1505,18 @@ __global__ void __launch_bounds__(1024, 1) k_coarse5(const ProbDev *__restrict__
 // p_new = z + beta p_old on the tile and a 1-pixel halo (as k_pupdate), then
 // q = A p_new and alpha = rho / (p_new . q) (as k_spmv<0>).  p_old and p_new
 // are different buffers (the halo of a neighbour must still see p_old).
-__global__ void __launch_bounds__(SP_THREADS) k_spmv5(const ProbDev *__restrict__ P, ProbState *st,
+// When the level width is a multiple of 4 the region is 40 x 34 (4-aligned
+// columns) and moves in groups of 4 cells, each thread then applying A to 4
+// cells of a row; the products p.q are summed in k_spmv<0>'s order.
+__global__ void __launch_bounds__(SP_THREADS, 8) k_spmv5(const ProbDev *__restrict__ P, ProbState *st,
 		const int4 *__restrict__ tl, const int *__restrict__ tbeg, const int *__restrict__ tcnt, double *partial,
 		Globals *gl, int new_is_p2)
 {
-	constexpr int R = SP_TILE + 2, N = R * R;
-	__shared__ float sp[N];
-	__shared__ uint8_t sm[N];
+	constexpr int R = SP_TILE + 2;                       // scalar region: 34 x 34
+	constexpr int RW = SP_TILE + 8, RH = SP_TILE + 2;    // vector region: 40 x 34
+	__shared__ __align__(16) float sp[RW * RH];
+	__shared__ __align__(16) uint8_t sc[RW * RH];
+	__shared__ float2 spq[SP_TILE * SP_TILE];   // (p, q) of the unknown tile cells
 	__shared__ double sh[32];
 	const int4 t = tl[blockIdx.x];
 	const int prob = t.x;
@@ -1373,37 +1526,86 @@ __global__ void __launch_bounds__(SP_THREADS) k_spmv5(const ProbDev *__restrict_
 	const float beta = (float)st[prob].beta;
 	const float *pold = new_is_p2 ? pr.p : pr.p2;
 	float *pnew = new_is_p2 ? pr.p2 : pr.p;
-	const int x0 = t.y * SP_TILE - 1, y0 = t.z * SP_TILE - 1;
+	FF pq = {0.f, 0.f};
+	if ((L.w & 3) == 0) {
+		const int x0 = t.y * SP_TILE - 4, y0 = t.z * SP_TILE - 1;
 #pragma unroll
-	for (int it = 0; it < (N + SP_THREADS - 1) / SP_THREADS; it++) {
-		const int c = threadIdx.x + it * SP_THREADS;
-		if (c < N) {
-			const int ry = c / R, rx = c - ry * R, gi = x0 + rx, gj = y0 + ry;
-			const bool in = gi >= 0 && gi < L.w && gj >= 0 && gj < L.h;
-			const size_t k = in ? (size_t)gj * L.w + gi : 0;
-			const uint8_t m = in ? L.mask[k] : 0;
-			const float zv = in ? L.z2[k] : 0.f;
-			const float po = (in && beta != 0.f) ? pold[k] : 0.f;
-			sm[c] = m;
-			sp[c] = m ? (beta != 0.f ? zv + beta * po : zv) : 0.f;
+		for (int it = 0; it < (RW * RH / 4 + SP_THREADS - 1) / SP_THREADS; it++) {
+			const int f = threadIdx.x + it * SP_THREADS;
+			if (f < RW * RH / 4) {
+				const int ry = f / (RW / 4), rx = 4 * (f - ry * (RW / 4)), gi = x0 + rx, gj = y0 + ry;
+				const bool in = gi >= 0 && gi < L.w && gj >= 0 && gj < L.h;
+				const size_t k = in ? (size_t)gj * L.w + gi : 0;
+				uint32_t cd = 0;
+				float4 zv = make_float4(0.f, 0.f, 0.f, 0.f), po = zv;
+				if (in) {
+					cd = *(const uint32_t *)(L.code + k);
+					zv = *(const float4 *)(L.z2 + k);
+					if (beta != 0.f) po = *(const float4 *)(pold + k);
+				}
+				const int c = ry * RW + rx;
+				*(uint32_t *)(sc + c) = cd;
+				*(float4 *)(sp + c) = make_float4((cd & 1u) ? (beta != 0.f ? zv.x + beta * po.x : zv.x) : 0.f,
+						(cd & 0x100u) ? (beta != 0.f ? zv.y + beta * po.y : zv.y) : 0.f,
+						(cd & 0x10000u) ? (beta != 0.f ? zv.z + beta * po.z : zv.z) : 0.f,
+						(cd & 0x1000000u) ? (beta != 0.f ? zv.w + beta * po.w : zv.w) : 0.f);
+			}
 		}
-	}
-	__syncthreads();
-	double pq = 0;
-	for (int c = threadIdx.x; c < SP_TILE * SP_TILE; c += SP_THREADS) {
-		const int ty = c >> 5, tx = c & 31, gi = x0 + 1 + tx, gj = y0 + 1 + ty;
-		const int rc = (ty + 1) * R + tx + 1;
-		if (gi < L.w && gj < L.h && sm[rc]) {
+		__syncthreads();
+		// 4 cells of a row per thread (every neighbour is in the region)
+		const int ty = threadIdx.x >> 3, tx = 4 * (threadIdx.x & 7);
+		const int gi = t.y * SP_TILE + tx, gj = t.z * SP_TILE + ty;
+		const int c = (ty + 1) * RW + tx + 4;
+		float pk[4], qk[4];
+#pragma unroll
+		for (int e = 0; e < 4; e++) {
+			const int code = sc[c + e];
+			pk[e] = sp[c + e];
+			qk[e] = 0.f;
+			if (code & 1) qk[e] = diag_code(code) * pk[e] + off_code(sp, c + e, RW, code);
+			spq[ty * SP_TILE + tx + e] = make_float2(pk[e], qk[e]);
+		}
+		if (gi < L.w && gj < L.h) {
 			const size_t k = (size_t)gj * L.w + gi;
-			const float pk = sp[rc];
-			const float qk = az5_cell(sp, sm, rc, R, gi, gj, L.w, L.h);
-			pnew[k] = pk;
-			pr.q[k] = qk;
-			pq += (double)pk * (double)qk;
+			*(float4 *)(pnew + k) = make_float4(pk[0], pk[1], pk[2], pk[3]);
+			*(float4 *)(pr.q + k) = make_float4(qk[0], qk[1], qk[2], qk[3]);
+		}
+		__syncthreads();
+		for (int q = threadIdx.x; q < SP_TILE * SP_TILE; q += SP_THREADS)
+			if (sc[((q >> 5) + 1) * RW + (q & 31) + 4] & 1) ff_add_prod(pq, spq[q].x, spq[q].y);
+	} else {
+		uint8_t *sm = sc;
+		const int x0 = t.y * SP_TILE - 1, y0 = t.z * SP_TILE - 1;
+#pragma unroll
+		for (int it = 0; it < (R * R + SP_THREADS - 1) / SP_THREADS; it++) {
+			const int c = threadIdx.x + it * SP_THREADS;
+			if (c < R * R) {
+				const int ry = c / R, rx = c - ry * R, gi = x0 + rx, gj = y0 + ry;
+				const bool in = gi >= 0 && gi < L.w && gj >= 0 && gj < L.h;
+				const size_t k = in ? (size_t)gj * L.w + gi : 0;
+				const uint8_t m = in ? L.mask[k] : 0;
+				const float zv = in ? L.z2[k] : 0.f;
+				const float po = (in && beta != 0.f) ? pold[k] : 0.f;
+				sm[c] = m;
+				sp[c] = m ? (beta != 0.f ? zv + beta * po : zv) : 0.f;
+			}
+		}
+		__syncthreads();
+		for (int c = threadIdx.x; c < SP_TILE * SP_TILE; c += SP_THREADS) {
+			const int ty = c >> 5, tx = c & 31, gi = x0 + 1 + tx, gj = y0 + 1 + ty;
+			const int rc = (ty + 1) * R + tx + 1;
+			if (gi < L.w && gj < L.h && sm[rc]) {
+				const size_t k = (size_t)gj * L.w + gi;
+				const float pk = sp[rc];
+				const float qk = az5_cell(sp, sm, rc, R, gi, gj, L.w, L.h);
+				pnew[k] = pk;
+				pr.q[k] = qk;
+				ff_add_prod(pq, pk, qk);
+			}
 		}
 	}
 	double tot[2];
-	if (problem_sum1(pq, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
+	if (problem_sum1_ff(pq, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
 		ProbState &s = st[prob];
 		double a = s.rho / tot[0];
 		if (!(tot[0] > 0) || !isfinite(a)) {
@@ -1413,6 +1615,7 @@ __global__ void __launch_bounds__(SP_THREADS) k_spmv5(const ProbDev *__restrict_
 			atomicSub(&gl->inner_count, 1);
 		} else {
 			s.alpha = a;
+			s.pending = 1;   // k_pre5 (or k_coarse5) at level 0 takes the step
 		}
 	}
 }
@@ -1751,6 +1954,7 @@ constexpr double BPX_PRE5 = 1 + 4 + 4 + 0.25 + 1;         // mask, b, z; coarse 
 constexpr double BPX_POST5 = 1 + 4 + 4 + 1 + 0.25 + 4;    // mask, b, z, coarse z2, coarse mask; z2
 constexpr double BPX_SPMV5 = 1 + 4 + 4 + 4 + 4;           // mask, z2, p_old; p_new, q
 constexpr double BPX_XR = 1 + 4 + 4 + 4 + 4 + 4 + 4;      // mask, x, p, b, q; x, b
+constexpr double BPX_STEP = 4 + 4 + 4 + 4 + 4;            // k_pre5's PCG step: q, x, p; x, r
 constexpr double BPX_RESID64 = 1 + 8 + 4 + 4 + 4;         // mask, U, rhs; b, x
 constexpr double BPX_UADD = 1 + 8 + 4 + 8;                // mask, U, x; U
 constexpr double BPC_COARSE5 = 1 + 4 + 4 + 0.34;          // per top coarse cell: mask, b; z2; coarser masks
@@ -1848,19 +2052,22 @@ void kt_refresh(const Plan &pl, cudaStream_t s)
 }
 
 // pcg = 0: the cycle is half of the biharmonic preconditioner and leaves the
-// 5-point PCG scalars alone.
-void launch_vcycle_fused(const Plan &pl, cudaStream_t s, int pcg = 1)
+// 5-point PCG scalars alone.  step: the cycle follows k_spmv5 (whose search
+// direction is p2 when use_p2), so level 0 first takes the pending PCG step;
+// it only changes the kernel timer's byte count (the kernels read `pending`).
+void launch_vcycle_fused(const Plan &pl, cudaStream_t s, int pcg = 1, int use_p2 = 0, int step = 0)
 {
 	kt_refresh(pl, s);
 	for (int l = 0; l < pl.nfine_max; l++) {
 		if (!pl.nact[l]) continue;
 		KT_BEGIN(pl, s);
-		k_pre5<<<pl.nact[l], SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[l], l); ++*pl.nl;
-		KT_END(pl, s, "k_pre5", pl.kt->px(l) * BPX_PRE5);
+		k_pre5<<<pl.nact[l], SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[l], l, pl.tbeg, pl.tcnt, pl.partial,
+				pl.gl, use_p2); ++*pl.nl;
+		KT_END(pl, s, "k_pre5", pl.kt->px(l) * (BPX_PRE5 + (l == 0 && step ? BPX_STEP : 0.0)));
 	}
 	{
 		KT_BEGIN(pl, s);
-		k_coarse5<<<pl.n, 1024, pl.coarse_smem, s>>>(pl.dp, pl.dst, pl.gl, pcg); ++*pl.nl;
+		k_coarse5<<<pl.n, 1024, pl.coarse_smem, s>>>(pl.dp, pl.dst, pl.gl, pcg, use_p2); ++*pl.nl;
 		KT_END(pl, s, "k_coarse5", pl.kt->cells() * BPC_COARSE5);
 	}
 	for (int l = pl.nfine_max - 1; l >= 0; l--) {
@@ -1912,13 +2119,7 @@ void launch_iteration_fused(const Plan &pl, cudaStream_t s)
 					parity); ++*pl.nl;
 			KT_END(pl, s, "k_spmv5", pl.kt->px(0) * BPX_SPMV5);
 		}
-		{
-			KT_BEGIN(pl, s);
-			k_xr<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl,
-					parity); ++*pl.nl;
-			KT_END(pl, s, "k_xr", pl.kt->px(0) * BPX_XR);
-		}
-		launch_vcycle_fused(pl, s);
+		launch_vcycle_fused(pl, s, 1, parity, 1);
 	}
 }
 
@@ -2201,8 +2402,8 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	pl.hp.resize(n);
 	int kinds = 0;
 	Layout Lo;
-	std::vector<size_t> off_mask[MAXLEV], off_b[MAXLEV], off_z[MAXLEV], off_z2[MAXLEV];
-	std::vector<size_t> off_U(n), off_x(n), off_p(n), off_q(n), off_p2(n);
+	std::vector<size_t> off_mask[MAXLEV], off_code[MAXLEV], off_b[MAXLEV], off_z[MAXLEV], off_z2[MAXLEV];
+	std::vector<size_t> off_U(n), off_x(n), off_p(n), off_q(n), off_p2(n), off_balt(n);
 	std::vector<size_t> off_r64(n, 0), off_p64(n, 0), off_q64(n, 0);
 	std::vector<std::vector<int4>> lists(MAXLEV);
 	const int cmax = opt.coarse_max > 0 ? clamp_coarse_max(opt.coarse_max) : default_coarse_max();
@@ -2225,6 +2426,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 			d.lv[l].w = lw[l];
 			d.lv[l].h = lh[l];
 			off_mask[l].push_back(Lo.take(px));
+			off_code[l].push_back(Lo.take(px));
 			off_b[l].push_back(Lo.take(px * 4));
 			off_z[l].push_back(Lo.take(px * 4));
 			off_z2[l].push_back(Lo.take(px * 4));
@@ -2233,6 +2435,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 		}
 		for (int l = nl; l < MAXLEV; l++) {
 			off_mask[l].push_back(0);
+			off_code[l].push_back(0);
 			off_b[l].push_back(0);
 			off_z[l].push_back(0);
 			off_z2[l].push_back(0);
@@ -2247,6 +2450,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 		off_p[k] = Lo.take(px * 4);
 		off_q[k] = Lo.take(px * 4);
 		off_p2[k] = Lo.take(px * 4);
+		off_balt[k] = Lo.take(px * 4);
 		if (q.kind == 1 && opt.fused && opt.use_mg) {   // FP64 Krylov vectors of the biharmonic PCG
 			off_r64[k] = Lo.take(px * 8);
 			off_p64[k] = Lo.take(px * 8);
@@ -2309,11 +2513,13 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 		d.p = (float *)(A + off_p[k]);
 		d.q = (float *)(A + off_q[k]);
 		d.p2 = (float *)(A + off_p2[k]);
+		d.b_alt = (float *)(A + off_balt[k]);
 		d.r64 = off_r64[k] ? (double *)(A + off_r64[k]) : nullptr;
 		d.p64 = off_p64[k] ? (double *)(A + off_p64[k]) : nullptr;
 		d.q64 = off_q64[k] ? (double *)(A + off_q64[k]) : nullptr;
 		for (int l = 0; l < d.nlev; l++) {
 			d.lv[l].mask = (uint8_t *)(A + off_mask[l][k]);
+			d.lv[l].code = (uint8_t *)(A + off_code[l][k]);
 			d.lv[l].b = (float *)(A + off_b[l][k]);
 			d.lv[l].z = (float *)(A + off_z[l][k]);
 			d.lv[l].z2 = (float *)(A + off_z2[l][k]);
