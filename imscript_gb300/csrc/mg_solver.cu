@@ -71,8 +71,12 @@ struct ProbDev {
 	const float *g;      // input channel
 	const float *rhs;    // fill: f (sign -1) ; adjoint: grad_out (sign +1)
 	float rhs_sign;
+	int known_zero;      // adjoint: the known pixels hold 0 (fill: g)
+	int vec4;            // w % 4 == 0 and g, out 16-byte aligned: setup and
+	                     // finalize move 4-pixel groups with vector accesses
 	float *out;
-	double *U;           // FP64 solution image (g or 0 at the known pixels)
+	double *U;           // FP64 solution at the unknown pixels (the known ones
+	                     // are read from g: see known_at)
 	float *x, *p, *q;    // level-0 PCG vectors
 	float *p2;           // fused path: second search-direction buffer
 	float *b_alt;        // fused path: the other level-0 residual buffer (k_pre5
@@ -152,15 +156,22 @@ __device__ __forceinline__ void split(const LevelDev &L, const float *__restrict
 	}
 }
 
-// A ufull at (i, j) in FP64 on a full image (known pixels included); when
-// `zero_unknown`, unknown pixels read as 0 (this gives A_UK g_K).
+// The FP64 solution image at pixel q: U at the unknowns, the known value
+// (g, or 0 for the adjoint) elsewhere.
+__device__ __forceinline__ double known_at(const double *__restrict__ U, const uint8_t *__restrict__ m,
+		const float *__restrict__ g, int known_zero, size_t q)
+{
+	return m[q] ? U[q] : (known_zero ? 0.0 : (double)g[q]);
+}
+
+// A u at (i, j) in FP64 on the full image (known pixels included, with the
+// clamp-to-edge extension).
 template <int K>
 __device__ __forceinline__ double apply64(const double *__restrict__ U, const uint8_t *__restrict__ m,
-		int w, int h, int i, int j, bool zero_unknown)
+		const float *__restrict__ g, int known_zero, int w, int h, int i, int j)
 {
 	auto at = [&](int a, int b) -> double {
-		int q = clampi(b, h) * w + clampi(a, w);
-		return (zero_unknown && m[q]) ? 0.0 : U[q];
+		return known_at(U, m, g, known_zero, (size_t)clampi(b, h) * w + clampi(a, w));
 	};
 	if (K == 0) return 4.0 * at(i, j) - at(i + 1, j) - at(i, j + 1) - at(i - 1, j) - at(i, j - 1);
 	double r = 20.0 * at(i, j);
@@ -252,44 +263,91 @@ __device__ bool problem_sum1_ff(FF v0, int prob, const int *__restrict__ tbeg, c
 
 // ------------------------------------------------------------------ setup kernels
 
-// Level 0 over all tiles: mask = isnan(g); U = g at the knowns (fill) or 0
-// (adjoint), 0 at the unknowns; flag = tile holds an unknown; per-problem
-// pixel counts.
-__global__ void k_setup0(const ProbDev *__restrict__ P, ProbState *st, const int4 *__restrict__ all,
-		int *__restrict__ flag, int adjoint)
+// Tiles per block of the passes over every tile (setup, finalize): each
+// thread takes a 4-pixel row group of each of its block's tiles, and every
+// load is issued before the first store.
+constexpr int TPB = 4;
+
+// The row group of tile t a thread covers: first pixel k and its pixel count
+// (0 when the group lies outside the image).
+__device__ __forceinline__ int group_of(const ProbDev &pr, int4 t, size_t &k)
 {
-	__shared__ int cnt[2];
-	int4 t = all[blockIdx.x];
-	const ProbDev &pr = P[t.x];
-	if (threadIdx.x < 2) cnt[threadIdx.x] = 0;
-	__syncthreads();
-	int i = tile_i(t);
-	int nu = 0, nk = 0;
-	for (int r = 0; r < SP_ROWS; r++) {
-		int j = tile_j(t, r);
-		if (i < pr.w && j < pr.h) {
-			size_t k = (size_t)j * pr.w + i;
-			float gv = pr.g[k];
-			bool u = isnan(gv);
-			pr.lv[0].mask[k] = u;
-			pr.U[k] = (u || adjoint) ? 0.0 : (double)gv;
-			nu += u;
-			nk += !u;
+	const int i = t.y * SP_TILE + 4 * (threadIdx.x & 7), j = t.z * SP_TILE + (threadIdx.x >> 3);
+	if (i >= pr.w || j >= pr.h) return 0;
+	k = (size_t)j * pr.w + i;
+	return min(4, pr.w - i);
+}
+
+// Level 0 over all tiles: mask = isnan(g); U = 0 at the unknowns; flag =
+// tile holds an unknown; per-problem pixel counts.
+__global__ void __launch_bounds__(SP_THREADS) k_setup0(const ProbDev *__restrict__ P, ProbState *st,
+		const int4 *__restrict__ all, int nall, int *__restrict__ flag)
+{
+	__shared__ int cnt[TPB][2];
+	if (threadIdx.x < 2 * TPB) cnt[threadIdx.x >> 1][threadIdx.x & 1] = 0;
+	int4 tt[TPB];
+	size_t kk[TPB];
+	int nv[TPB];
+	float gv[TPB][4];
+#pragma unroll
+	for (int q = 0; q < TPB; q++) {
+		const int b = blockIdx.x * TPB + q;
+		tt[q] = b < nall ? all[b] : make_int4(-1, 0, 0, 0);
+	}
+#pragma unroll
+	for (int q = 0; q < TPB; q++) {
+		nv[q] = 0;
+		kk[q] = 0;
+		if (tt[q].x < 0) continue;
+		const ProbDev &pr = P[tt[q].x];
+		nv[q] = group_of(pr, tt[q], kk[q]);
+		if (nv[q] == 4 && pr.vec4) {
+			const float4 v = *(const float4 *)(pr.g + kk[q]);
+			gv[q][0] = v.x; gv[q][1] = v.y; gv[q][2] = v.z; gv[q][3] = v.w;
+		} else {
+#pragma unroll
+			for (int e = 0; e < 4; e++) gv[q][e] = e < nv[q] ? pr.g[kk[q] + e] : 0.f;
 		}
 	}
-	for (int o = 16; o > 0; o >>= 1) {
-		nu += __shfl_down_sync(0xffffffffu, nu, o);
-		nk += __shfl_down_sync(0xffffffffu, nk, o);
-	}
-	if ((threadIdx.x & 31) == 0) {
-		atomicAdd(&cnt[0], nu);
-		atomicAdd(&cnt[1], nk);
+	__syncthreads();   // cnt is zeroed
+#pragma unroll
+	for (int q = 0; q < TPB; q++) {
+		int nu = 0, nk = 0;
+		if (nv[q]) {
+			const ProbDev &pr = P[tt[q].x];
+			uint32_t mw = 0;
+#pragma unroll
+			for (int e = 0; e < 4; e++) {
+				if (e >= nv[q]) break;
+				const bool u = isnan(gv[q][e]);
+				nu += u;
+				nk += !u;
+				if (u) pr.U[kk[q] + e] = 0.0;   // known pixels: read from g when needed
+				mw |= (uint32_t)u << (8 * e);
+			}
+			if (nv[q] == 4 && (pr.w & 3) == 0) {   // the mask lives in the arena
+				*(uint32_t *)(pr.lv[0].mask + kk[q]) = mw;
+			} else {
+				for (int e = 0; e < nv[q]; e++) pr.lv[0].mask[kk[q] + e] = (mw >> (8 * e)) & 1u;
+			}
+		}
+		for (int o = 16; o > 0; o >>= 1) {
+			nu += __shfl_down_sync(0xffffffffu, nu, o);
+			nk += __shfl_down_sync(0xffffffffu, nk, o);
+		}
+		if ((threadIdx.x & 31) == 0 && (nu || nk)) {
+			atomicAdd(&cnt[q][0], nu);
+			atomicAdd(&cnt[q][1], nk);
+		}
 	}
 	__syncthreads();
-	if (threadIdx.x == 0) {
-		flag[blockIdx.x] = cnt[0] > 0;
-		if (cnt[0]) atomicAdd(&st[t.x].nunknown, cnt[0]);
-		if (cnt[1]) atomicAdd(&st[t.x].nknown, cnt[1]);
+	if (threadIdx.x < TPB) {
+		const int q = threadIdx.x, b = blockIdx.x * TPB + q;
+		if (b < nall) {
+			flag[b] = cnt[q][0] > 0;
+			if (cnt[q][0]) atomicAdd(&st[tt[q].x].nunknown, cnt[q][0]);
+			if (cnt[q][1]) atomicAdd(&st[tt[q].x].nknown, cnt[q][1]);
+		}
 	}
 }
 
@@ -337,9 +395,38 @@ __global__ void k_mask_down(const ProbDev *__restrict__ P, const int4 *__restric
 	__syncthreads();
 	if (threadIdx.x == 0) flag[blockIdx.x] = any;
 	// the mask of level l-1 is complete: its cell codes under this tile
-	for (int q = threadIdx.x; q < 4 * SP_TILE * SP_TILE; q += SP_THREADS) {
-		const int fi = 2 * SP_TILE * t.y + (q & (2 * SP_TILE - 1)), fj = 2 * SP_TILE * t.z + q / (2 * SP_TILE);
-		if (fi < F.w && fj < F.h) F.code[(size_t)fj * F.w + fi] = cell_code(F.mask, fi, fj, F.w, F.h);
+	if ((F.w & 3) == 0) {
+		// 4 cells of a row per step: 3 word loads and 2 byte loads for 4 codes
+		for (int q = threadIdx.x; q < SP_TILE * SP_TILE; q += SP_THREADS) {
+			const int fi = 2 * SP_TILE * t.y + 4 * (q & (SP_TILE / 2 - 1)), fj = 2 * SP_TILE * t.z + q / (SP_TILE / 2);
+			if (fi >= F.w || fj >= F.h) continue;
+			const size_t k = (size_t)fj * F.w + fi;
+			const uint32_t mc = *(const uint32_t *)(F.mask + k);
+			const uint32_t mn = fj > 0 ? *(const uint32_t *)(F.mask + k - F.w) : 0u;
+			const uint32_t ms = fj + 1 < F.h ? *(const uint32_t *)(F.mask + k + F.w) : 0u;
+			const uint32_t ml = fi > 0 ? F.mask[k - 1] : 0u, mr = fi + 4 < F.w ? F.mask[k + 4] : 0u;
+			uint32_t out = 0;
+#pragma unroll
+			for (int e = 0; e < 4; e++) {
+				if (!((mc >> (8 * e)) & 1u)) continue;
+				uint32_t code = 1, nd = 0;
+				if (e < 3) { if ((mc >> (8 * e + 8)) & 1u) code |= 2; }
+				else if (fi + 4 < F.w) { if (mr) code |= 2; }
+				else nd++;
+				if (e > 0) { if ((mc >> (8 * e - 8)) & 1u) code |= 4; }
+				else if (fi > 0) { if (ml) code |= 4; }
+				else nd++;
+				if (fj + 1 < F.h) { if ((ms >> (8 * e)) & 1u) code |= 8; } else nd++;
+				if (fj > 0) { if ((mn >> (8 * e)) & 1u) code |= 16; } else nd++;
+				out |= (code | (nd << 5)) << (8 * e);
+			}
+			*(uint32_t *)(F.code + k) = out;
+		}
+	} else {
+		for (int q = threadIdx.x; q < 4 * SP_TILE * SP_TILE; q += SP_THREADS) {
+			const int fi = 2 * SP_TILE * t.y + (q & (2 * SP_TILE - 1)), fj = 2 * SP_TILE * t.z + q / (2 * SP_TILE);
+			if (fi < F.w && fj < F.h) F.code[(size_t)fj * F.w + fi] = cell_code(F.mask, fi, fj, F.w, F.h);
+		}
 	}
 }
 
@@ -413,20 +500,19 @@ __global__ void k_resid64(const ProbDev *__restrict__ P, ProbState *st, const in
 		const size_t k = in ? (size_t)j * w + i : 0;
 		const uint8_t m = in ? L.mask[k] : 0;
 		double rk = 0;
-		if (K == 0) {
-			// the five loads do not depend on the mask: all in flight together
+		if (K == 0 && m) {
 			const int ie = i + 1 < w ? i + 1 : i, iw = i > 0 ? i - 1 : i;
 			const int js = j + 1 < h ? j + 1 : j, jn = j > 0 ? j - 1 : j;
-			const double uc = in ? pr.U[k] : 0.0;
-			const double ue = in ? pr.U[(size_t)j * w + ie] : 0.0;
-			const double us = in ? pr.U[(size_t)js * w + i] : 0.0;
-			const double uw = in ? pr.U[(size_t)j * w + iw] : 0.0;
-			const double un = in ? pr.U[(size_t)jn * w + i] : 0.0;
-			const double s = (in && pr.rhs) ? (double)pr.rhs_sign * (double)pr.rhs[k] : 0.0;
+			const double uc = pr.U[k];
+			const double ue = known_at(pr.U, L.mask, pr.g, pr.known_zero, (size_t)j * w + ie);
+			const double us = known_at(pr.U, L.mask, pr.g, pr.known_zero, (size_t)js * w + i);
+			const double uw = known_at(pr.U, L.mask, pr.g, pr.known_zero, (size_t)j * w + iw);
+			const double un = known_at(pr.U, L.mask, pr.g, pr.known_zero, (size_t)jn * w + i);
+			const double s = pr.rhs ? (double)pr.rhs_sign * (double)pr.rhs[k] : 0.0;
 			rk = s - (4.0 * uc - ue - us - uw - un);
 		} else if (m) {
 			const double s = pr.rhs ? (double)pr.rhs_sign * (double)pr.rhs[k] : 0.0;
-			rk = s - apply64<K>(pr.U, L.mask, w, h, i, j, false);
+			rk = s - apply64<K>(pr.U, L.mask, pr.g, pr.known_zero, w, h, i, j);
 		}
 		if (m) {
 			if (pr.r64) {
@@ -827,6 +913,9 @@ __global__ void k_coarsest(const ProbDev *__restrict__ P, const ProbState *__res
 constexpr int FH = 2 * NU5;           // halo: one pixel per half-sweep
 constexpr int FR = SP_TILE + 2 * FH;  // side of the shared region (40)
 constexpr int FN = FR * FR;
+// the vectorised region loads move aligned groups of 4 cells: the region's
+// first column (tile x - FH) and its width must be multiples of 4
+static_assert(FH % 4 == 0 && FR % 4 == 0, "region columns must stay 4-aligned");
 // FP32 inner solves stop at this relative decrease at the latest (the FP32
 // recurrence drifts below it); SIMPOIS_TAU_MIN overrides it for tuning.
 double tau_min()
@@ -1786,17 +1875,51 @@ __global__ void k_xr64(const ProbDev *__restrict__ P, ProbState *st, const int4 
 }
 
 // out = unknown ? (float)U : g over all tiles (fill)
-__global__ void k_finalize(const ProbDev *__restrict__ P, const int4 *__restrict__ all)
+__global__ void __launch_bounds__(SP_THREADS) k_finalize(const ProbDev *__restrict__ P,
+		const int4 *__restrict__ all, int nall)
 {
-	int4 t = all[blockIdx.x];
-	const ProbDev &pr = P[t.x];
-	int i = tile_i(t);
-	for (int r = 0; r < SP_ROWS; r++) {
-		int j = tile_j(t, r);
-		if (i < pr.w && j < pr.h) {
-			size_t k = (size_t)j * pr.w + i;
-			pr.out[k] = pr.lv[0].mask[k] ? (float)pr.U[k] : pr.g[k];
+	int4 tt[TPB];
+	size_t kk[TPB];
+	int nv[TPB];
+	float gv[TPB][4];
+	uint32_t mw[TPB];
+#pragma unroll
+	for (int q = 0; q < TPB; q++) {
+		const int b = blockIdx.x * TPB + q;
+		tt[q] = b < nall ? all[b] : make_int4(-1, 0, 0, 0);
+	}
+#pragma unroll
+	for (int q = 0; q < TPB; q++) {
+		nv[q] = 0;
+		kk[q] = 0;
+		mw[q] = 0;
+		if (tt[q].x < 0) continue;
+		const ProbDev &pr = P[tt[q].x];
+		nv[q] = group_of(pr, tt[q], kk[q]);
+		if (nv[q] == 4 && pr.vec4) {
+			const float4 v = *(const float4 *)(pr.g + kk[q]);
+			gv[q][0] = v.x; gv[q][1] = v.y; gv[q][2] = v.z; gv[q][3] = v.w;
+			mw[q] = *(const uint32_t *)(pr.lv[0].mask + kk[q]);
+		} else {
+#pragma unroll
+			for (int e = 0; e < 4; e++) {
+				gv[q][e] = e < nv[q] ? pr.g[kk[q] + e] : 0.f;
+				mw[q] |= (e < nv[q] ? (uint32_t)pr.lv[0].mask[kk[q] + e] : 0u) << (8 * e);
+			}
 		}
+	}
+#pragma unroll
+	for (int q = 0; q < TPB; q++) {
+		if (!nv[q]) continue;
+		const ProbDev &pr = P[tt[q].x];
+		float v[4];
+#pragma unroll
+		for (int e = 0; e < 4; e++)   // U is read (and converted) at the unknowns only
+			v[e] = ((mw[q] >> (8 * e)) & 1u) ? (float)pr.U[kk[q] + e] : gv[q][e];
+		if (nv[q] == 4 && pr.vec4)
+			*(float4 *)(pr.out + kk[q]) = make_float4(v[0], v[1], v[2], v[3]);
+		else
+			for (int e = 0; e < nv[q]; e++) pr.out[kk[q] + e] = v[e];
 	}
 }
 
@@ -2501,12 +2624,15 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 		const MgProblem &q = probs[k];
 		d.g = q.g;
 		d.out = q.out;
+		d.vec4 = q.w % 4 == 0 && ((uintptr_t)q.g & 15) == 0 && ((uintptr_t)q.out & 15) == 0;
 		if (opt.mode == MG_ADJOINT) {
 			d.rhs = opt.grad_out[k];
 			d.rhs_sign = 1.f;
+			d.known_zero = 1;
 		} else {
 			d.rhs = q.f;
 			d.rhs_sign = -1.f;
+			d.known_zero = 0;
 		}
 		d.U = (double *)(A + off_U[k]);
 		d.x = (float *)(A + off_x[k]);
@@ -2582,7 +2708,8 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	}
 
 	// masks, tile flags, compacted lists
-	k_setup0<<<pl.nall[0], SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.all[0], pl.flag[0], opt.mode == MG_ADJOINT); ++*pl.nl;
+	k_setup0<<<(pl.nall[0] + TPB - 1) / TPB, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.all[0], pl.nall[0], pl.flag[0]);
+	++*pl.nl;
 	for (int l = 1; l < pl.nlev_max; l++) {
 		k_mask_down<<<pl.nall[l], SP_THREADS, 0, s>>>(pl.dp, pl.all[l], l, pl.flag[l]); ++*pl.nl;
 	}
@@ -2622,7 +2749,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 		k_adjoint_scatter<<<pl.nall[0], SP_THREADS, 0, s>>>(pl.dp, pl.all[0], pl.gout, pl.gin, pl.gdat); ++*pl.nl;
 	}
 	else {
-		k_finalize<<<pl.nall[0], SP_THREADS, 0, s>>>(pl.dp, pl.all[0]); ++*pl.nl;
+		k_finalize<<<(pl.nall[0] + TPB - 1) / TPB, SP_THREADS, 0, s>>>(pl.dp, pl.all[0], pl.nall[0]); ++*pl.nl;
 	}
 	SP_LAUNCH_CHECK(ctx);
 	ProbState *hs = (ProbState *)stage;
