@@ -490,7 +490,7 @@ __global__ void k_resid64(const ProbDev *__restrict__ P, ProbState *st, const in
 	const ProbDev &pr = P[prob];
 	const LevelDev &L = pr.lv[0];
 	const int i = tile_i(t), w = pr.w, h = pr.h;
-	double rr = 0;
+	FF rr = {0.f, 0.f};   // |r|^2 from the float r (FP64 issues at 1/70 rate)
 	// U is 0 at every unknown until the first refinement step adds to it, so
 	// there b = rhs - A_UK g_K is exactly this residual: ||b|| = ||r||.
 #pragma unroll
@@ -508,24 +508,25 @@ __global__ void k_resid64(const ProbDev *__restrict__ P, ProbState *st, const in
 			const double us = known_at(pr.U, L.mask, pr.g, pr.known_zero, (size_t)js * w + i);
 			const double uw = known_at(pr.U, L.mask, pr.g, pr.known_zero, (size_t)j * w + iw);
 			const double un = known_at(pr.U, L.mask, pr.g, pr.known_zero, (size_t)jn * w + i);
-			const double s = pr.rhs ? (double)pr.rhs_sign * (double)pr.rhs[k] : 0.0;
-			rk = s - (4.0 * uc - ue - us - uw - un);
+			const double s = pr.rhs ? (double)(pr.rhs_sign * pr.rhs[k]) : 0.0;   // exact sign flip
+			rk = s - (fma(4.0, uc, -ue) - us - uw - un);
 		} else if (m) {
-			const double s = pr.rhs ? (double)pr.rhs_sign * (double)pr.rhs[k] : 0.0;
+			const double s = pr.rhs ? (double)(pr.rhs_sign * pr.rhs[k]) : 0.0;
 			rk = s - apply64<K>(pr.U, L.mask, pr.g, pr.known_zero, w, h, i, j);
 		}
 		if (m) {
+			const float rf = (float)rk;
 			if (pr.r64) {
 				pr.r64[k] = rk;     // the FP64 PCG starts from this residual
 			} else {
-				L.b[k] = (float)rk;
+				L.b[k] = rf;
 				pr.x[k] = 0.f;
 			}
-			rr += rk * rk;
+			ff_add_prod(rr, rf, rf);
 		}
 	}
 	double tot[2];
-	if (problem_sum1(rr, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
+	if (problem_sum1_ff(rr, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
 		ProbState &s = st[prob];
 		if (first) s.bnorm2 = tot[0];
 		if (first && s.nknown == 0) s.status = SIMPOIS_SINGULAR;
