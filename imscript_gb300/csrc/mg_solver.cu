@@ -78,6 +78,9 @@ struct ProbDev {
 	double *U;           // FP64 solution at the unknown pixels (the known ones
 	                     // are read from g: see known_at)
 	float *x, *p, *q;    // level-0 PCG vectors
+	float *xlo;          // x is carried as x + xlo (float-float): an FP32 x
+	                     // alone cannot hold a solution much larger than the
+	                     // right-hand side to the accuracy the residual needs
 	float *p2;           // fused path: second search-direction buffer
 	float *b_alt;        // fused path: the other level-0 residual buffer (k_pre5
 	                     // writes the updated r there, then swaps it with lv[0].b)
@@ -366,8 +369,52 @@ __device__ __forceinline__ uint8_t cell_code(const uint8_t *m, int i, int j, int
 	return (uint8_t)(code | (nd << 5));
 }
 
+// Cell codes of the 4 cells (fi..fi+3, fj) of a level whose width is a
+// multiple of 4: 3 word loads and 2 byte loads for 4 codes.
+__device__ __forceinline__ void codes4(const LevelDev &F, int fi, int fj)
+{
+	const size_t k = (size_t)fj * F.w + fi;
+	const uint32_t mc = *(const uint32_t *)(F.mask + k);
+	const uint32_t mn = fj > 0 ? *(const uint32_t *)(F.mask + k - F.w) : 0u;
+	const uint32_t ms = fj + 1 < F.h ? *(const uint32_t *)(F.mask + k + F.w) : 0u;
+	const uint32_t ml = fi > 0 ? F.mask[k - 1] : 0u, mr = fi + 4 < F.w ? F.mask[k + 4] : 0u;
+	uint32_t out = 0;
+#pragma unroll
+	for (int e = 0; e < 4; e++) {
+		if (!((mc >> (8 * e)) & 1u)) continue;
+		uint32_t code = 1, nd = 0;
+		if (e < 3) { if ((mc >> (8 * e + 8)) & 1u) code |= 2; }
+		else if (fi + 4 < F.w) { if (mr) code |= 2; }
+		else nd++;
+		if (e > 0) { if ((mc >> (8 * e - 8)) & 1u) code |= 4; }
+		else if (fi > 0) { if (ml) code |= 4; }
+		else nd++;
+		if (fj + 1 < F.h) { if ((ms >> (8 * e)) & 1u) code |= 8; } else nd++;
+		if (fj > 0) { if ((mn >> (8 * e)) & 1u) code |= 16; } else nd++;
+		out |= (code | (nd << 5)) << (8 * e);
+	}
+	*(uint32_t *)(F.code + k) = out;
+}
+
+// The PCG operator A p at a cell in difference form: p_c per known in-image
+// neighbour plus (p_c - p_n) per unknown in-image neighbour, in the order E,
+// W, S, N.  Mathematically diag * p_c + off; the differences of neighbouring
+// values are exact, so there is no cancellation of 4 p_c against its
+// neighbours where p is much larger than A p (smooth iterates of large holes),
+// which keeps the FP32 recurrence's residual close to the true one.
+__device__ __forceinline__ float a5_diff(float pc, float pe, float pw, float ps, float pn, int code)
+{
+	const int nunk = ((code >> 1) & 1) + ((code >> 2) & 1) + ((code >> 3) & 1) + ((code >> 4) & 1);
+	float q = __fmul_rn((float)(4 - (code >> 5) - nunk), pc);
+	if (code & 2) q = __fadd_rn(q, __fsub_rn(pc, pe));
+	if (code & 4) q = __fadd_rn(q, __fsub_rn(pc, pw));
+	if (code & 8) q = __fadd_rn(q, __fsub_rn(pc, ps));
+	if (code & 16) q = __fadd_rn(q, __fsub_rn(pc, pn));
+	return q;
+}
+
 // Level l >= 1 over all tiles: unknown iff every existing child is unknown;
-// also the cell codes of level l-1.
+// also the cell codes of level l-1 (when l-1 >= 1).
 __global__ void k_mask_down(const ProbDev *__restrict__ P, const int4 *__restrict__ all, int l, int *__restrict__ flag)
 {
 	__shared__ int any;
@@ -394,38 +441,42 @@ __global__ void k_mask_down(const ProbDev *__restrict__ P, const int4 *__restric
 	if (__any_sync(0xffffffffu, mine) && (threadIdx.x & 31) == 0) atomicOr(&any, 1);
 	__syncthreads();
 	if (threadIdx.x == 0) flag[blockIdx.x] = any;
-	// the mask of level l-1 is complete: its cell codes under this tile
+	// the mask of level l-1 >= 1 is complete: its cell codes under this tile
+	// (level 0 has its own pass, k_codes0)
+	if (l - 1 < 1) return;
 	if ((F.w & 3) == 0) {
-		// 4 cells of a row per step: 3 word loads and 2 byte loads for 4 codes
 		for (int q = threadIdx.x; q < SP_TILE * SP_TILE; q += SP_THREADS) {
 			const int fi = 2 * SP_TILE * t.y + 4 * (q & (SP_TILE / 2 - 1)), fj = 2 * SP_TILE * t.z + q / (SP_TILE / 2);
-			if (fi >= F.w || fj >= F.h) continue;
-			const size_t k = (size_t)fj * F.w + fi;
-			const uint32_t mc = *(const uint32_t *)(F.mask + k);
-			const uint32_t mn = fj > 0 ? *(const uint32_t *)(F.mask + k - F.w) : 0u;
-			const uint32_t ms = fj + 1 < F.h ? *(const uint32_t *)(F.mask + k + F.w) : 0u;
-			const uint32_t ml = fi > 0 ? F.mask[k - 1] : 0u, mr = fi + 4 < F.w ? F.mask[k + 4] : 0u;
-			uint32_t out = 0;
-#pragma unroll
-			for (int e = 0; e < 4; e++) {
-				if (!((mc >> (8 * e)) & 1u)) continue;
-				uint32_t code = 1, nd = 0;
-				if (e < 3) { if ((mc >> (8 * e + 8)) & 1u) code |= 2; }
-				else if (fi + 4 < F.w) { if (mr) code |= 2; }
-				else nd++;
-				if (e > 0) { if ((mc >> (8 * e - 8)) & 1u) code |= 4; }
-				else if (fi > 0) { if (ml) code |= 4; }
-				else nd++;
-				if (fj + 1 < F.h) { if ((ms >> (8 * e)) & 1u) code |= 8; } else nd++;
-				if (fj > 0) { if ((mn >> (8 * e)) & 1u) code |= 16; } else nd++;
-				out |= (code | (nd << 5)) << (8 * e);
-			}
-			*(uint32_t *)(F.code + k) = out;
+			if (fi < F.w && fj < F.h) codes4(F, fi, fj);
 		}
 	} else {
 		for (int q = threadIdx.x; q < 4 * SP_TILE * SP_TILE; q += SP_THREADS) {
 			const int fi = 2 * SP_TILE * t.y + (q & (2 * SP_TILE - 1)), fj = 2 * SP_TILE * t.z + q / (2 * SP_TILE);
 			if (fi < F.w && fj < F.h) F.code[(size_t)fj * F.w + fi] = cell_code(F.mask, fi, fj, F.w, F.h);
+		}
+	}
+}
+
+// Cell codes of level 0 over all tiles (TPB per block), once its mask is
+// complete: every problem has them, even one of a single level.
+__global__ void __launch_bounds__(SP_THREADS) k_codes0(const ProbDev *__restrict__ P, const int4 *__restrict__ all,
+		int nall)
+{
+#pragma unroll
+	for (int q = 0; q < TPB; q++) {
+		const int b = blockIdx.x * TPB + q;
+		if (b >= nall) return;
+		const int4 t = all[b];
+		const LevelDev &F = P[t.x].lv[0];
+		if ((F.w & 3) == 0) {
+			const int fi = t.y * SP_TILE + 4 * (threadIdx.x & 7), fj = t.z * SP_TILE + (threadIdx.x >> 3);
+			if (fi < F.w && fj < F.h) codes4(F, fi, fj);
+		} else {
+			const int fi = t.y * SP_TILE + (threadIdx.x & 31);
+			for (int r = 0; r < SP_ROWS; r++) {
+				const int fj = t.z * SP_TILE + (threadIdx.x >> 5) + SP_BLOCK_Y * r;
+				if (fi < F.w && fj < F.h) F.code[(size_t)fj * F.w + fi] = cell_code(F.mask, fi, fj, F.w, F.h);
+			}
 		}
 	}
 }
@@ -521,6 +572,7 @@ __global__ void k_resid64(const ProbDev *__restrict__ P, ProbState *st, const in
 			} else {
 				L.b[k] = rf;
 				pr.x[k] = 0.f;
+				pr.xlo[k] = 0.f;
 			}
 			ff_add_prod(rr, rf, rf);
 		}
@@ -607,7 +659,7 @@ __global__ void k_uadd(const ProbDev *__restrict__ P, const ProbState *__restric
 		int j = tile_j(t, r);
 		if (i < pr.w && j < pr.h) {
 			size_t k = (size_t)j * pr.w + i;
-			if (pr.lv[0].mask[k]) pr.U[k] += (double)pr.x[k];
+			if (pr.lv[0].mask[k]) pr.U[k] += (double)pr.x[k] + (double)pr.xlo[k];
 		}
 	}
 }
@@ -650,10 +702,17 @@ __global__ void k_spmv(const ProbDev *__restrict__ P, ProbState *st, const int4 
 		if (i < pr.w && j < pr.h) {
 			size_t k = (size_t)j * pr.w + i;
 			if (L.mask[k]) {
-				float d, o;
-				split<K>(L, pr.p, i, j, d, o);
-				float pk = pr.p[k];
-				float qk = d * pk + o;
+				float pk = pr.p[k], qk;
+				if (K == 0) {
+					const int code = L.code[k];
+					const float *p = pr.p;
+					qk = a5_diff(pk, (code & 2) ? p[k + 1] : 0.f, (code & 4) ? p[k - 1] : 0.f,
+							(code & 8) ? p[k + pr.w] : 0.f, (code & 16) ? p[k - pr.w] : 0.f, code);
+				} else {
+					float d, o;
+					split<K>(L, pr.p, i, j, d, o);
+					qk = d * pk + o;
+				}
 				pr.q[k] = qk;
 				ff_add_prod(pq, pk, qk);
 			}
@@ -691,7 +750,7 @@ __global__ void __launch_bounds__(SP_THREADS) k_xr(const ProbDev *__restrict__ P
 	FF rr = {0.f, 0.f};
 	// all loads of the four rows first (they depend only on coordinates)
 	uint8_t m[SP_ROWS];
-	float xv[SP_ROWS], pk[SP_ROWS], bk[SP_ROWS], qk[SP_ROWS];
+	float xv[SP_ROWS], xl[SP_ROWS], pk[SP_ROWS], bk[SP_ROWS], qk[SP_ROWS];
 	int kk[SP_ROWS];
 #pragma unroll
 	for (int r = 0; r < SP_ROWS; r++) {
@@ -700,6 +759,7 @@ __global__ void __launch_bounds__(SP_THREADS) k_xr(const ProbDev *__restrict__ P
 		kk[r] = in ? j * pr.w + i : 0;
 		m[r] = in ? L.mask[kk[r]] : 0;
 		xv[r] = in ? pr.x[kk[r]] : 0.f;
+		xl[r] = in ? pr.xlo[kk[r]] : 0.f;
 		pk[r] = in ? pv[kk[r]] : 0.f;
 		bk[r] = in ? L.b[kk[r]] : 0.f;
 		qk[r] = in ? pr.q[kk[r]] : 0.f;
@@ -707,7 +767,10 @@ __global__ void __launch_bounds__(SP_THREADS) k_xr(const ProbDev *__restrict__ P
 #pragma unroll
 	for (int r = 0; r < SP_ROWS; r++) {
 		if (m[r]) {
-			pr.x[kk[r]] = __fmaf_rn(a, pk[r], xv[r]);
+			FF xn = {xv[r], xl[r]};
+			ff_add_prod(xn, a, pk[r]);
+			pr.x[kk[r]] = xn.hi;
+			pr.xlo[kk[r]] = xn.lo;
 			const float rk = __fmaf_rn(-a, qk[r], bk[r]);
 			L.b[kk[r]] = rk;
 			ff_add_prod(rr, rk, rk);
@@ -1143,7 +1206,7 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 	if (upd) {
 		const float *pv = use_p2 ? pr.p2 : pr.p;
 		const int i = tile_i(t);
-		float xv[SP_ROWS], pk[SP_ROWS];
+		float xv[SP_ROWS], xl[SP_ROWS], pk[SP_ROWS];
 		uint8_t mk[SP_ROWS];
 		int kk[SP_ROWS];
 #pragma unroll
@@ -1153,13 +1216,17 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 			kk[r] = in ? j * L.w + i : 0;
 			mk[r] = in ? L.mask[kk[r]] : 0;
 			xv[r] = in ? pr.x[kk[r]] : 0.f;
+			xl[r] = in ? pr.xlo[kk[r]] : 0.f;
 			pk[r] = in ? pv[kk[r]] : 0.f;
 		}
 		__syncthreads();   // sb holds the new r
 #pragma unroll
 		for (int r = 0; r < SP_ROWS; r++) {
 			if (mk[r]) {
-				pr.x[kk[r]] = __fmaf_rn(a, pk[r], xv[r]);
+				FF xn = {xv[r], xl[r]};
+				ff_add_prod(xn, a, pk[r]);
+				pr.x[kk[r]] = xn.hi;
+				pr.xlo[kk[r]] = xn.lo;
 				const float rk = sb[(tile_j(t, r) - y0) * FR + (i - x0)];
 				pr.b_alt[kk[r]] = rk;
 				ff_add_prod(rr, rk, rk);
@@ -1492,7 +1559,10 @@ __global__ void __launch_bounds__(1024, 1) k_coarse5(const ProbDev *__restrict__
 		if (l == c0) {
 			float bv = mv ? gb[c] : 0.f;
 			if (upd && mv) {
-				pr.x[c] = __fmaf_rn(a, pv[c], pr.x[c]);
+				FF xn = {pr.x[c], pr.xlo[c]};
+				ff_add_prod(xn, a, pv[c]);
+				pr.x[c] = xn.hi;
+				pr.xlo[c] = xn.lo;
 				bv = __fmaf_rn(-a, pr.q[c], bv);
 				pr.lv[0].b[c] = bv;
 				ff_add_prod(rr, bv, bv);
@@ -1652,7 +1722,10 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_spmv5(const ProbDev *__restri
 			const int code = sc[c + e];
 			pk[e] = sp[c + e];
 			qk[e] = 0.f;
-			if (code & 1) qk[e] = diag_code(code) * pk[e] + off_code(sp, c + e, RW, code);
+			if (code & 1) {
+				const int ce = c + e;
+				qk[e] = a5_diff(pk[e], sp[ce + 1], sp[ce - 1], sp[ce + RW], sp[ce - RW], code);
+			}
 			spq[ty * SP_TILE + tx + e] = make_float2(pk[e], qk[e]);
 		}
 		if (gi < L.w && gj < L.h) {
@@ -1673,21 +1746,22 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_spmv5(const ProbDev *__restri
 				const int ry = c / R, rx = c - ry * R, gi = x0 + rx, gj = y0 + ry;
 				const bool in = gi >= 0 && gi < L.w && gj >= 0 && gj < L.h;
 				const size_t k = in ? (size_t)gj * L.w + gi : 0;
-				const uint8_t m = in ? L.mask[k] : 0;
+				const uint8_t m = in ? L.code[k] : 0;
 				const float zv = in ? L.z2[k] : 0.f;
 				const float po = (in && beta != 0.f) ? pold[k] : 0.f;
 				sm[c] = m;
-				sp[c] = m ? (beta != 0.f ? zv + beta * po : zv) : 0.f;
+				sp[c] = (m & 1) ? (beta != 0.f ? zv + beta * po : zv) : 0.f;
 			}
 		}
 		__syncthreads();
 		for (int c = threadIdx.x; c < SP_TILE * SP_TILE; c += SP_THREADS) {
 			const int ty = c >> 5, tx = c & 31, gi = x0 + 1 + tx, gj = y0 + 1 + ty;
 			const int rc = (ty + 1) * R + tx + 1;
-			if (gi < L.w && gj < L.h && sm[rc]) {
+			if (gi < L.w && gj < L.h && (sm[rc] & 1)) {
 				const size_t k = (size_t)gj * L.w + gi;
 				const float pk = sp[rc];
-				const float qk = az5_cell(sp, sm, rc, R, gi, gj, L.w, L.h);
+				const int code = sm[rc];
+				const float qk = a5_diff(pk, sp[rc + 1], sp[rc - 1], sp[rc + R], sp[rc - R], code);
 				pnew[k] = pk;
 				pr.q[k] = qk;
 				ff_add_prod(pq, pk, qk);
@@ -2527,7 +2601,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	int kinds = 0;
 	Layout Lo;
 	std::vector<size_t> off_mask[MAXLEV], off_code[MAXLEV], off_b[MAXLEV], off_z[MAXLEV], off_z2[MAXLEV];
-	std::vector<size_t> off_U(n), off_x(n), off_p(n), off_q(n), off_p2(n), off_balt(n);
+	std::vector<size_t> off_U(n), off_x(n), off_xlo(n), off_p(n), off_q(n), off_p2(n), off_balt(n);
 	std::vector<size_t> off_r64(n, 0), off_p64(n, 0), off_q64(n, 0);
 	std::vector<std::vector<int4>> lists(MAXLEV);
 	const int cmax = opt.coarse_max > 0 ? clamp_coarse_max(opt.coarse_max) : default_coarse_max();
@@ -2571,6 +2645,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 		size_t px = (size_t)q.w * q.h;
 		off_U[k] = Lo.take(px * 8);
 		off_x[k] = Lo.take(px * 4);
+		off_xlo[k] = Lo.take(px * 4);
 		off_p[k] = Lo.take(px * 4);
 		off_q[k] = Lo.take(px * 4);
 		off_p2[k] = Lo.take(px * 4);
@@ -2637,6 +2712,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 		}
 		d.U = (double *)(A + off_U[k]);
 		d.x = (float *)(A + off_x[k]);
+		d.xlo = (float *)(A + off_xlo[k]);
 		d.p = (float *)(A + off_p[k]);
 		d.q = (float *)(A + off_q[k]);
 		d.p2 = (float *)(A + off_p2[k]);
@@ -2711,6 +2787,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	// masks, tile flags, compacted lists
 	k_setup0<<<(pl.nall[0] + TPB - 1) / TPB, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.all[0], pl.nall[0], pl.flag[0]);
 	++*pl.nl;
+	k_codes0<<<(pl.nall[0] + TPB - 1) / TPB, SP_THREADS, 0, s>>>(pl.dp, pl.all[0], pl.nall[0]); ++*pl.nl;
 	for (int l = 1; l < pl.nlev_max; l++) {
 		k_mask_down<<<pl.nall[l], SP_THREADS, 0, s>>>(pl.dp, pl.all[l], l, pl.flag[l]); ++*pl.nl;
 	}
