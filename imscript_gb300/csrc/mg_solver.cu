@@ -2001,30 +2001,39 @@ __global__ void __launch_bounds__(SP_THREADS) k_finalize(const ProbDev *__restri
 // Adjoint scatter (5-point): grad_in = grad_out + sum of lambda over the
 // unknown 5-neighbours at the known pixels, 0 at the unknowns; grad_dat =
 // -lambda at the unknowns, 0 elsewhere.
-__global__ void k_adjoint_scatter(const ProbDev *__restrict__ P, const int4 *__restrict__ all,
+__global__ void k_adjoint_scatter(const ProbDev *__restrict__ P, const int4 *__restrict__ all, int nall,
 		const float *const *__restrict__ gout, float *const *__restrict__ gin, float *const *__restrict__ gdat)
 {
-	int4 t = all[blockIdx.x];
-	const ProbDev &pr = P[t.x];
-	const uint8_t *m = pr.lv[0].mask;
-	const int w = pr.w, h = pr.h;
-	int i = tile_i(t);
-	for (int r = 0; r < SP_ROWS; r++) {
-		int j = tile_j(t, r);
-		if (i < w && j < h) {
-			size_t k = (size_t)j * w + i;
+	for (int q = 0; q < TPB; q++) {   // TPB tiles per block
+		const int b = blockIdx.x * TPB + q;
+		if (b >= nall) return;
+		const int4 t = all[b];
+		const ProbDev &pr = P[t.x];
+		const uint8_t *m = pr.lv[0].mask;
+		const int w = pr.w, h = pr.h;
+		const int i = tile_i(t);
+		for (int r = 0; r < SP_ROWS; r++) {
+			const int j = tile_j(t, r);
+			if (i >= w || j >= h) continue;
+			const size_t k = (size_t)j * w + i;
 			if (m[k]) {
 				gin[t.x][k] = 0.f;
 				if (gdat[t.x]) gdat[t.x][k] = -(float)pr.U[k];
-			} else {
-				double s = gout[t.x][k];
-				if (i + 1 < w && m[k + 1]) s += pr.U[k + 1];
-				if (i > 0 && m[k - 1]) s += pr.U[k - 1];
-				if (j + 1 < h && m[k + w]) s += pr.U[k + w];
-				if (j > 0 && m[k - w]) s += pr.U[k - w];
-				gin[t.x][k] = (float)s;
-				if (gdat[t.x]) gdat[t.x][k] = 0.f;
+				continue;
 			}
+			const bool e = i + 1 < w && m[k + 1], wn = i > 0 && m[k - 1];
+			const bool sn = j + 1 < h && m[k + w], nn = j > 0 && m[k - w];
+			if (e || wn || sn || nn) {   // FP64 only next to an unknown
+				double s = gout[t.x][k];
+				if (e) s += pr.U[k + 1];
+				if (wn) s += pr.U[k - 1];
+				if (sn) s += pr.U[k + w];
+				if (nn) s += pr.U[k - w];
+				gin[t.x][k] = (float)s;
+			} else {
+				gin[t.x][k] = gout[t.x][k];   // (float)(double)v == v
+			}
+			if (gdat[t.x]) gdat[t.x][k] = 0.f;
 		}
 	}
 }
@@ -2824,7 +2833,8 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	if (pl.kt) kt_collect(ctx, kt);
 
 	if (opt.mode == MG_ADJOINT) {
-		k_adjoint_scatter<<<pl.nall[0], SP_THREADS, 0, s>>>(pl.dp, pl.all[0], pl.gout, pl.gin, pl.gdat); ++*pl.nl;
+		k_adjoint_scatter<<<(pl.nall[0] + TPB - 1) / TPB, SP_THREADS, 0, s>>>(pl.dp, pl.all[0], pl.nall[0], pl.gout,
+				pl.gin, pl.gdat); ++*pl.nl;
 	}
 	else {
 		k_finalize<<<(pl.nall[0] + TPB - 1) / TPB, SP_THREADS, 0, s>>>(pl.dp, pl.all[0], pl.nall[0]); ++*pl.nl;
