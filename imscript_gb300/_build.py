@@ -20,8 +20,9 @@ OUT = os.path.join(PKG, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 LIB = os.path.join(OUT, "libsimpois_gpu.so")
 CLI_BIN = os.path.join(OUT, "simpois")
+AMLE_BIN = os.path.join(OUT, "amle")
 
-CU_SOURCES = ["abi.cu", "ref_schedule.cu", "mg_solver.cu", "noalloc.cu"]
+CU_SOURCES = ["abi.cu", "ref_schedule.cu", "mg_solver.cu", "noalloc.cu", "amle.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr"]
 
@@ -74,20 +75,25 @@ def build_library(verbose=False, force=False) -> str:
     return LIB
 
 
+# the commands: each main source linked with the image I/O and the library
+COMMANDS = {"simpois": "simpois_main.c", "amle": "amle_main.c"}
+
+
 def build_cli(verbose=False, force=False) -> str:
-    srcs = [os.path.join(CLI, f) for f in sorted(os.listdir(CLI)) if f.endswith(".c")]
     hdrs = [os.path.join(CLI, f) for f in os.listdir(CLI) if f.endswith(".h")]
-    if not srcs:
-        return ""
-    if force or _stale(CLI_BIN, srcs + hdrs + [LIB, os.path.join(INCLUDE, "simpois_gpu.h")]):
-        cc = os.environ.get("CC", "gcc")
-        cmd = [cc, "-O2", "-std=gnu99", "-Wall", "-I", INCLUDE, *srcs, "-o", CLI_BIN,
-               "-L", OUT, "-lsimpois_gpu", "-Wl,-rpath,$ORIGIN", "-lm"]
-        if verbose:
-            print(" ".join(cmd))
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(f"cc failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    io = os.path.join(CLI, "imageio.c")
+    for name, main in COMMANDS.items():
+        srcs = [os.path.join(CLI, main), io]
+        binary = os.path.join(OUT, name)
+        if force or _stale(binary, srcs + hdrs + [LIB, os.path.join(INCLUDE, "simpois_gpu.h")]):
+            cc = os.environ.get("CC", "gcc")
+            cmd = [cc, "-O2", "-std=gnu99", "-Wall", "-I", INCLUDE, *srcs, "-o", binary,
+                   "-L", OUT, "-lsimpois_gpu", "-Wl,-rpath,$ORIGIN", "-lm"]
+            if verbose:
+                print(" ".join(cmd))
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"cc failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     return CLI_BIN
 
 

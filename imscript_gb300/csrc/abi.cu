@@ -374,6 +374,7 @@ int simpois_destroy(simpois_ctx *ctx)
 	if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
 	for (cudaEvent_t e : ctx->evpool) cudaEventDestroy(e);
 	if (ctx->solve_exec) cudaGraphExecDestroy(ctx->solve_exec);
+	if (ctx->amle_exec) cudaGraphExecDestroy(ctx->amle_exec);
 	delete ctx;
 	return SIMPOIS_OK;
 }
@@ -669,6 +670,82 @@ void poisson_recursive(float *u, float *g, float *f, int w, int h, float tstep, 
 	if (rc != SIMPOIS_OK) {
 		fprintf(stderr, "simpois: %s\n", simpois_strerror(rc));
 		if (u && g && u != g && w > 0 && h > 0) memcpy(u, g, sizeof(float) * (size_t)w * h);
+	}
+}
+
+int simpois_amle_device(simpois_ctx *ctx, float *out, const float *in, int w, int h, int pd, int nn, int niter,
+		const float *init, double *gap)
+{
+	if (!ctx || !out || !in) return ctx_fail(ctx, SIMPOIS_EINVAL, "null context or buffer");
+	int rc = check_dims(ctx, w, h, pd);
+	if (rc) return rc;
+	if (cudaSetDevice(ctx->device) != cudaSuccess) return ctx_fail(ctx, SIMPOIS_ECUDA, "cudaSetDevice");
+	rc = amle_run(ctx, out, in, w, h, pd, nn, niter, init, gap);
+	if (rc) return rc;
+	SP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+	return SIMPOIS_OK;
+}
+
+int simpois_amle(simpois_ctx *ctx, float *out, const float *in, int w, int h, int pd, int nn, int niter,
+		const float *init, double *gap)
+{
+	if (!ctx || !out || !in) return ctx_fail(ctx, SIMPOIS_EINVAL, "null context or buffer");
+	int rc = check_dims(ctx, w, h, pd);
+	if (rc) return rc;
+	if (cudaSetDevice(ctx->device) != cudaSuccess) return ctx_fail(ctx, SIMPOIS_ECUDA, "cudaSetDevice");
+	const size_t bytes = (size_t)w * h * pd * sizeof(float), slot = (bytes + 255) / 256 * 256;
+	rc = ctx_io_reserve(ctx, slot * (init ? 3 : 2));
+	if (rc) return rc;
+	float *din = (float *)ctx->io, *dout = (float *)(ctx->io + slot);
+	float *dini = init ? (float *)(ctx->io + 2 * slot) : nullptr;
+	cudaStream_t s = ctx->stream;
+	SP_CUDA(ctx, cudaMemcpyAsync(din, in, bytes, cudaMemcpyHostToDevice, s));
+	if (init) SP_CUDA(ctx, cudaMemcpyAsync(dini, init, bytes, cudaMemcpyHostToDevice, s));
+	rc = amle_run(ctx, dout, din, w, h, pd, nn, niter, dini, gap);
+	if (rc) return rc;
+	SP_CUDA(ctx, cudaMemcpyAsync(out, dout, bytes, cudaMemcpyDeviceToHost, s));
+	SP_CUDA(ctx, cudaStreamSynchronize(s));
+	return SIMPOIS_OK;
+}
+
+// A smart parameter as the reference reads it (smapa.h:19-41): a double
+// scanned from the variable once per process, else the default, with the
+// reference's message on stderr.
+static double smart_parameter(const char *name, double def, bool *known, double *value)
+{
+	if (!*known) {
+		fprintf(stderr, "scanning the environment for \"%s\"... ", name);
+		const char *v = getenv(name);
+		double y;
+		if (v && sscanf(v, "%lf", &y) == 1) {
+			fprintf(stderr, "got value %g\n", y);
+			*value = y;
+		} else {
+			fprintf(stderr, "kept default value %g\n", def);
+			*value = def;
+		}
+		*known = true;
+	}
+	return *value;
+}
+
+void amle(float *y, float *x, int w, int h)
+{
+	std::lock_guard<std::mutex> lock(g_dropin_mu);
+	int rc = SIMPOIS_OK;
+	if (!g_dropin_ctx) rc = simpois_create(&g_dropin_ctx, 0, nullptr);
+	if (rc == SIMPOIS_OK) {
+		if (getenv("AMLE_INIT"))
+			fprintf(stderr, "amle: AMLE_INIT is read by the amle command, not by this function\n");
+		static bool kn = false, ki = false;
+		static double vn = 4, vi = 100;
+		const int niter = (int)smart_parameter("AMLE_NITER", 100, &ki, &vi);
+		const int nn = niter > 0 ? (int)smart_parameter("AMLE_NN", 4, &kn, &vn) : 4;
+		rc = simpois_amle(g_dropin_ctx, y, x, w, h, 1, nn, niter, nullptr, nullptr);
+	}
+	if (rc != SIMPOIS_OK) {
+		fprintf(stderr, "amle: %s\n", simpois_strerror(rc));
+		if (y && x && y != x && w > 0 && h > 0) memcpy(y, x, sizeof(float) * (size_t)w * h);
 	}
 }
 

@@ -59,6 +59,10 @@ struct simpois_ctx {
 	// autotuner's choice per batch shape
 	int coarse_max_fixed = 0;
 	std::map<std::string, int> tuned;
+
+	// the AMLE sweeps of the last call and the call they were captured for
+	cudaGraphExec_t amle_exec = nullptr;
+	std::string amle_sig;
 };
 
 // Record a message on the context and return the status.

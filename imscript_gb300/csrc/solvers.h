@@ -52,6 +52,12 @@ int mg_handover_level(int w, int h, int coarse_max);
 // The hand-over size used when a solve names none (64, or SIMPOIS_COARSE_MAX).
 int mg_default_coarse_max();
 
+// AMLE fill of a planar w x h x pd image (device pointers), nn neighbours,
+// niter iterations, optional init planes; gap (may be null) receives per
+// channel the max and the mean of |tinf - tsup| over the unknowns.
+int amle_run(simpois_ctx *ctx, float *out, const float *in, int w, int h, int pd, int nn, int niter,
+		const float *init, double *gap);
+
 // FP64 relative residual of a float output for n problems (kind per problem).
 int mg_residual(simpois_ctx *ctx, const MgProblem *probs, const float *const *u, int n,
 		double *rel, double *bnorm);

@@ -68,6 +68,7 @@ EXPORTS = [
     "simpois_strerror", "simpois_last_error", "simpois_solve", "simpois_solve_device",
     "simpois_solve_batch", "simpois_residual_device", "simpois_residual_device_noalloc",
     "simpois_adjoint_device", "simpois_autotune", "simpois_set_coarse_max",
+    "simpois_amle_device", "simpois_amle", "amle",
     "simpois_launch_count", "simpois_reset_launch_count", "simpois_kernel_stats",
     "simpois_reset_kernel_stats",
     "poisson_solver_separable", "poisson_rec", "poisson_recursive",
@@ -117,6 +118,11 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
         L.simpois_adjoint_device.argtypes = [vp, vp, vp, ip, ip, ip, vp, vp, P, R]
         L.simpois_autotune.argtypes = [vp, ctypes.POINTER(Image), ip, P, R, ctypes.POINTER(ip)]
         L.simpois_set_coarse_max.argtypes = [vp, ip]
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.simpois_amle_device.argtypes = [vp, vp, vp, ip, ip, ip, ip, ip, vp, dp]
+        L.simpois_amle.argtypes = [vp, vp, vp, ip, ip, ip, ip, ip, vp, dp]
+        L.amle.argtypes = [vp, vp, ip, ip]
+        L.amle.restype = None
         L.simpois_launch_count.argtypes = [vp]
         L.simpois_launch_count.restype = ctypes.c_longlong
         L.simpois_reset_launch_count.argtypes = [vp]

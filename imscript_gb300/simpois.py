@@ -201,3 +201,40 @@ def adjoint(grad_out, g, *, rtol=1e-6, max_iter=0, flags=0, want_dat=True, allow
                                             ctypes.byref(prm), reps)
     ctx.check(rc, allow)
     return gi, gd, [r.as_dict() for r in reps]
+
+
+def amle(inp, nn=4, niter=100, init=None, *, out=None):
+    """AMLE fill of every channel (src/amle.c:196-246): ``nn`` neighbours
+    (AMLE_NN), ``niter`` iterations (AMLE_NITER), ``init`` the start of the
+    upper iterate at the unknowns (AMLE_INIT; same shape as ``inp``).  Returns
+    (out, gaps) with gaps[c] = (max, mean) of |lower - upper| over channel c's
+    unknowns after the last iteration.  numpy arrays or CUDA tensors."""
+    pd, h, w = _shape3(inp)
+    gaps = (ctypes.c_double * (2 * pd))()
+    if _is_torch(inp) and inp.is_cuda:
+        import torch
+        g = inp.contiguous()
+        if g.dtype != torch.float32:
+            raise TypeError("float32 input expected")
+        ini = None
+        if init is not None:
+            ini = init.contiguous()
+            if ini.shape != g.shape or ini.dtype != torch.float32 or ini.device != g.device:
+                raise ValueError("init must match inp (shape, float32, device)")
+        o = torch.empty_like(g) if out is None else out
+        ctx = context(g.device.index or 0, _torch_stream(g))
+        rc = _lib.load().simpois_amle_device(ctx.handle, o.data_ptr(), g.data_ptr(), w, h, pd, int(nn),
+                                             int(niter), None if ini is None else ini.data_ptr(), gaps)
+    else:
+        if _is_torch(inp):
+            inp = inp.numpy()
+        g = np.ascontiguousarray(inp, dtype=np.float32)
+        ini = None if init is None else np.ascontiguousarray(init, dtype=np.float32)
+        if ini is not None and ini.shape != g.shape:
+            raise ValueError("init shape mismatch")
+        o = np.empty_like(g) if out is None else out
+        ctx = context(0)
+        rc = _lib.load().simpois_amle(ctx.handle, o.ctypes.data, g.ctypes.data, w, h, pd, int(nn), int(niter),
+                                      None if ini is None else ini.ctypes.data, gaps)
+    ctx.check(rc)
+    return o, [(gaps[2 * c], gaps[2 * c + 1]) for c in range(pd)]

@@ -14,6 +14,8 @@
  *    (5-point -Laplacian for tstep > 0, 13-point bilaplacian for tstep < 0)
  *    is at most rtol, for every channel of every image independently.
  *
+ * It also offers imscript's AMLE interpolator (src/amle.c), simpois_amle*.
+ *
  * Images are planar: sample (channel l, row j, column i) of a w x h x pd
  * image is at x[w*h*l + w*j + i], the layout of iio's *_split functions
  * (iio.h:42-43).  NaN marks an unknown pixel; every other value is copied to
@@ -171,6 +173,26 @@ int simpois_adjoint_device(simpois_ctx *ctx, const float *grad_out,
 		float *grad_dat, const simpois_params *params,
 		simpois_report *reports);
 
+/* AMLE fill (absolutely minimizing Lipschitz extension), the work of
+ * imscript's amle (src/amle.c:196-246, replaces that function) on every
+ * channel of a planar w x h x pd image whose NaN pixels are unknown: nn
+ * neighbours of the reference's table (AMLE_NN: 4, 6, 8, 16, 24 or 32; 0..32),
+ * niter iterations (AMLE_NITER, the reference's default 100), init (may be
+ * NULL, planar like in) the start of the upper iterate at the unknowns (the
+ * AMLE_INIT image).  out receives the upper iterate, as the reference's.  The
+ * sweeps visit the colour classes (i + k j) mod m in turn instead of raster
+ * order: the output is bit for bit the colour-ordered restatement of the
+ * reference; with the default 4 neighbours both orders reach the same fixed
+ * point.  gap, if not NULL, receives 2 pd values: per channel the max and the
+ * mean of |lower - upper| over the unknowns after the last iteration (what
+ * the reference prints).  simpois_amle_device takes device pointers,
+ * simpois_amle host pointers. */
+int simpois_amle_device(simpois_ctx *ctx, float *out, const float *in,
+		int w, int h, int pd, int nn, int niter, const float *init,
+		double *gap);
+int simpois_amle(simpois_ctx *ctx, float *out, const float *in, int w, int h,
+		int pd, int nn, int niter, const float *init, double *gap);
+
 /* Autotuner (no counterpart in the reference, which has no launch-shape
  * knobs).  The converged 5-point V-cycle runs the levels wider than a
  * hand-over size in 32 x 32 tile kernels and the rest in one shared-memory
@@ -214,6 +236,12 @@ void poisson_solver_separable(float *out, float *in, float *dat, int w, int h,
 		int pd, float tstep, int niter, int scale, float cgrad);
 void poisson_rec(float *u, float *g, float *f, int w, int h, float tstep,
 		int niter, int scale, int cgit);
+
+/* Drop-in for imscript's amle(y, x, w, h) (src/amle.c:196): one channel on
+ * device 0 through the process-wide context, AMLE_NN and AMLE_NITER read from
+ * the environment as the reference reads them; AMLE_INIT, an image file, is
+ * read by the amle command only. */
+void amle(float *y, float *x, int w, int h);
 
 /* Drop-in for poisson_recursive of the ftr viewers (ftr/minisimpois.c:127-149,
  * called in place by ftr/vnav.c:855,893): one channel, the GS-only pyramid of

@@ -32,6 +32,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle_simpois.so")
 REF_BIN = os.path.join(HERE, "_ref", "simpois")
 MINI_BIN = os.path.join(HERE, "_ref", "minisimpois")
+AMLE_BIN = os.path.join(HERE, "_ref", "amle")
 
 ORDER = {"raster": 0, "colour": 1}
 
@@ -62,8 +63,9 @@ def build(reference: bool | None = None) -> None:
 def lib() -> ctypes.CDLL:
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB_PATH) or (
-            os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, "simpois_oracle.c"))
+        if not os.path.exists(LIB_PATH) or any(
+            os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, src))
+            for src in ("simpois_oracle.c", "amle_oracle.c")
         ):
             build(reference=False)
         L = ctypes.CDLL(LIB_PATH)
@@ -88,6 +90,12 @@ def lib() -> ctypes.CDLL:
         L.oracle_apply_mask.argtypes = [fp, fp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.oracle_poisson_recursive.argtypes = [fp, fp, fp, ctypes.c_int, ctypes.c_int, ctypes.c_float,
                                                ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.amle_oracle.argtypes = [fp, fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, fp,
+                                  ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+        L.amle_oracle.restype = ctypes.c_int
+        L.amle_oracle_colouring.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                            ctypes.POINTER(ctypes.c_int)]
+        L.amle_oracle_colouring.restype = None
         _lib = L
     return _lib
 
@@ -255,3 +263,61 @@ def run_reference(inp=None, dat=None, mask=None, args=(), env=None, timeout=600,
             if stdin is not None:
                 stdin.close()
         return from_hwc(np.load(out))
+
+
+# ------------------------------------------------------------------ AMLE (src/amle.c)
+
+def amle(inp, nn=4, niter=100, init=None, order="raster", gaps=False):
+    """AMLE fill of every channel of a planar (pd, h, w) float32 image (NaN =
+    unknown), as src/amle.c:196-246 does for one channel; init (same shape)
+    replaces the upper start at the unknowns.  order "raster" is the
+    reference's sweep (bit-exact), "colour" the GPU's.  With gaps, also the
+    per-channel (max, mean) of |tinf - tsup| over the unknowns."""
+    x = _planar(inp, "inp")
+    pd, h, w = x.shape
+    ini = None if init is None else _planar(init, "init")
+    out = np.empty_like(x)
+    g = np.zeros((pd, 2))
+    L = lib()
+    for c in range(pd):
+        y = np.empty((h, w), np.float32)
+        gp = (ctypes.c_double * 2)()
+        rc = L.amle_oracle(_fptr(y), _fptr(np.ascontiguousarray(x[c])), w, h, int(nn), int(niter),
+                           None if ini is None else _fptr(np.ascontiguousarray(ini[c])),
+                           0 if order == "raster" else 1, gp)
+        if rc:
+            raise MemoryError("amle oracle")
+        out[c] = y
+        g[c] = (gp[0], gp[1])
+    return (out, g) if gaps else out
+
+
+def amle_colouring(nn):
+    """(m, k): the colour classes (i + k j) mod m of the parallel AMLE sweep."""
+    m, k = ctypes.c_int(), ctypes.c_int()
+    lib().amle_oracle_colouring(int(nn), ctypes.byref(m), ctypes.byref(k))
+    return m.value, k.value
+
+
+def run_reference_amle(inp, mask=None, env=None, timeout=600):
+    """Run the reference amle binary (`amle in mask out`, src/amle.c:330-367)
+    on one channel (h, w); returns the (h, w) output."""
+    if not os.path.isfile(AMLE_BIN):
+        raise FileNotFoundError(AMLE_BIN)
+    with tempfile.TemporaryDirectory() as td:
+        p = os.path.join(td, "in.npy")
+        np.save(p, np.asarray(inp, np.float32))
+        pm = ""
+        if mask is not None:
+            pm = os.path.join(td, "m.npy")
+            np.save(pm, np.asarray(mask, np.float32))
+        out = os.path.join(td, "out.npy")
+        e = dict(os.environ)
+        for k in ("AMLE_NN", "AMLE_NITER", "AMLE_INIT", "AMLE_TAU"):
+            e.pop(k, None)
+        if env:
+            e.update({k: str(v) for k, v in env.items()})
+        subprocess.run([AMLE_BIN, p, pm, out], env=e, check=True, timeout=timeout,
+                       stderr=subprocess.DEVNULL)
+        y = np.load(out)
+        return y.reshape(y.shape[0], y.shape[1])

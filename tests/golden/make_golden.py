@@ -14,6 +14,11 @@ environment the reference ran with, and its planar output ``out``.
 * ``conv_*``  single-channel cases run to convergence with the reference
               recipe ``CG_EPS=rtol*||b|| simpois -s 1 -c -1`` (rtol 1e-7); the
               GPU solver must agree within 1e-4 relative max-abs.
+* ``amle_*``  the reference ``amle`` (src/amle.c) on one channel: neighbourhood
+              sizes (AMLE_NN), iteration counts (AMLE_NITER), a mask file, an
+              AMLE_INIT start image, all-known, all-NaN and 1-pixel images.
+
+``python tests/golden/make_golden.py amle`` regenerates only the AMLE group.
 """
 from __future__ import annotations
 
@@ -32,9 +37,11 @@ from imscript_gb300 import synth  # noqa: E402
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 
-def save(name, g, f=None, mask=None, args=(), env=None, out=None, extra=None):
+def save(name, g, f=None, mask=None, args=(), env=None, out=None, extra=None, init=None):
     d = {"g": g, "args": np.array(json.dumps(list(args))),
          "env": np.array(json.dumps(env or {})), "out": out}
+    if init is not None:
+        d["init"] = init
     if f is not None:
         d["f"] = f
     if mask is not None:
@@ -224,17 +231,62 @@ def mini_cases(rng):
     return k
 
 
+def amle_cases(rng):
+    """The reference amle command: `amle in.npy [mask.npy] out.npy` with its
+    environment (AMLE_NN, AMLE_NITER, AMLE_INIT)."""
+    import tempfile
+    k = 0
+    shapes = [(20, 30), (33, 17), (1, 9), (12, 1), (48, 40), (7, 7)]
+    for si, (h, w) in enumerate(shapes):
+        for nn, niter in [(4, 1), (4, 30), (6, 5), (8, 12), (16, 5), (32, 3)]:
+            x = (rng.standard_normal((h, w)) * 0.5).astype(np.float32)
+            x += synth.gaussian_field(rng, h, w, 3)
+            x[rng.random((h, w)) < 0.4] = np.nan
+            env = {"AMLE_NN": nn, "AMLE_NITER": niter}
+            mask = None
+            if k % 5 == 3:
+                mask = (rng.random((h, w)) < 0.2).astype(np.float32)
+            out = O.run_reference_amle(x, mask=mask, env=env)
+            save(f"amle_{k:03d}", x[None], mask=mask, env=env, out=out[None])
+            k += 1
+    # AMLE_INIT: a start image for the upper iterate at the unknowns
+    with tempfile.TemporaryDirectory() as td:
+        for (h, w) in [(16, 21), (30, 30)]:
+            x = synth.gaussian_field(rng, h, w, 3)
+            x[rng.random((h, w)) < 0.5] = np.nan
+            ini = (rng.standard_normal((h, w))).astype(np.float32)
+            pi = os.path.join(td, "init.npy")
+            np.save(pi, ini)
+            env = {"AMLE_NN": 8, "AMLE_NITER": 9, "AMLE_INIT": pi}
+            out = O.run_reference_amle(x, env=env)
+            env["AMLE_INIT"] = "init"
+            save(f"amle_{k:03d}", x[None], env=env, out=out[None], init=ini[None])
+            k += 1
+    # all known, all unknown, one unknown pixel
+    for x in [synth.gaussian_field(rng, 9, 11, 2), np.full((6, 5), np.nan, np.float32),
+              np.full((1, 1), np.nan, np.float32)]:
+        env = {"AMLE_NN": 4, "AMLE_NITER": 3}
+        out = O.run_reference_amle(x, env=env)
+        save(f"amle_{k:03d}", x[None].astype(np.float32), env=env, out=out[None])
+        k += 1
+    return k
+
+
 def main():
     if not O.have_reference():
         O.build(reference=True)
+    if sys.argv[1:] == ["amle"]:
+        print(f"wrote {amle_cases(np.random.default_rng(5150))} AMLE cases into {OUT}")
+        return
     rng = np.random.default_rng(20261203)
     n1 = pin_cases(rng)
     n2 = conv_cases(rng)
     n3 = cli_cases()
     n4 = io_cases()
     n5 = mini_cases(np.random.default_rng(4242))
-    print(f"wrote {n1} pin cases, {n2} converged cases, {n3} CLI cases, {n4} I/O cases and "
-          f"{n5} minisimpois cases into {OUT}")
+    n6 = amle_cases(np.random.default_rng(5150))
+    print(f"wrote {n1} pin cases, {n2} converged cases, {n3} CLI cases, {n4} I/O cases, "
+          f"{n5} minisimpois cases and {n6} AMLE cases into {OUT}")
 
 
 if __name__ == "__main__":

@@ -36,9 +36,32 @@ def load(path):
     d["extra"] = json.loads(str(d["extra"])) if "extra" in d else {}
     d["f"] = d.get("f")
     d["mask"] = d.get("mask")
+    d["init"] = d.get("init")
     d["name"] = os.path.splitext(os.path.basename(path))[0]
     return d
 
 
 def cases(prefix):
     return sorted(glob.glob(os.path.join(GOLDEN, prefix + "*.npz")))
+
+
+def amle_inputs(d):
+    """(x, nn, niter, init) of an amle_* fixture as the reference ran it:
+    mask > 0 becomes NaN (src/amle.c:357-360), AMLE_NN / AMLE_NITER truncated
+    to int, AMLE_INIT the stored start image."""
+    x = d["g"].copy()
+    if d["mask"] is not None:
+        x[:, d["mask"] > 0] = np.nan
+    nn = int(float(d["env"].get("AMLE_NN", 4)))
+    niter = int(float(d["env"].get("AMLE_NITER", 100)))
+    return x, nn, niter, d["init"]
+
+
+def same_bits_or_nan(a, b):
+    """Bit-equal where finite or infinite; NaN where the other is NaN (the
+    NaN of 0/0 has another sign bit on x86-64 than on aarch64 or the GPU)."""
+    a, b = np.asarray(a, np.float32), np.asarray(b, np.float32)
+    if a.shape != b.shape:
+        return False
+    na, nb = np.isnan(a), np.isnan(b)
+    return bool(np.array_equal(na, nb) and np.array_equal(a[~na].view(np.uint32), b[~nb].view(np.uint32)))

@@ -2,7 +2,7 @@
 import numpy as np
 import pytest
 
-from golden_cases import cases, load, parse_args
+from golden_cases import amle_inputs, cases, load, parse_args, same_bits_or_nan
 
 
 @pytest.mark.parametrize("path", cases("pin_"), ids=lambda p: p.rsplit("/", 1)[-1][:-4])
@@ -73,3 +73,39 @@ def test_oracle_reproduces_minisimpois_bit_exact(oracle_mod, path):
     d = load(path)
     out = oracle_mod.poisson_recursive(d["g"], d["f"], order="raster", **_mini_kw(d["args"]))
     assert np.array_equal(out.view(np.uint32), d["out"].view(np.uint32))
+
+
+@pytest.mark.parametrize("path", cases("amle_"), ids=lambda p: p.rsplit("/", 1)[-1][:-4])
+def test_amle_oracle_reproduces_reference_bit_exact(oracle_mod, path):
+    d = load(path)
+    x, nn, niter, init = amle_inputs(d)
+    out = oracle_mod.amle(x, nn=nn, niter=niter, init=init, order="raster")
+    assert same_bits_or_nan(out, d["out"])
+
+
+def test_amle_colourings_separate_every_neighbour(oracle_mod):
+    """No neighbour offset of the first nn falls in the pixel's own class, so
+    a class updates in parallel (the GPU sweep)."""
+    offsets = [(1, 0), (0, 1), (-1, 0), (0, -1), (1, 1), (-1, -1), (-1, 1), (1, -1),
+               (2, 1), (1, 2), (2, -1), (1, -2), (-2, -1), (-1, -2), (-2, 1), (-1, 2),
+               (3, 1), (1, 3), (3, -1), (1, -3), (-3, -1), (-1, -3), (-3, 1), (-1, 3),
+               (3, 2), (2, 3), (3, -2), (2, -3), (-3, -2), (-2, -3), (-3, 2), (-2, 3)]
+    for nn in range(1, 33):
+        m, k = oracle_mod.amle_colouring(nn)
+        assert all((a + k * b) % m != 0 for a, b in offsets[:nn]), nn
+    assert oracle_mod.amle_colouring(4) == (2, 1)
+
+
+def test_amle_colour_order_converges_with_raster(oracle_mod):
+    """With the 4-neighbourhood both sweep orders reach the same fixed point
+    (and tinf meets tsup).  With 8 or more neighbours the weighted min/max
+    iteration stalls with tinf and tsup apart (the reference's own gap stays
+    ~0.04 here), so the two orders stop at different points: only the
+    colour-ordered restatement is a bit-exact target for the GPU there."""
+    rng = np.random.default_rng(8)
+    from imscript_gb300 import synth
+    x = synth.gaussian_field(rng, 24, 30, 3)[None]
+    x[0, 6:18, 8:22] = np.nan
+    a, ga = oracle_mod.amle(x, nn=4, niter=400, order="raster", gaps=True)
+    b, gb = oracle_mod.amle(x, nn=4, niter=400, order="colour", gaps=True)
+    assert np.abs(a - b).max() < 1e-5 and ga[0, 0] < 1e-5 and gb[0, 0] < 1e-5
