@@ -16,6 +16,7 @@
 // the colour-ordered restatement of the reference.
 #include <math.h>
 #include <stdint.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <string>
@@ -28,6 +29,18 @@ namespace {
 // The neighbour table of get_nvals (src/amle.c:17-30): offsets and squared
 // lengths, the weights of the midpoint.
 constexpr int AMLE_MAXNN = 32;
+// Target halo of the fused sweeps (pixels): how many iterations one launch
+// takes.  The grouping changes no result bit; SIMPOIS_AMLE_HALO (1..32)
+// overrides the default 8.
+int amle_halo()
+{
+	static int v = [] {
+		const char *e = getenv("SIMPOIS_AMLE_HALO");
+		int x = e ? atoi(e) : 8;
+		return x < 1 ? 1 : (x > 32 ? 32 : x);
+	}();
+	return v;
+}
 __constant__ int8_t c_adi[AMLE_MAXNN] = {1, 0, -1, 0, 1, -1, -1, 1, 2, 1, 2, 1, -2, -1, -2, -1,
 	3, 1, 3, 1, -3, -1, -3, -1, 3, 2, 3, 2, -3, -2, -3, -2};
 __constant__ int8_t c_adj[AMLE_MAXNN] = {0, 1, 0, -1, 1, -1, 1, -1, 1, 2, -1, -2, -1, -2, 1, 2,
@@ -61,6 +74,7 @@ struct AmleArgs {
 	int w, h, pd, nn, m, k;
 	const float *in, *init;
 	float *out, *tinf, *tsup;
+	float *tinf2, *tsup2;   // the second buffers of the fused sweeps
 	uint8_t *unk;
 	unsigned int *mm;    // per channel: sortable keys of the minimum and the maximum
 	int *tflag;          // per channel and tile: the tile holds an unknown
@@ -131,8 +145,11 @@ __global__ void k_amle_init(AmleArgs a)
 		const float v = a.in[k];
 		const bool u = v != v;
 		a.unk[k] = u;
-		a.tinf[k] = u ? lo : v;
-		a.tsup[k] = u ? (a.init ? a.init[k] : hi) : v;
+		const float vi = u ? lo : v, vs = u ? (a.init ? a.init[k] : hi) : v;
+		a.tinf[k] = vi;
+		a.tsup[k] = vs;
+		a.tinf2[k] = vi;
+		a.tsup2[k] = vs;
 		mine |= u;
 	}
 	if (__any_sync(0xffffffffu, mine) && (threadIdx.x & 31) == 0) atomicOr(&any, 1);
@@ -140,49 +157,102 @@ __global__ void k_amle_init(AmleArgs a)
 	if (threadIdx.x == 0) a.tflag[(size_t)c * gridDim.x + t] = any;
 }
 
-// The reference's update of unknown (i, j) of x (amle_iteration's body):
-// the first nn in-image neighbours in table order, the first minimum and the
-// first maximum, (a v_min + b v_max) / (a + b) with a the weight of the
-// maximum and b that of the minimum.
-__device__ __forceinline__ float amle_new(const float *x, int w, int h, int i, int j, int nn)
+// Several half-sweeps of both iterates of one tile in shared memory
+// (temporal blocking): the tile and a halo of H = r x S pixels, r the reach
+// of the neighbourhood, are loaded once; half-sweep s (global number s0 + s)
+// updates the class ((s0 + s) mod m) cells at distance >= r (s + 1) from the
+// region's edge, whose
+// neighbours all still hold the values the sequential order gives them, so
+// after S half-sweeps the tile itself (distance >= H) is exact; it alone is
+// written back.  The same updates, in the same class order, as S / m calls of
+// one-class-per-launch sweep, with the iterates read and written once.  Tiles of a launch run concurrently and a tile's halo is other tiles'
+// pixels, so the iterates are double-buffered (src -> dst); both buffers hold
+// the same values outside the tiles with unknowns, which no launch touches.
+__global__ void __launch_bounds__(SP_THREADS) k_amle_fused(AmleArgs a, const float *__restrict__ sinf,
+		const float *__restrict__ ssup, float *__restrict__ dinf, float *__restrict__ dsup, int r, int s0, int S)
 {
-	float vmin = 0.f, vmax = 0.f, wmin = 0.f, wmax = 0.f;
-	int nv = 0;
-	for (int p = 0; p < nn; p++) {
-		const int ii = i + c_adi[p], jj = j + c_adj[p];
-		if (ii < 0 || jj < 0 || ii >= w || jj >= h) continue;
-		const float v = x[(size_t)jj * w + ii], wt = c_aw[p];
-		if (nv == 0) {
-			vmin = vmax = v;
-			wmin = wmax = wt;
-		} else {
-			if (v < vmin) { vmin = v; wmin = wt; }
-			if (v > vmax) { vmax = v; wmax = wt; }
-		}
-		nv++;
-	}
-	const float a = wmax, b = wmin;
-	return __fdiv_rn(__fadd_rn(__fmul_rn(a, vmin), __fmul_rn(b, vmax)), __fadd_rn(a, b));
-}
-
-// One colour class of both iterates of every channel, in place.
-__global__ void k_amle_sweep(AmleArgs a, int colour)
-{
+	extern __shared__ __align__(16) unsigned char smem[];
+	__shared__ int cnt[64];
 	const int c = blockIdx.y, t = blockIdx.x;
 	if (!a.tflag[(size_t)c * gridDim.x + t]) return;
 	const int tx = t % ntx(a.w), ty = t / ntx(a.w);
 	const size_t off = (size_t)a.w * a.h * c;
-	const int i = tx * SP_TILE + (threadIdx.x & 31);
-	for (int r = 0; r < SP_ROWS; r++) {
-		const int j = ty * SP_TILE + (threadIdx.x >> 5) + SP_BLOCK_Y * r;
-		if (i >= a.w || j >= a.h) continue;
-		const int col = (i + a.k * j) % a.m;
-		const size_t k = off + (size_t)j * a.w + i;
-		if (col != colour || !a.unk[k]) continue;
-		const float ni = amle_new(a.tinf + off, a.w, a.h, i, j, a.nn);
-		const float ns = amle_new(a.tsup + off, a.w, a.h, i, j, a.nn);
-		a.tinf[k] = ni;
-		a.tsup[k] = ns;
+	const int H = r * S, R = SP_TILE + 2 * H, N = R * R, m = a.m;
+	const int cap = R * ((R + m - 1) / m);   // cells of one colour in the region, at most
+	float *zi = (float *)smem, *zs = zi + N;
+	int *lists = (int *)(zs + N);            // per colour: unknown cells, packed (q | ring << 16)
+	const int x0 = tx * SP_TILE - H, y0 = ty * SP_TILE - H;
+	const bool interior = x0 >= 0 && y0 >= 0 && x0 + R <= a.w && y0 + R <= a.h;
+	for (int q = threadIdx.x; q < m; q += blockDim.x) cnt[q] = 0;
+	__syncthreads();
+	for (int q = threadIdx.x; q < N; q += blockDim.x) {
+		const int ry = q / R, rx = q - ry * R, gi = x0 + rx, gj = y0 + ry;
+		const bool in = gi >= 0 && gi < a.w && gj >= 0 && gj < a.h;
+		const size_t k = in ? off + (size_t)gj * a.w + gi : 0;
+		zi[q] = in ? sinf[k] : 0.f;
+		zs[q] = in ? ssup[k] : 0.f;
+		if (in && a.unk[k]) {
+			const int ring = min(min(rx, ry), min(R - 1 - rx, R - 1 - ry));
+			if (ring >= r) {   // cells nearer the edge are never updated
+				const int col = (gi + a.k * gj) % m;
+				const int e = atomicAdd(&cnt[col], 1);
+				lists[col * cap + e] = q | (ring << 16);
+			}
+		}
+	}
+	__syncthreads();
+	for (int s = 0; s < S; s++) {
+		const int colour = (s0 + s) % m, lo = r * (s + 1), n = cnt[colour];
+		const int *list = lists + colour * cap;
+		for (int e = threadIdx.x; e < n; e += blockDim.x) {
+			const int v = list[e];
+			if ((v >> 16) < lo) continue;
+			const int q = v & 0xffff;
+			// the reference's update (amle_iteration's body) of both iterates:
+			// the first nn in-image neighbours in table order, the first
+			// minimum and the first maximum, (a v_min + b v_max) / (a + b)
+			// with a the weight of the maximum and b that of the minimum
+			int gi = 0, gj = 0;
+			if (!interior) {
+				const int ry = q / R;
+				gi = x0 + q - ry * R;
+				gj = y0 + ry;
+			}
+			float mn0 = 0.f, mx0 = 0.f, mn1 = 0.f, mx1 = 0.f;
+			float wmn0 = 0.f, wmx0 = 0.f, wmn1 = 0.f, wmx1 = 0.f;
+			bool first = true;
+			for (int p = 0; p < a.nn; p++) {
+				if (!interior) {
+					const int ii = gi + c_adi[p], jj = gj + c_adj[p];
+					if (ii < 0 || jj < 0 || ii >= a.w || jj >= a.h) continue;
+				}
+				const int qq = q + c_adj[p] * R + c_adi[p];
+				const float v0 = zi[qq], v1 = zs[qq], wt = c_aw[p];
+				if (first) {
+					mn0 = mx0 = v0;
+					mn1 = mx1 = v1;
+					wmn0 = wmx0 = wmn1 = wmx1 = wt;
+					first = false;
+				} else {
+					if (v0 < mn0) { mn0 = v0; wmn0 = wt; }
+					if (v0 > mx0) { mx0 = v0; wmx0 = wt; }
+					if (v1 < mn1) { mn1 = v1; wmn1 = wt; }
+					if (v1 > mx1) { mx1 = v1; wmx1 = wt; }
+				}
+			}
+			zi[q] = __fdiv_rn(__fadd_rn(__fmul_rn(wmx0, mn0), __fmul_rn(wmn0, mx0)), __fadd_rn(wmx0, wmn0));
+			zs[q] = __fdiv_rn(__fadd_rn(__fmul_rn(wmx1, mn1), __fmul_rn(wmn1, mx1)), __fadd_rn(wmx1, wmn1));
+		}
+		__syncthreads();
+	}
+	for (int q = threadIdx.x; q < SP_TILE * SP_TILE; q += blockDim.x) {
+		const int i = tx * SP_TILE + (q & 31), j = ty * SP_TILE + (q >> 5);
+		if (i < a.w && j < a.h) {
+			const size_t k = off + (size_t)j * a.w + i;
+			const int rq = ((q >> 5) + H) * R + (q & 31) + H;
+			dinf[k] = zi[rq];
+			dsup[k] = zs[rq];
+		}
 	}
 }
 
@@ -223,6 +293,10 @@ __global__ void k_amle_finish(AmleArgs a)
 
 }  // namespace
 
+// dynamic shared memory of k_amle_fused for a region of side R, m colours:
+// the two iterates and the per-colour cell lists
+static int amle_smem(int R, int m) { return R * R * 8 + m * R * ((R + m - 1) / m) * 4; }
+
 int amle_run(simpois_ctx *ctx, float *out, const float *in, int w, int h, int pd, int nn, int niter,
 		const float *init, double *gap)
 {
@@ -234,6 +308,7 @@ int amle_run(simpois_ctx *ctx, float *out, const float *in, int w, int h, int pd
 	const int ntiles = ((w + SP_TILE - 1) / SP_TILE) * ((h + SP_TILE - 1) / SP_TILE);
 	Layout Lo;
 	const size_t o_tinf = Lo.take(n * 4), o_tsup = Lo.take(n * 4), o_unk = Lo.take(n);
+	const size_t o_tinf2 = Lo.take(n * 4), o_tsup2 = Lo.take(n * 4);
 	const size_t o_mm = Lo.take(sizeof(unsigned int) * 2 * pd), o_gmax = Lo.take(sizeof(unsigned int) * pd);
 	const size_t o_flag = Lo.take(sizeof(int) * (size_t)ntiles * pd);
 	const size_t o_part = Lo.take(sizeof(double) * (size_t)ntiles * pd);
@@ -252,6 +327,8 @@ int amle_run(simpois_ctx *ctx, float *out, const float *in, int w, int h, int pd
 	a.out = out;
 	a.tinf = (float *)(A + o_tinf);
 	a.tsup = (float *)(A + o_tsup);
+	a.tinf2 = (float *)(A + o_tinf2);
+	a.tsup2 = (float *)(A + o_tsup2);
 	a.unk = (uint8_t *)(A + o_unk);
 	a.mm = (unsigned int *)(A + o_mm);
 	a.gmax = (unsigned int *)(A + o_gmax);
@@ -271,12 +348,21 @@ int amle_run(simpois_ctx *ctx, float *out, const float *in, int w, int h, int pd
 	k_amle_init<<<gt, SP_THREADS, 0, s>>>(a);
 	ctx->launches += 2;
 	SP_LAUNCH_CHECK(ctx);
-	// the sweeps: one graph of niter x m launches, cached while the call's
-	// pointers and sizes are unchanged
-	if (niter > 0) {
+	// the sweeps: spl half-sweeps (colour classes, in order) per launch, a
+	// halo of about amle_halo() pixels; the launches of a call in one graph,
+	// cached while the call's pointers and sizes are unchanged
+	int reach = 0;
+	for (int p = 0; p < nn; p++) reach = std::max(reach, std::max(abs(h_adi[p]), abs(h_adj[p])));
+	const long long total = (long long)niter * a.m;   // half-sweeps of the call
+	const int spl = reach ? std::max(1, amle_halo() / reach) : (int)std::min<long long>(total, 1 << 20);
+	const int launches = total > 0 ? (int)((total + spl - 1) / spl) : 0;
+	if (total > 0) {
+		const int Rmax = SP_TILE + 2 * reach * spl;
+		const int smem_max = amle_smem(Rmax, a.m);
+		SP_CUDA(ctx, cudaFuncSetAttribute(k_amle_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max));
 		char buf[256];
-		snprintf(buf, sizeof buf, "%p/%p/%p/%p/%d/%d/%d/%d/%d", (void *)A, (const void *)in, (const void *)init,
-				(void *)out, w, h, pd, nn, niter);
+		snprintf(buf, sizeof buf, "%p/%p/%p/%p/%d/%d/%d/%d/%d/%d", (void *)A, (const void *)in,
+				(const void *)init, (void *)out, w, h, pd, nn, niter, spl);
 		if (!ctx->amle_exec || ctx->amle_sig != buf) {
 			if (ctx->amle_exec) {
 				cudaGraphExecDestroy(ctx->amle_exec);
@@ -284,8 +370,15 @@ int amle_run(simpois_ctx *ctx, float *out, const float *in, int w, int h, int pd
 			}
 			cudaStream_t cs = ctx->capture_stream;
 			SP_CUDA(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-			for (int it = 0; it < niter; it++)
-				for (int c = 0; c < a.m; c++) k_amle_sweep<<<gt, SP_THREADS, 0, cs>>>(a, c);
+			long long done = 0;
+			for (int L = 0; L < launches; L++) {
+				const int S = (int)std::min<long long>(spl, total - done), R = SP_TILE + 2 * reach * S;
+				const bool even = (L & 1) == 0;
+				k_amle_fused<<<gt, SP_THREADS, amle_smem(R, a.m), cs>>>(a, even ? a.tinf : a.tinf2,
+						even ? a.tsup : a.tsup2, even ? a.tinf2 : a.tinf, even ? a.tsup2 : a.tsup, reach,
+						(int)(done % a.m), S);
+				done += S;
+			}
 			cudaGraph_t g;
 			SP_CUDA(ctx, cudaStreamEndCapture(cs, &g));
 			cudaError_t e = cudaGraphInstantiate(&ctx->amle_exec, g, 0);
@@ -297,7 +390,11 @@ int amle_run(simpois_ctx *ctx, float *out, const float *in, int w, int h, int pd
 			ctx->amle_sig = buf;
 		}
 		SP_CUDA(ctx, cudaGraphLaunch(ctx->amle_exec, s));
-		ctx->launches += (long long)niter * a.m;
+		ctx->launches += launches;
+	}
+	if (launches & 1) {   // the result is in the second buffers
+		std::swap(a.tinf, a.tinf2);
+		std::swap(a.tsup, a.tsup2);
 	}
 	k_amle_finish<<<gt, SP_THREADS, 0, s>>>(a);
 	ctx->launches++;

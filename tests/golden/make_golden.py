@@ -272,11 +272,42 @@ def amle_cases(rng):
     return k
 
 
+def amle_cli_cases():
+    """The reference amle command's texts, usage error and exit codes, and
+    the bytes of a file it writes (tests/golden/amle_cli.json)."""
+    import subprocess
+    import tempfile
+    res = {}
+    for a in ["-h", "--help", "--version", "-?"]:
+        r = subprocess.run([O.AMLE_BIN, a], capture_output=True, text=True)
+        res[a] = {"stdout": r.stdout, "stderr": r.stderr, "rc": r.returncode}
+    r = subprocess.run([O.AMLE_BIN, "a", "b", "c", "d"], capture_output=True, text=True)
+    res["extra_args"] = {"stderr": r.stderr.replace(O.AMLE_BIN, "ARGV0"), "rc": r.returncode}
+    with tempfile.TemporaryDirectory() as td:
+        a, b = os.path.join(td, "a.npy"), os.path.join(td, "b.npy")
+        np.save(a, np.zeros((4, 5, 1), np.float32))
+        np.save(b, np.zeros((4, 6, 1), np.float32))
+        r = subprocess.run([O.AMLE_BIN, a, b, os.path.join(td, "o.npy")], capture_output=True, text=True)
+        res["mask_mismatch"] = {"rc": r.returncode, "tail": r.stderr.strip().split(": ", 1)[-1]}
+        # a one-iteration fill: raster and colour order agree on a 1-pixel hole
+        x = np.arange(20, dtype=np.float32).reshape(4, 5) / 7
+        x[2, 2] = np.nan
+        np.save(a, x)
+        o = os.path.join(td, "o.npy")
+        e = dict(os.environ, AMLE_NITER="1")
+        subprocess.run([O.AMLE_BIN, a, "", o], check=True, env=e, capture_output=True)
+        res["file"] = {"in": x.ravel().tolist(), "out_bytes": list(open(o, "rb").read())}
+    with open(os.path.join(OUT, "amle_cli.json"), "w") as fh:
+        json.dump(res, fh)
+    return len(res)
+
+
 def main():
     if not O.have_reference():
         O.build(reference=True)
     if sys.argv[1:] == ["amle"]:
-        print(f"wrote {amle_cases(np.random.default_rng(5150))} AMLE cases into {OUT}")
+        n = amle_cases(np.random.default_rng(5150))
+        print(f"wrote {n} AMLE cases and {amle_cli_cases()} AMLE command cases into {OUT}")
         return
     rng = np.random.default_rng(20261203)
     n1 = pin_cases(rng)
@@ -284,7 +315,7 @@ def main():
     n3 = cli_cases()
     n4 = io_cases()
     n5 = mini_cases(np.random.default_rng(4242))
-    n6 = amle_cases(np.random.default_rng(5150))
+    n6 = amle_cases(np.random.default_rng(5150)) + amle_cli_cases()
     print(f"wrote {n1} pin cases, {n2} converged cases, {n3} CLI cases, {n4} I/O cases, "
           f"{n5} minisimpois cases and {n6} AMLE cases into {OUT}")
 

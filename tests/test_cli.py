@@ -140,3 +140,46 @@ def test_cli_end_to_end_matches_oracle(cli, tmp_path, oracle_mod):
     assert np.all(rel < 2e-6)
     known = ~np.isnan(gm)
     assert np.array_equal(out[known].view(np.uint32), gm[known].view(np.uint32))
+
+
+# ------------------------------------------------------------------ the amle command
+
+@pytest.fixture(scope="module")
+def amle_cli():
+    from imscript_gb300 import _build
+    _build.build()
+    return _build.AMLE_BIN
+
+
+@pytest.mark.parametrize("arg", ["-h", "--help", "--version", "-?"])
+def test_amle_help_texts(amle_cli, arg):
+    want = _fixtures("amle_cli.json")[arg]
+    r = subprocess.run([amle_cli, arg], capture_output=True, text=True)
+    assert (r.stdout, r.stderr, r.returncode) == (want["stdout"], want["stderr"], want["rc"])
+
+
+def test_amle_extra_arguments_print_usage(amle_cli):
+    want = _fixtures("amle_cli.json")["extra_args"]
+    r = subprocess.run([amle_cli, "a", "b", "c", "d"], capture_output=True, text=True)
+    assert (r.stderr.replace(amle_cli, "ARGV0"), r.returncode) == (want["stderr"], want["rc"])
+
+
+def test_amle_mask_size_mismatch_fails(amle_cli, tmp_path):
+    want = _fixtures("amle_cli.json")["mask_mismatch"]
+    a, b = str(tmp_path / "a.npy"), str(tmp_path / "b.npy")
+    np.save(a, np.zeros((4, 5, 1), np.float32))
+    np.save(b, np.zeros((4, 6, 1), np.float32))
+    r = subprocess.run([amle_cli, a, b, str(tmp_path / "o.npy")], capture_output=True, text=True)
+    assert r.returncode == want["rc"] == 255
+    assert r.stderr.strip().endswith(want["tail"])
+
+
+@pytest.mark.gpu
+def test_amle_command_writes_the_reference_bytes(amle_cli, tmp_path):
+    want = _fixtures("amle_cli.json")["file"]
+    x = np.array(want["in"], np.float32).reshape(4, 5)
+    a, o = str(tmp_path / "a.npy"), str(tmp_path / "o.npy")
+    np.save(a, x)
+    env = dict(os.environ, AMLE_NITER="1")
+    subprocess.run([amle_cli, a, "", o], check=True, env=env, capture_output=True)
+    assert list(open(o, "rb").read()) == want["out_bytes"]
