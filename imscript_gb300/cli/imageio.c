@@ -232,8 +232,55 @@ static int read_asc(raw_image *x, const unsigned char *b, size_t n)
 	return 0;
 }
 
+/* iio's semantic names (iio.c:5604-5633): "zero:WxH[,pd]" and "one:WxH[,pd]"
+ * (byte samples), "constant:V:WxH" (one float channel); 1 when `name` is
+ * one (x filled, or a message on a malformed one), 0 otherwise. */
+static int semantic_name(const char *name, raw_image *x, int *rc)
+{
+	int s[2], pd = 1;
+	double value;
+	if (name == strstr(name, "zero:") || name == strstr(name, "one:")) {
+		const int one = name[0] == 'o';
+		const char *q = name + (one ? 4 : 5);
+		if (sscanf(q, "%dx%d,%d", s, s + 1, &pd) != 3 && sscanf(q, "%dx%d", s, s + 1) != 2) {
+			fprintf(stderr, "imageio: bad semantical name \"%s\"\n", name);
+			*rc = 1;
+			return 1;
+		}
+		value = one;
+		x->type = T_U8;
+	} else if (name == strstr(name, "constant:")) {
+		float v;
+		if (sscanf(name + 9, "%g:%dx%d", &v, s, s + 1) != 3) {
+			fprintf(stderr, "imageio: bad semantical name \"%s\"\n", name);
+			*rc = 1;
+			return 1;
+		}
+		value = v;
+		x->type = T_F32;
+	} else {
+		return 0;
+	}
+	if (s[0] <= 0 || s[1] <= 0 || pd <= 0) {
+		fprintf(stderr, "imageio: bad semantical name \"%s\"\n", name);
+		*rc = 1;
+		return 1;
+	}
+	x->w = s[0];
+	x->h = s[1];
+	x->pd = pd;
+	size_t n = (size_t)s[0] * s[1] * pd;
+	x->v = xcalloc(n, sizeof(double));
+	if (!x->v) { *rc = 1; return 1; }
+	for (size_t i = 0; i < n; i++) x->v[i] = value;
+	*rc = 0;
+	return 1;
+}
+
 static int read_raw(const char *name, raw_image *x)
 {
+	int rc;
+	if (semantic_name(name, x, &rc)) return rc;
 	FILE *f = strcmp(name, "-") ? fopen(name, "rb") : stdin;
 	if (!f) {
 		fprintf(stderr, "imageio: can not open file \"%s\" in mode \"r\"\n", name);

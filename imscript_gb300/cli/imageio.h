@@ -3,7 +3,8 @@
  * following iio's conventions (iio.h:33-43, iio.c:5164-5346, 6166-6300):
  *
  *  - images are returned "split": planar float, x[w*h*l + w*j + i];
- *  - "-" names stdin (reading) or stdout (writing);
+ *  - "-" names stdin (reading) or stdout (writing); iio's semantic names
+ *    "zero:WxH[,pd]", "one:WxH[,pd]" and "constant:V:WxH" read as images;
  *  - the input format is sniffed from the first bytes: NumPy .npy (1.0,
  *    every numeric dtype), PFM ("Pf"/"PF"), PNM ("P2","P3","P5","P6") and the
  *    ASC text format ("w h 1 pd" header, planar samples);

@@ -183,3 +183,26 @@ def test_amle_command_writes_the_reference_bytes(amle_cli, tmp_path):
     env = dict(os.environ, AMLE_NITER="1")
     subprocess.run([amle_cli, a, "", o], check=True, env=env, capture_output=True)
     assert list(open(o, "rb").read()) == want["out_bytes"]
+
+
+@pytest.mark.parametrize("name,shape,value", [("zero:6x4,3", (4, 6, 3), 0.0), ("one:3x2", (2, 3, 1), 1.0),
+                                              ("constant:1.5:7x5", (5, 7, 1), 1.5),
+                                              ("constant:-2e-3:2x9", (9, 2, 1), np.float32(-2e-3))])
+def test_semantic_image_names(harness, tmp_path, name, shape, value):
+    """iio's semantic names read as images (iio.c:5604-5633); where the
+    reference binary is built here, its reading of the same name agrees."""
+    dst = str(tmp_path / "o.npy")
+    subprocess.run([harness, "read", name, dst], check=True)
+    got = np.load(dst)
+    assert got.reshape(shape[0], shape[1], -1).shape == shape
+    assert np.all(got == np.float32(value))
+    from oracle import oracle as O
+    if O.have_reference():
+        ref = str(tmp_path / "r.npy")
+        subprocess.run([O.REF_BIN, "-i", name, "-n", "0", "-o", ref], check=True, capture_output=True)
+        assert open(ref, "rb").read() == open(dst, "rb").read()
+
+
+def test_bad_semantic_name_fails(harness, tmp_path):
+    r = subprocess.run([harness, "read", "zero:axb", str(tmp_path / "o.npy")], capture_output=True, text=True)
+    assert r.returncode != 0 and "bad semantical name" in r.stderr
