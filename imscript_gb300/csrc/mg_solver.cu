@@ -88,6 +88,9 @@ struct ProbDev {
 	double tau_min;            // FP32 inner solve: smallest relative decrease
 	double rtol;
 	LevelDev lv[MAXLEV];
+	// k_coarse5's shared-memory layout of levels nfine.. (byte offsets of b,
+	// z and the cell codes), planned on the host
+	int coff_b[MAXLEV], coff_z[MAXLEV], coff_m[MAXLEV];
 };
 
 struct ProbState {
@@ -1410,6 +1413,19 @@ __device__ __host__ inline CoarseLayout coarse_layout(const int *lw, const int *
 
 // One red-black half-sweep (colour) over a whole level held in shared memory;
 // the 1024 threads map to 32 x 32 (half-columns, rows) of the colour's cells.
+// The Gauss-Seidel update and A z of a cell from its cell code (the same
+// operations, in the same order, as gs5_cell and az5_cell).
+__device__ __forceinline__ void gs5_code(float *z, const float *b, int code, int c, int w)
+{
+	z[c] = gs_div(b[c] - off_code(z, c, w, code), diag_code(code));
+}
+
+__device__ __forceinline__ float az5_code(const float *z, int code, int c, int w)
+{
+	return diag_code(code) * z[c] + off_code(z, c, w, code);
+}
+
+// m holds cell codes (0 at known cells)
 __device__ __forceinline__ void smem_sweep5(float *z, const float *b, const uint8_t *m, int w, int h, int colour)
 {
 	const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
@@ -1418,7 +1434,7 @@ __device__ __forceinline__ void smem_sweep5(float *z, const float *b, const uint
 		for (int k = tx; k < hw; k += 32) {
 			const int i = 2 * k + ((colour ^ j) & 1);
 			const int c = j * w + i;
-			if (i < w && m[c]) gs5_cell(z, b, m, c, w, i, j, w, h);
+			if (i < w && m[c]) gs5_code(z, b, m[c], c, w);
 		}
 	__syncthreads();
 }
@@ -1433,13 +1449,13 @@ __device__ __forceinline__ void warp_sweep5(float *z, const float *b, const uint
 		for (int j = lane >> 3; j < h; j += 4) {
 			const int ic = i + ((colour ^ j) & 1);
 			const int c = j * w + ic;
-			if (ic < w && m[c]) gs5_cell(z, b, m, c, w, ic, j, w, h);
+			if (ic < w && m[c]) gs5_code(z, b, m[c], c, w);
 		}
 	} else {
 		for (int q = lane; q < hw * h; q += 32) {
 			const int j = q / hw, i = 2 * (q - j * hw) + ((colour ^ j) & 1);
 			const int c = j * w + i;
-			if (i < w && m[c]) gs5_cell(z, b, m, c, w, i, j, w, h);
+			if (i < w && m[c]) gs5_code(z, b, m[c], c, w);
 		}
 	}
 	__syncwarp();
@@ -1467,7 +1483,7 @@ __device__ void warp_vcycle5(float *const *Z, float *const *B, const uint8_t *co
 					const int fi = 2 * ci + aa, fj = 2 * cj + bb;
 					if (fi < lw[l] && fj < lh[l]) {
 						const int f = fj * lw[l] + fi;
-						acc += B[l][f] - az5_cell(Z[l], M[l], f, lw[l], fi, fj, lw[l], lh[l]);
+						acc += B[l][f] - az5_code(Z[l], M[l][f], f, lw[l]);
 					}
 				}
 			B[l + 1][c] = 1.f * acc;
@@ -1525,18 +1541,21 @@ __global__ void __launch_bounds__(1024, 1) k_coarse5(const ProbDev *__restrict__
 	const float *pv = use_p2 ? pr.p2 : pr.p;
 	FF rr = {0.f, 0.f};
 	if (threadIdx.x < L) {
-		s_w[threadIdx.x] = pr.lv[threadIdx.x].w;
-		s_h[threadIdx.x] = pr.lv[threadIdx.x].h;
-		s_gm[threadIdx.x] = pr.lv[threadIdx.x].mask;
+		const int l = threadIdx.x;
+		s_w[l] = pr.lv[l].w;
+		s_h[l] = pr.lv[l].h;
+		// cell codes (the coarsest level has none: its code is formed below)
+		s_gm[l] = l + 1 < L ? pr.lv[l].code : pr.lv[l].mask;
+		if (l >= c0) {
+			s_Z[l] = (float *)(smem + pr.coff_z[l]);
+			s_B[l] = (float *)(smem + pr.coff_b[l]);
+			s_M[l] = (uint8_t *)(smem + pr.coff_m[l]);
+		}
 	}
 	__syncthreads();
 	if (threadIdx.x == 0) {
-		const CoarseLayout cl = coarse_layout(s_w, s_h, c0, L);
 		int pre = 0;
 		for (int l = c0; l < L; l++) {
-			s_Z[l] = (float *)(smem + cl.off_z[l]);
-			s_B[l] = (float *)(smem + cl.off_b[l]);
-			s_M[l] = (uint8_t *)(smem + cl.off_m[l]);
 			s_pre[l] = pre;
 			pre += s_w[l] * s_h[l];
 		}
@@ -1544,8 +1563,8 @@ __global__ void __launch_bounds__(1024, 1) k_coarse5(const ProbDev *__restrict__
 		stopped = 0;
 	}
 	__syncthreads();
-	// every level's mask (and b of level c0) in one flat loop: the loads of
-	// successive iterations do not depend on each other
+	// every level's cell codes (and b of level c0) in one flat loop: the
+	// loads of successive iterations do not depend on each other
 	const int total = s_pre[L];
 	const float *gb = pr.lv[c0].b;
 #pragma unroll 4
@@ -1553,7 +1572,11 @@ __global__ void __launch_bounds__(1024, 1) k_coarse5(const ProbDev *__restrict__
 		int l = c0;
 		while (q >= s_pre[l + 1]) l++;
 		const int c = q - s_pre[l];
-		const uint8_t mv = s_gm[l][c];
+		uint8_t mv = s_gm[l][c];
+		if (l + 1 == L && mv) {   // the coarsest level: its code from its mask
+			const int w = s_w[l], h = s_h[l], j = c / w;
+			mv = cell_code(s_gm[l], c - j * w, j, w, h);
+		}
 		s_M[l][c] = mv;
 		s_Z[l][c] = 0.f;
 		if (l == c0) {
@@ -1612,7 +1635,7 @@ __global__ void __launch_bounds__(1024, 1) k_coarse5(const ProbDev *__restrict__
 						const int fi = 2 * ci + aa, fj = 2 * cj + bb;
 						if (fi < w && fj < h) {
 							const int f = fj * w + fi;
-							acc += b[f] - az5_cell(z, m, f, w, fi, fj, w, h);
+							acc += b[f] - az5_code(z, m[f], f, w);
 						}
 					}
 				bc[c] = 1.f * acc;
@@ -2650,7 +2673,15 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 		// fused path: the tile kernels cover the levels above the hand-over
 		d.nfine = handover_level(lw, lh, nl, cmax);
 		pl.nfine_max = std::max(pl.nfine_max, d.nfine);
-		pl.coarse_smem = std::max(pl.coarse_smem, coarse_layout(lw, lh, d.nfine, nl).bytes);
+		{
+			const CoarseLayout cl = coarse_layout(lw, lh, d.nfine, nl);
+			pl.coarse_smem = std::max(pl.coarse_smem, cl.bytes);
+			for (int l = d.nfine; l < nl; l++) {
+				d.coff_b[l] = cl.off_b[l];
+				d.coff_z[l] = cl.off_z[l];
+				d.coff_m[l] = cl.off_m[l];
+			}
+		}
 		size_t px = (size_t)q.w * q.h;
 		off_U[k] = Lo.take(px * 8);
 		off_x[k] = Lo.take(px * 4);
