@@ -305,3 +305,24 @@ def test_unaligned_caller_buffers(sp):
     b, rb = sp.solve_batch([gin], rtol=1e-6, outs=[out])
     assert ra[0]["iterations"] == rb[0]["iterations"]
     assert torch.equal(a[0].view(torch.int32), b[0].view(torch.int32))
+
+
+@pytest.mark.parametrize("h,w", [(1, 300), (300, 1), (2, 2), (3, 1000), (1000, 3), (65, 1)])
+def test_converged_thin_images(sp, h, w):
+    """Rows, columns and tiny images on the converged schedule: FP64
+    residual <= rtol, close to the FP64 direct solve, knowns bit-exact."""
+    from oracle import fp64
+    rng = np.random.default_rng(h * 7 + w)
+    g = (rng.standard_normal((1, h, w)) * 0.3 + 1).astype(np.float32)
+    m = rng.random((h, w)) < 0.5
+    m.flat[0] = False           # at least one known pixel
+    g[:, m] = np.nan
+    f = (rng.standard_normal((1, h, w)) * 0.01).astype(np.float32)
+    for kind, t in ((0, 0.25), (1, -0.08)):
+        out, reps = sp.solve(_cuda(g), _cuda(f) if kind == 0 else None, tstep=t, rtol=1e-6, max_iter=5000)
+        r = reps[0]
+        assert r["status"] == 0 and r["rel_residual"] <= 1e-6, (kind, r)
+        o = out.cpu().numpy()[0]
+        x = fp64.solve(g[0], f[0] if kind == 0 else None, kind)
+        assert np.abs(o[m] - x[m]).max() <= 1e-4 * max(1.0, np.abs(x[m]).max())
+        assert np.array_equal(_bits(o[~m]), _bits(g[0][~m]))
