@@ -168,9 +168,13 @@ __global__ void k_amle_init(AmleArgs a)
 // one-class-per-launch sweep, with the iterates read and written once.  Tiles of a launch run concurrently and a tile's halo is other tiles'
 // pixels, so the iterates are double-buffered (src -> dst); both buffers hold
 // the same values outside the tiles with unknowns, which no launch touches.
+// NN > 0: the neighbourhood size known at compile time (the loop over the
+// neighbours unrolls); NN == 0: a.nn at run time.
+template <int NN>
 __global__ void __launch_bounds__(SP_THREADS) k_amle_fused(AmleArgs a, const float *__restrict__ sinf,
 		const float *__restrict__ ssup, float *__restrict__ dinf, float *__restrict__ dsup, int r, int s0, int S)
 {
+	const int nn = NN > 0 ? NN : a.nn;
 	extern __shared__ __align__(16) unsigned char smem[];
 	__shared__ int cnt[64];
 	const int c = blockIdx.y, t = blockIdx.x;
@@ -221,7 +225,9 @@ __global__ void __launch_bounds__(SP_THREADS) k_amle_fused(AmleArgs a, const flo
 			float mn0 = 0.f, mx0 = 0.f, mn1 = 0.f, mx1 = 0.f;
 			float wmn0 = 0.f, wmx0 = 0.f, wmn1 = 0.f, wmx1 = 0.f;
 			bool first = true;
-			for (int p = 0; p < a.nn; p++) {
+#pragma unroll
+			for (int p = 0; p < (NN > 0 ? NN : AMLE_MAXNN); p++) {
+				if (NN == 0 && p >= nn) break;
 				if (!interior) {
 					const int ii = gi + c_adi[p], jj = gj + c_adj[p];
 					if (ii < 0 || jj < 0 || ii >= a.w || jj >= a.h) continue;
@@ -359,7 +365,8 @@ int amle_run(simpois_ctx *ctx, float *out, const float *in, int w, int h, int pd
 	if (total > 0) {
 		const int Rmax = SP_TILE + 2 * reach * spl;
 		const int smem_max = amle_smem(Rmax, a.m);
-		SP_CUDA(ctx, cudaFuncSetAttribute(k_amle_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max));
+		auto kern = nn == 4 ? k_amle_fused<4> : nn == 8 ? k_amle_fused<8> : k_amle_fused<0>;
+		SP_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max));
 		char buf[256];
 		snprintf(buf, sizeof buf, "%p/%p/%p/%p/%d/%d/%d/%d/%d/%d", (void *)A, (const void *)in,
 				(const void *)init, (void *)out, w, h, pd, nn, niter, spl);
@@ -374,7 +381,7 @@ int amle_run(simpois_ctx *ctx, float *out, const float *in, int w, int h, int pd
 			for (int L = 0; L < launches; L++) {
 				const int S = (int)std::min<long long>(spl, total - done), R = SP_TILE + 2 * reach * S;
 				const bool even = (L & 1) == 0;
-				k_amle_fused<<<gt, SP_THREADS, amle_smem(R, a.m), cs>>>(a, even ? a.tinf : a.tinf2,
+				kern<<<gt, SP_THREADS, amle_smem(R, a.m), cs>>>(a, even ? a.tinf : a.tinf2,
 						even ? a.tsup : a.tsup2, even ? a.tinf2 : a.tinf, even ? a.tsup2 : a.tsup, reach,
 						(int)(done % a.m), S);
 				done += S;
