@@ -228,6 +228,7 @@ int run_converged(simpois_ctx *ctx, const simpois_image *im, int n, const simpoi
 	opt.out_resid = (p->flags & SIMPOIS_FLAG_OUT_RESID) != 0;
 	opt.fused = !(p->flags & SIMPOIS_FLAG_UNFUSED);
 	opt.ktimer = (p->flags & SIMPOIS_FLAG_KTIMER) != 0;
+	opt.tma = (p->flags & SIMPOIS_FLAG_TMA) != 0;
 	int rc = SIMPOIS_OK;
 	// one batched solve per operator kind
 	for (int kind = 0; kind < 2; kind++) {

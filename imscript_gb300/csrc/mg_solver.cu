@@ -38,6 +38,8 @@
 #include <cmath>
 #include <cstring>
 
+#include <cudaTypedefs.h>   // CUtensorMap and the cuTensorMapEncodeTiled prototype
+
 #include "common.cuh"
 #include "solvers.h"
 
@@ -57,6 +59,9 @@ struct LevelDev {
 	int w, h;
 	uint8_t *mask;   // 1 = unknown
 	uint8_t *code;   // 5-point cell code (cell_code), levels below the coarsest
+	// TMA tile maps of b (40 x 40 floats) and code (64 x 40 bytes) for the
+	// tile kernels' region loads; null where the level's layout allows none
+	const CUtensorMap *tmb, *tmc;
 	float *b;        // right-hand side (level 0: the PCG residual r)
 	float *z;        // correction (level 0: the preconditioned residual);
 	                 // fused path: the pre-smoothed correction
@@ -84,6 +89,7 @@ struct ProbDev {
 	float *p2;           // fused path: second search-direction buffer
 	float *b_alt;        // fused path: the other level-0 residual buffer (k_pre5
 	                     // writes the updated r there, then swaps it with lv[0].b)
+	const CUtensorMap *tmb_alt;   // the TMA map of b_alt (swapped with lv[0].tmb)
 	double *r64, *p64, *q64;   // 13-point: FP64 Krylov vectors (else null)
 	double tau_min;            // FP32 inner solve: smallest relative decrease
 	double rtol;
@@ -110,7 +116,8 @@ struct Globals {
 	int guard_outer;    // refinement bodies run
 	int n_inner;        // inner-loop bodies run in total (launch accounting)
 	int n_outer;        // refinement bodies run in total
-	int pad[26];
+	int tma_timeout;    // a TMA region load did not complete in time
+	int pad[25];
 };
 
 // ------------------------------------------------------------------ stencils
@@ -1061,6 +1068,66 @@ __device__ __forceinline__ float az5_cell(const float *z, const uint8_t *m, int 
 	return diag * z[c] + off;
 }
 
+// ------------------------------------------------------------------ TMA
+// Region loads of the tile kernels through the tensor memory accelerator: one
+// thread arms an mbarrier with the byte count and issues the 2-D tile copies;
+// every thread waits on the barrier's phase.  The wait is bounded: after
+// TMA_SPIN unsuccessful probes it records the failure in Globals::tma_timeout
+// and keeps waiting (bounded again) for the copies it started, so that no
+// copy lands in shared memory after the block has moved on.
+constexpr int TMA_SPIN = 1 << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+	return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+	asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+			: "memory");
+}
+
+// 2-D tile copy of the box at element coordinates (x, y) of map into dst;
+// x * element size is a multiple of 16 bytes, dst is 128-byte aligned
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar)
+{
+	asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+			" [%0], [%1, {%2, %3}], [%4];"
+			::"r"(smem_u32(dst)), "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
+			: "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+	uint32_t ok;
+	asm volatile("{\n\t.reg .pred p;\n\t"
+			"mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+			"selp.u32 %0, 1, 0, p;\n\t}"
+			: "=r"(ok)
+			: "r"(smem_u32(bar)), "r"(parity)
+			: "memory");
+	return ok != 0;
+}
+
+// wait for phase 0 of bar; false (and the failure recorded) if it did not
+// complete within the bound
+__device__ __forceinline__ bool mbar_wait0(uint64_t *bar, int *timeout_flag)
+{
+	for (int it = 0; it < TMA_SPIN; it++)
+		if (mbar_try_wait(bar, 0)) return true;
+	atomicExch(timeout_flag, 1);
+	for (int it = 0; it < TMA_SPIN; it++)
+		if (mbar_try_wait(bar, 0)) return false;
+	return false;
+}
+
 // Region code of a shared region cell: the level's cell code (cell_code) with
 // the neighbour bits that point out of the region cleared (those cells are
 // not in shared memory).  For a group of 4 cells of a row (x the lowest byte)
@@ -1144,9 +1211,12 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 		int l, const int *__restrict__ tbeg, const int *__restrict__ tcnt, double *partial, Globals *gl,
 		int use_p2)
 {
-	__shared__ __align__(16) float sb[FN], sz[FN];
+	__shared__ __align__(128) float sb[FN];
+	__shared__ __align__(128) uint8_t stc[FR * 64];   // TMA: the code box (64 bytes a row)
+	__shared__ __align__(16) float sz[FN];
 	__shared__ __align__(16) uint8_t sc[FN];
 	__shared__ double sh[32];
+	__shared__ uint64_t bar;
 	const int4 t = tl[blockIdx.x];
 	const int prob = t.x;
 	const ProbDev &pr = P[prob];
@@ -1157,7 +1227,39 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 	const float *qv = pr.q;
 	const int x0 = t.y * SP_TILE - FH, y0 = t.z * SP_TILE - FH;
 	// every load depends only on the coordinates, so all are in flight at once
-	if ((L.w & 3) == 0) {
+	if (L.tmb) {
+		// TMA: b as a 40 x 40 box at (x0, y0) straight into sb, the codes as a
+		// 64 x 40 box from x0 - 12 (a 16-byte boundary); out of the image both
+		// read 0 (a known cell).  b stays unmasked: it is read at unknown cells
+		// only (sweeps, restriction of unknown children, the PCG step).
+		if (threadIdx.x == 0) {
+			mbar_init(&bar, 1);
+			mbar_expect_tx(&bar, (uint32_t)(FN * sizeof(float) + FR * 64));
+			tma_load_2d(sb, L.tmb, x0, y0, &bar);
+			tma_load_2d(stc, L.tmc, x0 - 12, y0, &bar);
+		}
+		for (int c = threadIdx.x; c < FN; c += SP_THREADS) sz[c] = 0.f;
+		__syncthreads();   // the barrier is initialised
+		mbar_wait0(&bar, &gl->tma_timeout);
+#pragma unroll
+		for (int it = 0; it < (FN / 4 + SP_THREADS - 1) / SP_THREADS; it++) {
+			const int f = threadIdx.x + it * SP_THREADS;
+			if (f < FN / 4) {
+				const int ry = f / (FR / 4), rx = 4 * (f - ry * (FR / 4));
+				const uint32_t cd = region_codes4(*(const uint32_t *)(stc + ry * 64 + rx + 12), rx, ry);
+				*(uint32_t *)(sc + ry * FR + rx) = cd;
+				if (upd && cd) {
+					const int gi = x0 + rx, gj = y0 + ry;   // a group with an unknown is in the image
+					const float4 qq = *(const float4 *)(qv + (size_t)gj * L.w + gi);
+					float *b4 = sb + ry * FR + rx;
+					b4[0] = __fmaf_rn(-a, qq.x, b4[0]);
+					b4[1] = __fmaf_rn(-a, qq.y, b4[1]);
+					b4[2] = __fmaf_rn(-a, qq.z, b4[2]);
+					b4[3] = __fmaf_rn(-a, qq.w, b4[3]);
+				}
+			}
+		}
+	} else if ((L.w & 3) == 0) {
 		// groups of 4 cells of a row (aligned, wholly inside or outside)
 #pragma unroll
 		for (int it = 0; it < (FN / 4 + SP_THREADS - 1) / SP_THREADS; it++) {
@@ -1277,6 +1379,9 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 		float *nb = w.b_alt;
 		w.b_alt = w.lv[0].b;
 		w.lv[0].b = nb;
+		const CUtensorMap *nm = w.tmb_alt;   // and its TMA map
+		w.tmb_alt = w.lv[0].tmb;
+		w.lv[0].tmb = nm;
 		if (tot[0] <= s.tau2 || s.iter >= INNER_MAX || s.total_iter >= s.max_iter) {
 			s.inner_active = 0;
 			atomicSub(&gl->inner_count, 1);
@@ -2613,6 +2718,35 @@ void kt_collect(simpois_ctx *ctx, KTimer &kt)
 
 }  // namespace
 
+// cuTensorMapEncodeTiled from the driver (the runtime is linked statically;
+// the driver entry point needs no link against libcuda); null if absent.
+PFN_cuTensorMapEncodeTiled_v12000 tma_encoder()
+{
+	static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+		void *f = nullptr;
+		cudaDriverEntryPointQueryResult q;
+		if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+				cudaSuccess || q != cudaDriverEntryPointSuccess)
+			f = nullptr;
+		return (PFN_cuTensorMapEncodeTiled_v12000)f;
+	}();
+	return fn;
+}
+
+// A 2-D tile map of a w x h level array (elem 4: float, 1: byte) with box bw x
+// bh, zero fill outside; false where the layout allows none (the row stride
+// must be a multiple of 16 bytes) or the driver refuses it.
+bool tma_map(CUtensorMap *m, void *base, int w, int h, int elem, int bw, int bh)
+{
+	PFN_cuTensorMapEncodeTiled_v12000 fn = tma_encoder();
+	if (!fn || ((size_t)w * elem) % 16 != 0 || ((uintptr_t)base & 15) != 0) return false;
+	cuuint64_t dims[2] = {(cuuint64_t)w, (cuuint64_t)h}, strides[1] = {(cuuint64_t)w * elem};
+	cuuint32_t box[2] = {(cuuint32_t)bw, (cuuint32_t)bh}, es[2] = {1, 1};
+	return fn(m, elem == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, base, dims,
+			strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+			CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 int mg_handover_level(int w, int h, int coarse_max)
 {
 	int lw[MAXLEV], lh[MAXLEV];
@@ -2722,6 +2856,12 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	size_t o_tbeg = Lo.take(sizeof(int) * n), o_tcnt = Lo.take(sizeof(int) * n);
 	size_t o_part = Lo.take(sizeof(double) * 2 * std::max<size_t>(1, lists[0].size()));
 	size_t o_gptr = Lo.take(sizeof(void *) * 3 * n);
+	// TMA maps (b and code) of the tile levels whose rows are 16-byte multiples
+	int nmaps = 0;
+	for (int k = 0; k < n && opt.tma; k++)
+		for (int l = 0; l < pl.hp[k].nfine; l++)
+			if (pl.hp[k].lv[l].w % 16 == 0) nmaps += l == 0 ? 3 : 2;   // level 0: also b_alt
+	size_t o_tmap = Lo.take(sizeof(CUtensorMap) * std::max(1, nmaps), 128);
 	size_t total = Lo.off;
 	int rc = ctx_arena_reserve(ctx, total);
 	if (rc) return rc;
@@ -2731,6 +2871,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	size_t stage_bytes = sizeof(ProbDev) * n + sizeof(ProbState) * n + sizeof(Globals);
 	for (int l = 0; l < pl.nlev_max; l++) stage_bytes += sizeof(int4) * lists[l].size();
 	stage_bytes += 64 * MAXLEV + sizeof(void *) * 3 * n + sizeof(int) * n + 16 * (MAXLEV + 16) + 4096;
+	stage_bytes += sizeof(CUtensorMap) * nmaps + 128;
 	rc = ctx_pinned_reserve(ctx, stage_bytes + 256);
 	if (rc) return rc;
 	char *stage = ctx->pinned + 256;  // the first 256 bytes hold read-back scalars
@@ -2766,6 +2907,31 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 			d.lv[l].b = (float *)(A + off_b[l][k]);
 			d.lv[l].z = (float *)(A + off_z[l][k]);
 			d.lv[l].z2 = (float *)(A + off_z2[l][k]);
+			d.lv[l].tmb = d.lv[l].tmc = nullptr;
+		}
+		d.tmb_alt = nullptr;
+	}
+	// the TMA maps: encoded on the host, uploaded with the tables
+	std::vector<CUtensorMap> maps(std::max(1, nmaps));
+	{
+		CUtensorMap *dmaps = (CUtensorMap *)(A + o_tmap);
+		int im = 0;
+		for (int k = 0; k < n && opt.tma; k++) {
+			ProbDev &d = pl.hp[k];
+			for (int l = 0; l < d.nfine; l++) {
+				LevelDev &L = d.lv[l];
+				if (L.w % 16 != 0) continue;
+				const int nm = l == 0 ? 3 : 2;
+				// level 0 swaps b with b_alt every PCG step, so both get a map
+				if (tma_map(&maps[im], L.b, L.w, L.h, 4, FR, FR) &&
+						tma_map(&maps[im + 1], L.code, L.w, L.h, 1, 64, FR) &&
+						(l != 0 || tma_map(&maps[im + 2], d.b_alt, L.w, L.h, 4, FR, FR))) {
+					L.tmb = dmaps + im;
+					L.tmc = dmaps + im + 1;
+					if (l == 0) d.tmb_alt = dmaps + im + 2;
+				}
+				im += nm;
+			}
 		}
 	}
 	pl.dp = (ProbDev *)(A + o_dp);
@@ -2804,6 +2970,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	Globals hg;
 	memset(&hg, 0, sizeof(hg));
 	SP_CUDA(ctx, put(pl.dp, pl.hp.data(), sizeof(ProbDev) * n));
+	if (nmaps) SP_CUDA(ctx, put(A + o_tmap, maps.data(), sizeof(CUtensorMap) * nmaps));
 	SP_CUDA(ctx, put(pl.dst, hst.data(), sizeof(ProbState) * n));
 	SP_CUDA(ctx, put(pl.gl, &hg, sizeof(hg)));
 	for (int l = 0; l < pl.nlev_max; l++)
@@ -2872,8 +3039,11 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	}
 	SP_LAUNCH_CHECK(ctx);
 	ProbState *hs = (ProbState *)stage;
+	int *htma = (int *)(stage + ((sizeof(ProbState) * n + 15) / 16 * 16));
 	SP_CUDA(ctx, cudaMemcpyAsync(hs, pl.dst, sizeof(ProbState) * n, cudaMemcpyDeviceToHost, s));
+	SP_CUDA(ctx, cudaMemcpyAsync(htma, &pl.gl->tma_timeout, sizeof(int), cudaMemcpyDeviceToHost, s));
 	SP_CUDA(ctx, cudaStreamSynchronize(s));
+	if (*htma) return ctx_fail(ctx, SIMPOIS_ECUDA, "a TMA region load did not complete in time");
 	for (int k = 0; k < n; k++) {
 		rep[k].status = hs[k].status;
 		rep[k].unknowns = hs[k].nunknown;

@@ -15,6 +15,7 @@ from . import _build
 OK, EINVAL, ENOMEM, NOT_CONVERGED, BREAKDOWN, ECUDA, ENODEV, SINGULAR = range(8)
 FLAG_NO_MG, FLAG_NO_GRAPH, FLAG_OUT_RESID, FLAG_UNFUSED, FLAG_KTIMER = 0x1, 0x2, 0x4, 0x8, 0x10
 FLAG_MINI = 0x20
+FLAG_TMA = 0x40
 
 STATUS_NAMES = {OK: "ok", EINVAL: "einval", ENOMEM: "enomem", NOT_CONVERGED: "not_converged",
                 BREAKDOWN: "breakdown", ECUDA: "ecuda", ENODEV: "enodev", SINGULAR: "singular"}

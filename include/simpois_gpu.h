@@ -84,6 +84,12 @@ typedef struct {
  * (ftr/minisimpois.c:127-162): the plain clamped Laplacian for every tstep,
  * nearest-neighbour prolongation, no CG branch */
 #define SIMPOIS_FLAG_MINI        0x20
+/* converged schedule: the fused V-cycle's tile kernels load their regions
+ * with the tensor memory accelerator (TMA) instead of vector loads, where a
+ * level's rows are multiples of 16 bytes.  Same results bit for bit; measured
+ * 1-4 % slower on the workloads here (the tiles are instruction-bound and a
+ * TMA load is a wait for the whole box), so it is off by default. */
+#define SIMPOIS_FLAG_TMA         0x40
 
 /* Per-channel result record. */
 typedef struct {

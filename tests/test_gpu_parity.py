@@ -326,3 +326,22 @@ def test_converged_thin_images(sp, h, w):
         x = fp64.solve(g[0], f[0] if kind == 0 else None, kind)
         assert np.abs(o[m] - x[m]).max() <= 1e-4 * max(1.0, np.abs(x[m]).max())
         assert np.array_equal(_bits(o[~m]), _bits(g[0][~m]))
+
+
+@pytest.mark.parametrize("h,w,pd", [(384, 512, 2), (330, 640, 1), (200, 520, 1)])
+def test_tma_region_loads_same_bits(sp, h, w, pd):
+    """SIMPOIS_FLAG_TMA: the tile kernels load their regions through the
+    tensor memory accelerator where a level's rows are 16-byte multiples;
+    the result is the same bits as the vector loads' (and as the unfused
+    kernels')."""
+    from imscript_gb300 import lib, synth
+    rng = np.random.default_rng(h + w + pd)
+    g = np.stack([synth.gaussian_field(rng, h, w, 8) for _ in range(pd)])
+    g[:, synth.disk_mask(rng, h, w, 0.25, rmin=3, rmax=30)] = np.nan
+    f = np.stack([synth.guidance(synth.gaussian_field(rng, h, w, 8))[2] for _ in range(pd)])
+    a, ra = sp.solve(_cuda(g), _cuda(f), rtol=1e-6)
+    b, rb = sp.solve(_cuda(g), _cuda(f), rtol=1e-6, flags=lib.FLAG_TMA)
+    c, rc = sp.solve(_cuda(g), _cuda(f), rtol=1e-6, flags=lib.FLAG_UNFUSED)
+    assert [r["iterations"] for r in ra] == [r["iterations"] for r in rb] == [r["iterations"] for r in rc]
+    assert torch.equal(a.view(torch.int32), b.view(torch.int32))
+    assert torch.equal(a.view(torch.int32), c.view(torch.int32))
