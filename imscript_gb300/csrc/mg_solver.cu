@@ -1167,19 +1167,40 @@ __device__ __forceinline__ float diag_code(int code) { return 4.f - (float)(code
 // The colour cells of the 40x40 region a thread owns: for colour col, cell
 // q = tid + 256 k (k < 4, q < 800) of the compacted class, packed as
 // (region index) | (ring << 11); ring = distance to the region's edge.
+// x0 + y0 is even for every tile (both are multiples of 32 minus FH), so
+// the cells depend on the thread alone: a table built at compile time.
+struct CellTable {
+	int v[2][4][SP_THREADS];
+};
+
+constexpr CellTable make_cell_table()
+{
+	CellTable t{};
+	for (int col = 0; col < 2; col++)
+		for (int k = 0; k < 4; k++)
+			for (int tid = 0; tid < SP_THREADS; tid++) {
+				const int q = tid + SP_THREADS * k;
+				if (q >= FN / 2) {
+					t.v[col][k][tid] = -1;
+					continue;
+				}
+				const int ry = q / (FR / 2);
+				const int rx = 2 * (q - ry * (FR / 2)) + ((col ^ ry) & 1);
+				const int a = rx < ry ? rx : ry, b = FR - 1 - rx < FR - 1 - ry ? FR - 1 - rx : FR - 1 - ry;
+				t.v[col][k][tid] = (ry * FR + rx) | ((a < b ? a : b) << 11);
+			}
+	return t;
+}
+
+__device__ const CellTable g_cells = make_cell_table();
+static_assert(FH % 2 == 0, "x0 + y0 must stay even for the cell table");
+
 __device__ __forceinline__ void own_cells(int x0, int y0, int cells[2][4])
 {
 #pragma unroll
 	for (int col = 0; col < 2; col++)
 #pragma unroll
-		for (int k = 0; k < 4; k++) {
-			const int q = threadIdx.x + SP_THREADS * k;
-			if (q >= FN / 2) { cells[col][k] = -1; continue; }
-			const int ry = q / (FR / 2);
-			const int rx = 2 * (q - ry * (FR / 2)) + ((col ^ (x0 + y0 + ry)) & 1);
-			const int ring = min(min(rx, ry), min(FR - 1 - rx, FR - 1 - ry));
-			cells[col][k] = (ry * FR + rx) | (ring << 11);
-		}
+		for (int k = 0; k < 4; k++) cells[col][k] = g_cells.v[col][k][threadIdx.x];
 }
 
 // Half-sweep of colour col over the cells with ring >= lo.
