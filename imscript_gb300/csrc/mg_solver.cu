@@ -200,6 +200,60 @@ __device__ __forceinline__ int colour_of(int K, int i, int j) { return K == 0 ? 
 __device__ __forceinline__ int tile_i(int4 t) { return t.y * SP_TILE + (threadIdx.x & 31); }
 __device__ __forceinline__ int tile_j(int4 t, int r) { return t.z * SP_TILE + (threadIdx.x >> 5) + SP_BLOCK_Y * r; }
 
+// The 4-pixel row group a thread takes in the level-0 PCG updates (k_xr,
+// k_rz and the fused kernels' PCG work): row tid / 8 of the tile, columns
+// 4 (tid % 8) + 0..3; a thread adds its terms left to right.  Level-0 arrays
+// live in the arena (256-byte aligned), so a full group of a level whose
+// width is a multiple of 4 moves as one 16-byte access.
+struct Grp {
+	size_t k;   // first pixel
+	int n;      // pixels of the group in the image (0..4)
+	bool vec;   // one aligned 16-byte access
+};
+
+__device__ __forceinline__ Grp grp_of(int4 t, int w, int h)
+{
+	const int i = t.y * SP_TILE + 4 * (threadIdx.x & 7), j = t.z * SP_TILE + (threadIdx.x >> 3);
+	Grp g;
+	g.n = (i < w && j < h) ? min(4, w - i) : 0;
+	g.k = g.n ? (size_t)j * w + i : 0;
+	g.vec = g.n == 4 && (w & 3) == 0;
+	return g;
+}
+
+__device__ __forceinline__ void ld4(const float *p, const Grp &g, float v[4])
+{
+	if (g.vec) {
+		const float4 q = *(const float4 *)(p + g.k);
+		v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+	} else {
+#pragma unroll
+		for (int e = 0; e < 4; e++) v[e] = e < g.n ? p[g.k + e] : 0.f;
+	}
+}
+
+__device__ __forceinline__ void ldm4(const uint8_t *p, const Grp &g, uint8_t v[4])
+{
+	if (g.vec) {
+		const uchar4 q = *(const uchar4 *)(p + g.k);
+		v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+	} else {
+#pragma unroll
+		for (int e = 0; e < 4; e++) v[e] = e < g.n ? p[g.k + e] : 0;
+	}
+}
+
+__device__ __forceinline__ void st4(float *p, const Grp &g, const float v[4])
+{
+	if (g.vec) {
+		*(float4 *)(p + g.k) = make_float4(v[0], v[1], v[2], v[3]);
+	} else {
+#pragma unroll
+		for (int e = 0; e < 4; e++)
+			if (e < g.n) p[g.k + e] = v[e];
+	}
+}
+
 // Per-problem deterministic reduction of up to two values over the level-0
 // tiles of the problem.  Returns true in the last tile's block (all threads);
 // the sums are then in tot[0..1] (thread 0).
@@ -756,35 +810,30 @@ __global__ void __launch_bounds__(SP_THREADS) k_xr(const ProbDev *__restrict__ P
 	const LevelDev &L = pr.lv[0];
 	const float a = (float)st[prob].alpha;
 	const float *pv = use_p2 ? pr.p2 : pr.p;
-	int i = tile_i(t);
 	FF rr = {0.f, 0.f};
-	// all loads of the four rows first (they depend only on coordinates)
-	uint8_t m[SP_ROWS];
-	float xv[SP_ROWS], xl[SP_ROWS], pk[SP_ROWS], bk[SP_ROWS], qk[SP_ROWS];
-	int kk[SP_ROWS];
+	const Grp g = grp_of(t, pr.w, pr.h);
+	if (g.n) {
+		uint8_t m[4];
+		float xv[4], xl[4], pk[4], bk[4], qk[4];
+		ldm4(L.mask, g, m);
+		ld4(pr.x, g, xv);
+		ld4(pr.xlo, g, xl);
+		ld4(pv, g, pk);
+		ld4(L.b, g, bk);
+		ld4(pr.q, g, qk);
 #pragma unroll
-	for (int r = 0; r < SP_ROWS; r++) {
-		const int j = tile_j(t, r);
-		const bool in = i < pr.w && j < pr.h;
-		kk[r] = in ? j * pr.w + i : 0;
-		m[r] = in ? L.mask[kk[r]] : 0;
-		xv[r] = in ? pr.x[kk[r]] : 0.f;
-		xl[r] = in ? pr.xlo[kk[r]] : 0.f;
-		pk[r] = in ? pv[kk[r]] : 0.f;
-		bk[r] = in ? L.b[kk[r]] : 0.f;
-		qk[r] = in ? pr.q[kk[r]] : 0.f;
-	}
-#pragma unroll
-	for (int r = 0; r < SP_ROWS; r++) {
-		if (m[r]) {
-			FF xn = {xv[r], xl[r]};
-			ff_add_prod(xn, a, pk[r]);
-			pr.x[kk[r]] = xn.hi;
-			pr.xlo[kk[r]] = xn.lo;
-			const float rk = __fmaf_rn(-a, qk[r], bk[r]);
-			L.b[kk[r]] = rk;
-			ff_add_prod(rr, rk, rk);
+		for (int e = 0; e < 4; e++) {
+			if (!m[e]) continue;   // known pixels are written back unchanged
+			FF xn = {xv[e], xl[e]};
+			ff_add_prod(xn, a, pk[e]);
+			xv[e] = xn.hi;
+			xl[e] = xn.lo;
+			bk[e] = __fmaf_rn(-a, qk[e], bk[e]);
+			ff_add_prod(rr, bk[e], bk[e]);
 		}
+		st4(pr.x, g, xv);
+		st4(pr.xlo, g, xl);
+		st4(L.b, g, bk);
 	}
 	double tot[2];
 	if (problem_sum1_ff(rr, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
@@ -809,14 +858,17 @@ __global__ void k_rz(const ProbDev *__restrict__ P, ProbState *st, const int4 *_
 	if (!st[prob].inner_active) return;
 	const ProbDev &pr = P[prob];
 	const LevelDev &L = pr.lv[0];
-	int i = tile_i(t);
 	FF rz = {0.f, 0.f};
-	for (int r = 0; r < SP_ROWS; r++) {
-		int j = tile_j(t, r);
-		if (i < pr.w && j < pr.h) {
-			size_t k = (size_t)j * pr.w + i;
-			if (L.mask[k]) ff_add_prod(rz, L.b[k], L.z[k]);
-		}
+	const Grp g = grp_of(t, pr.w, pr.h);
+	if (g.n) {
+		uint8_t m[4];
+		float bv[4], zv[4];
+		ldm4(L.mask, g, m);
+		ld4(L.b, g, bv);
+		ld4(L.z, g, zv);
+#pragma unroll
+		for (int e = 0; e < 4; e++)
+			if (m[e]) ff_add_prod(rz, bv[e], zv[e]);
 	}
 	double tot[2];
 	if (problem_sum1_ff(rz, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
@@ -1331,32 +1383,32 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 	FF rr = {0.f, 0.f};
 	if (upd) {
 		const float *pv = use_p2 ? pr.p2 : pr.p;
-		const int i = tile_i(t);
-		float xv[SP_ROWS], xl[SP_ROWS], pk[SP_ROWS];
-		uint8_t mk[SP_ROWS];
-		int kk[SP_ROWS];
-#pragma unroll
-		for (int r = 0; r < SP_ROWS; r++) {
-			const int j = tile_j(t, r);
-			const bool in = i < L.w && j < L.h;
-			kk[r] = in ? j * L.w + i : 0;
-			mk[r] = in ? L.mask[kk[r]] : 0;
-			xv[r] = in ? pr.x[kk[r]] : 0.f;
-			xl[r] = in ? pr.xlo[kk[r]] : 0.f;
-			pk[r] = in ? pv[kk[r]] : 0.f;
+		const Grp g = grp_of(t, L.w, L.h);
+		float xv[4], xl[4], pk[4];
+		uint8_t mk[4];
+		if (g.n) {
+			ldm4(L.mask, g, mk);
+			ld4(pr.x, g, xv);
+			ld4(pr.xlo, g, xl);
+			ld4(pv, g, pk);
 		}
 		__syncthreads();   // sb holds the new r
+		if (g.n) {
+			const float *rb = sb + ((threadIdx.x >> 3) + FH) * FR + 4 * (threadIdx.x & 7) + FH;
+			float rk[4];
 #pragma unroll
-		for (int r = 0; r < SP_ROWS; r++) {
-			if (mk[r]) {
-				FF xn = {xv[r], xl[r]};
-				ff_add_prod(xn, a, pk[r]);
-				pr.x[kk[r]] = xn.hi;
-				pr.xlo[kk[r]] = xn.lo;
-				const float rk = sb[(tile_j(t, r) - y0) * FR + (i - x0)];
-				pr.b_alt[kk[r]] = rk;
-				ff_add_prod(rr, rk, rk);
+			for (int e = 0; e < 4; e++) {
+				rk[e] = rb[e];
+				if (!mk[e]) continue;
+				FF xn = {xv[e], xl[e]};
+				ff_add_prod(xn, a, pk[e]);
+				xv[e] = xn.hi;
+				xl[e] = xn.lo;
+				ff_add_prod(rr, rk[e], rk[e]);
 			}
+			st4(pr.x, g, xv);
+			st4(pr.xlo, g, xl);
+			st4(pr.b_alt, g, rk);
 		}
 	}
 	int cells[2][4];
@@ -1369,9 +1421,9 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 		__syncthreads();
 	}
 	// write the pre-smoothed correction of the tile
-	for (int c = threadIdx.x; c < SP_TILE * SP_TILE; c += SP_THREADS) {
-		const int ty = c >> 5, tx = c & 31, gi = x0 + FH + tx, gj = y0 + FH + ty;
-		if (gi < L.w && gj < L.h) L.z[(size_t)gj * L.w + gi] = sz[(ty + FH) * FR + tx + FH];
+	{
+		const Grp g = grp_of(t, L.w, L.h);
+		if (g.n) st4(L.z, g, sz + ((threadIdx.x >> 3) + FH) * FR + 4 * (threadIdx.x & 7) + FH);
 	}
 	// restriction: one coarse cell per thread (16 x 16 per tile)
 	const int ci = t.y * (SP_TILE / 2) + (threadIdx.x & 15), cj = t.z * (SP_TILE / 2) + (threadIdx.x >> 4);
@@ -1488,13 +1540,16 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_post5(const ProbDev *__restri
 		sweep_cells(sz, sb, sc, cells, 1 - (s & 1), s + 1);
 		__syncthreads();
 	}
+	// z2 of the tile and, in k_rz's order, r.z
 	FF rz = {0.f, 0.f};
-	for (int c = threadIdx.x; c < SP_TILE * SP_TILE; c += SP_THREADS) {
-		const int ty = c >> 5, tx = c & 31, gi = x0 + FH + tx, gj = y0 + FH + ty;
-		if (gi < L.w && gj < L.h) {
-			const int rc = (ty + FH) * FR + tx + FH;
-			L.z2[(size_t)gj * L.w + gi] = sz[rc];
-			if (sc[rc] & 1) ff_add_prod(rz, sb[rc], sz[rc]);
+	{
+		const Grp g = grp_of(t, L.w, L.h);
+		if (g.n) {
+			const int rc = ((threadIdx.x >> 3) + FH) * FR + 4 * (threadIdx.x & 7) + FH;
+			st4(L.z2, g, sz + rc);
+#pragma unroll
+			for (int e = 0; e < 4; e++)
+				if (e < g.n && (sc[rc + e] & 1)) ff_add_prod(rz, sb[rc + e], sz[rc + e]);
 		}
 	}
 	if (l != 0 || !pcg) return;
