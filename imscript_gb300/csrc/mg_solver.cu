@@ -7,23 +7,41 @@
 // cleant_cgpois.c:67-89) or the 13-point bilaplacian with a single clamp
 // (kind 1, cleant_cgpois.c:91-121), restricted to U, and b = -f_U - A_UK g_K.
 //
-// Refinement (FP64).  The solution lives in an FP64 image Ufull (g at the
-// known pixels).  Each refinement step computes r = b - A Ufull in FP64 and
-// its norm (the FP64 relative residual reported to the caller), stops when it
-// is <= rtol, otherwise solves A d = (float)r in FP32 and adds d in FP64.
+// Refinement (FP64).  The solution of the unknowns lives in FP64 (U; known
+// pixels are read from g).  Each refinement step computes r = b - A u in
+// FP64 and its norm (the FP64 relative residual reported to the caller),
+// stops when it is <= rtol, otherwise solves A d = (float)r and adds d in
+// FP64.  FP64 issues at about 1/70 of the FP32 rate on this GPU, so it is
+// spent only there: the FP32 PCG's dot products sum their per-pixel terms as
+// float-float pairs and go to double once per warp.
 //
-// Inner solve (FP32 vectors, FP64 reductions).  Preconditioned CG, the
-// preconditioner one V(2,2)-cycle of geometric multigrid on the masked grid:
+// Inner solve, 5-point (FP32).  Preconditioned CG; the preconditioner is one
+// V(2,2)-cycle of geometric multigrid on the masked grid:
 //   * level l+1 is ceil(w/2) x ceil(h/2); a coarse pixel is unknown iff all
 //     its (existing) children are unknown, so that every coarse level keeps
 //     the known pixels that make it non-singular;
-//   * the coarse operators are the same clamped stencils on the coarse masks;
-//   * smoothing is colour-ordered Gauss-Seidel (2 colours and 2 sweeps for 5
-//     points, 5 colours and 4 sweeps for 13 points), forward before the coarse correction and backward after it,
-//     so the cycle is a symmetric operator when A is;
-//   * restriction sums the children's residuals (times 2 for the 13-point
-//     operator), prolongation injects the coarse correction into the unknown
-//     children; the coarsest level (<= 4 x 4) gets 4 symmetric sweeps.
+//   * the coarse operators are the same clamped stencils on the coarse masks,
+//     read through per-level cell codes (which neighbours are unknown, how
+//     many sides are clamped);
+//   * smoothing is red-black Gauss-Seidel, forward before the coarse
+//     correction and backward after it, so the cycle is symmetric;
+//   * restriction sums the children's residuals, prolongation injects the
+//     coarse correction into the unknown children; the coarsest level
+//     (<= 4 x 4) gets 4 symmetric sweeps.
+// The fused cycle: k_pre5 / k_post5 take one 32 x 32 tile per block with a
+// halo of 4 in shared memory (all sweeps of a level in one launch, the
+// restriction or the injection fused in), k_coarse5 takes every level below
+// the hand-over size of a problem in one block.  k_pre5 at level 0 also takes
+// the PCG step (x, r), so an iteration is k_spmv5 and one V-cycle.  The SpMV
+// is evaluated in difference form and the iterate carried as float-float, so
+// that the FP32 recurrence's residual stays close to the true one.
+//
+// Inner solve, 13-point.  PCG with FP64 vectors and A p (an FP32 recurrence
+// cannot resolve the biharmonic's smoothest modes), preconditioned by two
+// fused 5-point V-cycles, with the flexible (Polak-Ribiere) beta since the
+// FP32 preconditioner is only approximately symmetric.  Without the fused
+// kernels (SIMPOIS_FLAG_UNFUSED), the one-launch-per-sweep cycle and FP32
+// PCG serve both operators (5 colours and 4 sweeps for 13 points).
 //
 // Batching.  All problems of a call share every launch: each level keeps one
 // list of 32 x 32 tiles that contain unknowns, over all problems.  Every
@@ -31,8 +49,9 @@
 // sum, the last tile of a problem to finish (an atomic counter) sums the
 // problem's partials in tile order and updates the problem's scalars.  A
 // problem whose inner solve has converged skips every later launch (early
-// retirement).  One PCG iteration is captured once into a CUDA graph and
-// replayed; the host reads one counter every few iterations.
+// retirement).  The whole solve is one CUDA graph with two nested
+// device-driven WHILE loops (refinement steps, PCG iterations), captured
+// once per plan and replayed.
 #include <algorithm>
 #include <climits>
 #include <cmath>
