@@ -138,6 +138,9 @@ struct Globals {
 	int tma_timeout;    // a TMA region load did not complete in time
 	int pad[25];
 };
+// read back into the first 256 bytes of the pinned staging, ahead of the
+// states that follow them
+static_assert(sizeof(Globals) <= 256, "Globals must fit the pinned read-back slot");
 
 // ------------------------------------------------------------------ stencils
 
@@ -506,19 +509,40 @@ __global__ void k_mask_down(const ProbDev *__restrict__ P, const int4 *__restric
 	const LevelDev &C = pr.lv[l], &F = pr.lv[l - 1];
 	if (threadIdx.x == 0) any = 0;
 	__syncthreads();
-	int i = tile_i(t);
 	int mine = 0;
-	for (int r = 0; r < SP_ROWS; r++) {
-		int j = tile_j(t, r);
-		if (i < C.w && j < C.h) {
-			bool u = true;
-			for (int b = 0; b < 2; b++)
-				for (int a = 0; a < 2; a++) {
-					int fi = 2 * i + a, fj = 2 * j + b;
-					if (fi < F.w && fj < F.h) u = u && F.mask[(size_t)fj * F.w + fi];
-				}
-			C.mask[(size_t)j * C.w + i] = u;
-			mine |= u;
+	if ((F.w & 7) == 0) {
+		// a row group of 4 coarse cells: its children are 8 bytes of each of
+		// two fine rows (aligned: F.w and 2 i are multiples of 8)
+		const Grp g = grp_of(t, C.w, C.h);
+		if (g.n) {
+			const int i = t.y * SP_TILE + 4 * (threadIdx.x & 7), j = t.z * SP_TILE + (threadIdx.x >> 3);
+			const uint8_t *f0 = F.mask + (size_t)(2 * j) * F.w + 2 * i;
+			const unsigned long long r0 = *(const unsigned long long *)f0;
+			const unsigned long long r1 = 2 * j + 1 < F.h ? *(const unsigned long long *)(f0 + F.w) : r0;
+			const unsigned long long both = r0 & r1;   // masks are 0 or 1
+			uint32_t out = 0;
+#pragma unroll
+			for (int e = 0; e < 4; e++) {
+				const uint32_t u = (uint32_t)((both >> (16 * e)) & (both >> (16 * e + 8)) & 1ull);
+				out |= u << (8 * e);
+			}
+			*(uint32_t *)(C.mask + g.k) = out;
+			mine = out != 0;
+		}
+	} else {
+		int i = tile_i(t);
+		for (int r = 0; r < SP_ROWS; r++) {
+			int j = tile_j(t, r);
+			if (i < C.w && j < C.h) {
+				bool u = true;
+				for (int b = 0; b < 2; b++)
+					for (int a = 0; a < 2; a++) {
+						int fi = 2 * i + a, fj = 2 * j + b;
+						if (fi < F.w && fj < F.h) u = u && F.mask[(size_t)fj * F.w + fi];
+					}
+				C.mask[(size_t)j * C.w + i] = u;
+				mine |= u;
+			}
 		}
 	}
 	if (__any_sync(0xffffffffu, mine) && (threadIdx.x & 31) == 0) atomicOr(&any, 1);
@@ -2336,6 +2360,9 @@ struct Plan {
 	int nfine_max = 0;         // largest nfine over the problems
 	int coarse_smem = 0;       // dynamic shared memory of k_coarse5
 	struct KTimer *kt = nullptr;   // kernel timer, or null
+	// device-driven solve: the loop counters are read back with the final
+	// states (one synchronisation); the launch count is completed then
+	const Globals *hg = nullptr;
 };
 
 // Kernel timer: an event pair around each launch of the main-loop kernels,
@@ -2678,10 +2705,9 @@ int run_device_loop(simpois_ctx *ctx, Plan &pl, const MgOptions &opt, int mode, 
 	}
 	cudaStream_t s = ctx->stream;
 	SP_CUDA(ctx, cudaGraphLaunch(ctx->solve_exec, s));
-	Globals *hg = (Globals *)ctx->pinned;
+	Globals *hg = (Globals *)ctx->pinned;   // read with the final states
 	SP_CUDA(ctx, cudaMemcpyAsync(hg, pl.gl, sizeof(Globals), cudaMemcpyDeviceToHost, s));
-	SP_CUDA(ctx, cudaStreamSynchronize(s));
-	*pl.nl += ctx->solve_nodes_outer * hg->n_outer + ctx->solve_nodes_inner * hg->n_inner;
+	pl.hg = hg;
 	*done = true;
 	return SIMPOIS_OK;
 }
@@ -3138,6 +3164,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	SP_CUDA(ctx, cudaMemcpyAsync(hs, pl.dst, sizeof(ProbState) * n, cudaMemcpyDeviceToHost, s));
 	SP_CUDA(ctx, cudaMemcpyAsync(htma, &pl.gl->tma_timeout, sizeof(int), cudaMemcpyDeviceToHost, s));
 	SP_CUDA(ctx, cudaStreamSynchronize(s));
+	if (pl.hg) *pl.nl += ctx->solve_nodes_outer * pl.hg->n_outer + ctx->solve_nodes_inner * pl.hg->n_inner;
 	if (*htma) return ctx_fail(ctx, SIMPOIS_ECUDA, "a TMA region load did not complete in time");
 	for (int k = 0; k < n; k++) {
 		rep[k].status = hs[k].status;
