@@ -277,10 +277,264 @@ static int semantic_name(const char *name, raw_image *x, int *rc)
 	return 1;
 }
 
+/* ------------------------------------------- transformations on reading */
+
+/* Exchange the samples of pixels (i, j) and (a, b). */
+static void swap_pixels(raw_image *x, int i, int j, int a, int b)
+{
+	double *p = x->v + ((size_t)j * x->w + i) * x->pd, *q = x->v + ((size_t)b * x->w + a) * x->pd;
+	for (int l = 0; l < x->pd; l++) {
+		double t = p[l];
+		p[l] = q[l];
+		q[l] = t;
+	}
+}
+
+static void flip_leftright(raw_image *x)
+{
+	for (int j = 0; j < x->h; j++)
+		for (int i = 0; i < x->w / 2; i++) swap_pixels(x, i, j, x->w - 1 - i, j);
+}
+
+static void flip_topdown(raw_image *x)
+{
+	for (int j = 0; j < x->h / 2; j++)
+		for (int i = 0; i < x->w; i++) swap_pixels(x, i, j, i, x->h - 1 - j);
+}
+
+/* out(i, j) = in(j, i); the image becomes h x w */
+static int transpose(raw_image *x)
+{
+	const int nw = x->h, nh = x->w, pd = x->pd;
+	double *y = xcalloc((size_t)nw * nh * pd, sizeof(double));
+	if (!y) return 1;
+	for (int j = 0; j < nh; j++)
+		for (int i = 0; i < nw; i++)
+			for (int l = 0; l < pd; l++)
+				y[((size_t)j * nw + i) * pd + l] = x->v[((size_t)i * x->w + j) * pd + l];
+	free(x->v);
+	x->v = y;
+	x->w = nw;
+	x->h = nh;
+	return 0;
+}
+
+/* iio's two-letter orientations (iio.c:814-823): an upper-case first letter
+ * flips left-right, an upper-case second letter flips top-down, and the
+ * letters in the order y, x transpose, in that order. */
+static int reorient(raw_image *x, int orx, int ory)
+{
+	if (isupper(orx)) flip_leftright(x);
+	if (isupper(ory)) flip_topdown(x);
+	if (toupper(orx) > toupper(ory)) return transpose(x);
+	return 0;
+}
+
+/* A permutation of the three axes of the interleaved samples, named "x"
+ * (the channels), "y" (the columns) and "z" (the rows); the i-th letter of
+ * t names the input axis that becomes output axis i, the first being the
+ * new channel axis (iio.c:887-956). */
+static int reorient3d(raw_image *x, const char *t)
+{
+	static const char *known[] = {"xyz", "yxz", "xzy", "zxy", "zyx", "yzx"};
+	int ok = 0;
+	for (int k = 0; k < 6; k++) ok |= !strcmp(t, known[k]);
+	if (!ok) {
+		fprintf(stderr, "imageio: unrecognized trasnposition string \"%s\"\n", t);
+		return 1;
+	}
+	const int u[3] = {x->pd, x->w, x->h};
+	int v[3], ax[3];
+	for (int k = 0; k < 3; k++) {
+		ax[k] = t[k] - 'x';
+		v[k] = u[ax[k]];
+	}
+	double *y = xcalloc((size_t)u[0] * u[1] * u[2], sizeof(double));
+	if (!y) return 1;
+	int a[3];
+	for (a[2] = 0; a[2] < v[2]; a[2]++)
+		for (a[1] = 0; a[1] < v[1]; a[1]++)
+			for (a[0] = 0; a[0] < v[0]; a[0]++) {
+				int c[3];
+				for (int k = 0; k < 3; k++) c[ax[k]] = a[k];
+				y[((size_t)a[2] * v[1] + a[1]) * v[0] + a[0]] =
+					x->v[((size_t)c[2] * u[1] + c[1]) * u[0] + c[0]];
+			}
+	free(x->v);
+	x->v = y;
+	x->pd = v[0];
+	x->w = v[1];
+	x->h = v[2];
+	return 0;
+}
+
+/* The value of a sample outside the old image after a trim: NaN for float
+ * samples, the bits of a float (double) NaN for 4-byte (8-byte) integer
+ * samples, 0 for narrower ones (iio.c:832-870). */
+static double pad_value(int type)
+{
+	switch (type) {
+	case T_F32: case T_F64: return NAN;
+	case T_I32: case T_U32: return 2143289344.0;            /* 0x7fc00000 */
+	case T_I64: case T_U64: return 9221120237041090560.0;   /* 0x7ff8000000000000 */
+	default: return 0;
+	}
+}
+
+/* Remove `left` columns on the left, `right` on the right, `top` rows at the
+ * top and `bottom` at the bottom; negative counts add padding. */
+static int trim(raw_image *x, int left, int bottom, int right, int top)
+{
+	const int nw = x->w - left - right, nh = x->h - bottom - top, pd = x->pd;
+	if (nw <= 0 || nh <= 0) {
+		fprintf(stderr, "imageio: trim of a %dx%d image to %dx%d\n", x->w, x->h, nw, nh);
+		return 1;
+	}
+	double *y = xcalloc((size_t)nw * nh * pd, sizeof(double));
+	if (!y) return 1;
+	const double pad = pad_value(x->type);
+	for (int j = 0; j < nh; j++)
+		for (int i = 0; i < nw; i++) {
+			const int si = i + left, sj = j + top;
+			const int in = si >= 0 && sj >= 0 && si < x->w && sj < x->h;
+			for (int l = 0; l < pd; l++)
+				y[((size_t)j * nw + i) * pd + l] = in ? x->v[((size_t)sj * x->w + si) * pd + l] : pad;
+		}
+	free(x->v);
+	x->v = y;
+	x->w = nw;
+	x->h = nh;
+	return 0;
+}
+
+static int flip(raw_image *x, const char *s)
+{
+	int r = 0;
+	if (!strcmp(s, "leftright")) flip_leftright(x);
+	if (!strcmp(s, "topdown")) flip_topdown(x);
+	if (!strcmp(s, "transpose")) r |= transpose(x);
+	if (!strcmp(s, "r270")) r |= reorient(x, 'y', 'X');
+	if (!strcmp(s, "r90")) r |= reorient(x, 'Y', 'x');
+	if (!strcmp(s, "r180")) r |= reorient(x, 'X', 'Y');
+	if (!strcmp(s, "posetrans")) r |= reorient(x, 'Y', 'X');
+	if (strlen(s) == 2) r |= reorient(x, s[0], s[1]);
+	if (strlen(s) == 3 && tolower(s[0]) + tolower(s[1]) + tolower(s[2]) == 3 * 'y') r |= reorient3d(x, s);
+	return r;
+}
+
+static int read_core(const char *name, raw_image *x);
+
+/* Filter the image through a shell command: the image goes to the command's
+ * standard input as a file, its standard output is read back as the image,
+ * IIO_TRANS unset for it (iio.c:3826-3852); a command that fails leaves the
+ * image as it was. */
+static int pipe_through(raw_image *x, const char *cmd)
+{
+	char in[] = "/tmp/imageio_in_XXXXXX", out[] = "/tmp/imageio_out_XXXXXX";
+	int fi = mkstemp(in);
+	if (fi < 0) return 1;
+	close(fi);
+	int fo = mkstemp(out);
+	if (fo < 0) { unlink(in); return 1; }
+	close(fo);
+	size_t np = (size_t)x->w * x->h;
+	float *pl = xcalloc(np * x->pd, sizeof(float));
+	int r = !pl;
+	if (pl) {
+		for (size_t i = 0; i < np; i++)
+			for (int l = 0; l < x->pd; l++) pl[np * l + i] = (float)x->v[i * x->pd + l];
+		r = imgio_write_split(in, pl, x->w, x->h, x->pd);
+		free(pl);
+	}
+	if (!r) {
+		size_t len = strlen(cmd) + strlen(in) + strlen(out) + 32;
+		char *c = malloc(len);
+		if (!c) r = 1;
+		else {
+			snprintf(c, len, "(unset IIO_TRANS; %s) <%s >%s", cmd, in, out);
+			if (!system(c)) {
+				raw_image y = {0};
+				r = read_core(out, &y);
+				if (!r) {
+					free(x->v);
+					*x = y;
+				} else {
+					free(y.v);
+				}
+			}
+			free(c);
+		}
+	}
+	unlink(in);
+	unlink(out);
+	return r;
+}
+
+/* Apply iio's list of transformations "op=value,op=value,..." (up to the
+ * first ']') in order (iio.c:3854-3884): flip=leftright|topdown|transpose|
+ * r90|r180|r270|posetrans|<two letters>|<three axes>, pipe=<command>, and
+ * the trims x=V (drop V columns on the left), y=V (V rows at the top), w=V
+ * (keep V columns), h=V (keep V rows).  Unknown operations are ignored. */
+static int trans_apply(raw_image *x, const char *list)
+{
+	size_t n = strcspn(list, "]");
+	char *t = malloc(n + 1);
+	if (!t) return 1;
+	memcpy(t, list, n);
+	t[n] = 0;
+	int r = 0;
+	for (char *tok = t; tok && !r;) {
+		char *next = strchr(tok, ',');
+		if (next) *next++ = 0;
+		char *eq = strchr(tok, '=');
+		if (eq && eq != tok && eq[1]) {
+			*eq = 0;
+			const char *o = tok, *v = eq + 1;
+			const int V = atoi(v), w = x->w, h = x->h;
+			if (!strcmp(o, "flip")) r = flip(x, v);
+			else if (!strcmp(o, "pipe")) r = pipe_through(x, v);
+			else if (!strcmp(o, "x")) r = trim(x, V, 0, 0, 0);
+			else if (!strcmp(o, "y")) r = trim(x, 0, 0, 0, V);
+			else if (!strcmp(o, "w")) r = trim(x, 0, 0, w - V, 0);
+			else if (!strcmp(o, "h")) r = trim(x, 0, h - V, 0, 0);
+		}
+		tok = next;
+	}
+	free(t);
+	return r;
+}
+
+/* "TRANS[list]:name" (iio.c:3796-3808): the colon after the closing bracket */
+static const char *trans_prefix(const char *name)
+{
+	if (name != strstr(name, "TRANS[")) return NULL;
+	const char *colon = strchr(name, ':');
+	return colon && colon[-1] == ']' ? colon : NULL;
+}
+
+/* A named image: semantic names as they are; "TRANS[list]:name" reads name
+ * and applies the list; then every image read from a file gets the list in
+ * IIO_TRANS, when set (iio.c:5587-5705). */
 static int read_raw(const char *name, raw_image *x)
 {
 	int rc;
 	if (semantic_name(name, x, &rc)) return rc;
+	const char *colon = trans_prefix(name);
+	if (colon) {
+		rc = read_raw(colon + 1, x);
+		if (!rc) rc = trans_apply(x, name + 6);
+	} else {
+		rc = read_core(name, x);
+	}
+	const char *env = getenv("IIO_TRANS");
+	if (!rc && env && *env) rc = trans_apply(x, env);
+	if (rc && colon) fprintf(stderr, "imageio: could not read image \"%s\"\n", name);
+	return rc;
+}
+
+/* An image from a file or stdin, its format sniffed from the first bytes. */
+static int read_core(const char *name, raw_image *x)
+{
 	FILE *f = strcmp(name, "-") ? fopen(name, "rb") : stdin;
 	if (!f) {
 		fprintf(stderr, "imageio: can not open file \"%s\" in mode \"r\"\n", name);

@@ -5,6 +5,10 @@
  *  - images are returned "split": planar float, x[w*h*l + w*j + i];
  *  - "-" names stdin (reading) or stdout (writing); iio's semantic names
  *    "zero:WxH[,pd]", "one:WxH[,pd]" and "constant:V:WxH" read as images;
+ *  - every image read from a file (not a semantic name) gets the list of
+ *    transformations in IIO_TRANS, and a name "TRANS[list]:file" gets that
+ *    list as well (iio.c:3796-3884, 5677-5705): flips and reorientations,
+ *    trims (negative ones pad with NaN), a pipe through a shell command;
  *  - the input format is sniffed from the first bytes: NumPy .npy (1.0,
  *    every numeric dtype), PFM ("Pf"/"PF"), PNM ("P2","P3","P5","P6") and the
  *    ASC text format ("w h 1 pd" header, planar samples);

@@ -1107,6 +1107,17 @@ bool verbose()
 	return v;
 }
 
+// Programmatic dependent launches between the fused V-cycle kernels (on by
+// default; SIMPOIS_NO_PDL=1 launches them plainly).  Results are the same.
+bool pdl_enabled()
+{
+	static bool v = [] {
+		const char *e = getenv("SIMPOIS_NO_PDL");
+		return !(e && atoi(e) > 0);
+	}();
+	return v;
+}
+
 // Hand-over size of the fused V-cycle: levels with max(w, h) <= it run in
 // k_coarse5 (one block per problem), wider levels in the tile kernels.
 // Level 0 of a problem of at most SMALL_MAX x SMALL_MAX always runs in
@@ -1288,6 +1299,15 @@ constexpr CellTable make_cell_table()
 }
 
 __device__ const CellTable g_cells = make_cell_table();
+
+// Programmatic dependent launch.  A kernel launched with programmatic stream
+// serialisation may be scheduled while the kernel before it drains; it calls
+// grid_wait() before its first access to anything an earlier kernel wrote
+// (and before any early return, so that its own completion still implies the
+// completion of every kernel before it), and grid_release() to let the next
+// kernel be scheduled.  Without the launch attribute both are no-ops.
+__device__ __forceinline__ void grid_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 static_assert(FH % 2 == 0, "x0 + y0 must stay even for the cell table");
 
 __device__ __forceinline__ void own_cells(int x0, int y0, int cells[2][4])
@@ -1334,6 +1354,8 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 	__shared__ double sh[32];
 	__shared__ uint64_t bar;
 	const int4 t = tl[blockIdx.x];
+	grid_wait();
+	grid_release();
 	const int prob = t.x;
 	const ProbDev &pr = P[prob];
 	if (!st[prob].inner_active || l >= pr.nfine) return;
@@ -1516,6 +1538,8 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_post5(const ProbDev *__restri
 	__shared__ __align__(16) uint8_t sc[FN];
 	__shared__ double sh[32];
 	const int4 t = tl[blockIdx.x];
+	grid_wait();
+	grid_release();
 	const int prob = t.x;
 	const ProbDev &pr = P[prob];
 	if (!st[prob].inner_active || l >= pr.nfine) return;
@@ -1757,6 +1781,8 @@ __global__ void __launch_bounds__(1024, 1) k_coarse5(const ProbDev *__restrict__
 	__shared__ uint8_t *s_M[MAXLEV];
 	__shared__ const uint8_t *s_gm[MAXLEV];
 	const int prob = blockIdx.x;
+	grid_wait();
+	grid_release();
 	if (!st[prob].inner_active) return;
 	const ProbDev &pr = P[prob];
 	const int c0 = pr.nfine, L = pr.nlev;
@@ -1926,6 +1952,8 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_spmv5(const ProbDev *__restri
 	__shared__ float2 spq[SP_TILE * SP_TILE];   // (p, q) of the unknown tile cells
 	__shared__ double sh[32];
 	const int4 t = tl[blockIdx.x];
+	grid_wait();
+	grid_release();
 	const int prob = t.x;
 	if (!st[prob].inner_active) return;
 	const ProbDev &pr = P[prob];
@@ -2363,7 +2391,30 @@ struct Plan {
 	// device-driven solve: the loop counters are read back with the final
 	// states (one synchronisation); the launch count is completed then
 	const Globals *hg = nullptr;
+	int pdl = 0;   // programmatic dependent launches between the V-cycle kernels
 };
+
+// Launch with programmatic stream serialisation when pdl is set (the kernel
+// must call grid_wait() before its dependent accesses), else a plain launch.
+template <typename... P, typename... A>
+void launch_k(int pdl, void (*k)(P...), int grid, int block, size_t smem, cudaStream_t s, A... args)
+{
+	if (!pdl) {
+		k<<<grid, block, smem, s>>>(args...);
+		return;
+	}
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = dim3(grid);
+	cfg.blockDim = dim3(block);
+	cfg.dynamicSmemBytes = smem;
+	cfg.stream = s;
+	cudaLaunchAttribute at[1];
+	at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	at[0].val.programmaticStreamSerializationAllowed = 1;
+	cfg.attrs = at;
+	cfg.numAttrs = 1;
+	cudaLaunchKernelEx(&cfg, k, args...);
+}
 
 // Kernel timer: an event pair around each launch of the main-loop kernels,
 // with the launch's algorithmic bytes counted over the active tiles of the
@@ -2518,20 +2569,22 @@ void launch_vcycle_fused(const Plan &pl, cudaStream_t s, int pcg = 1, int use_p2
 	for (int l = 0; l < pl.nfine_max; l++) {
 		if (!pl.nact[l]) continue;
 		KT_BEGIN(pl, s);
-		k_pre5<<<pl.nact[l], SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[l], l, pl.tbeg, pl.tcnt, pl.partial,
-				pl.gl, use_p2); ++*pl.nl;
+		launch_k(pl.pdl, k_pre5, pl.nact[l], SP_THREADS, 0, s, pl.dp, pl.dst, (const int4 *)pl.act[l], l,
+				(const int *)pl.tbeg, (const int *)pl.tcnt, pl.partial, pl.gl, use_p2); ++*pl.nl;
 		KT_END(pl, s, "k_pre5", pl.kt->px(l) * (BPX_PRE5 + (l == 0 && step ? BPX_STEP : 0.0)));
 	}
 	{
 		KT_BEGIN(pl, s);
-		k_coarse5<<<pl.n, 1024, pl.coarse_smem, s>>>(pl.dp, pl.dst, pl.gl, pcg, use_p2); ++*pl.nl;
+		launch_k(pl.pdl, k_coarse5, pl.n, 1024, pl.coarse_smem, s, (const ProbDev *)pl.dp, pl.dst, pl.gl, pcg,
+				use_p2); ++*pl.nl;
 		KT_END(pl, s, "k_coarse5", pl.kt->cells() * BPC_COARSE5);
 	}
 	for (int l = pl.nfine_max - 1; l >= 0; l--) {
 		if (!pl.nact[l]) continue;
 		KT_BEGIN(pl, s);
-		k_post5<<<pl.nact[l], SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[l], l, pl.tbeg, pl.tcnt, pl.partial,
-				pl.gl, pcg); ++*pl.nl;
+		launch_k(pl.pdl, k_post5, pl.nact[l], SP_THREADS, 0, s, (const ProbDev *)pl.dp, pl.dst,
+				(const int4 *)pl.act[l], l, (const int *)pl.tbeg, (const int *)pl.tcnt, pl.partial, pl.gl, pcg);
+		++*pl.nl;
 		KT_END(pl, s, "k_post5", pl.kt->px(l) * BPX_POST5);
 	}
 }
@@ -2572,7 +2625,9 @@ void launch_iteration_fused(const Plan &pl, cudaStream_t s)
 		kt_refresh(pl, s);
 		{
 			KT_BEGIN(pl, s);
-			k_spmv5<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl,
+			// the first launch of the loop body follows no kernel of the body
+			launch_k(parity ? pl.pdl : 0, k_spmv5, nt, SP_THREADS, 0, s, (const ProbDev *)pl.dp, pl.dst,
+					(const int4 *)pl.act[0], (const int *)pl.tbeg, (const int *)pl.tcnt, pl.partial, pl.gl,
 					parity); ++*pl.nl;
 			KT_END(pl, s, "k_spmv5", pl.kt->px(0) * BPX_SPMV5);
 		}
@@ -2587,8 +2642,8 @@ std::string plan_signature(const simpois_ctx *ctx, const Plan &pl, int K, int fu
 {
 	std::string sig;
 	char buf[96];
-	snprintf(buf, sizeof buf, "%p/%d/%d/%d/%d/%d/%d/%d|", (void *)ctx->arena, pl.n, K, (int)fused, pl.nfine_max,
-			pl.nlev_max, pl.coarse_smem, opt.use_mg);
+	snprintf(buf, sizeof buf, "%p/%d/%d/%d/%d/%d/%d/%d/%d|", (void *)ctx->arena, pl.n, K, (int)fused,
+			pl.nfine_max, pl.nlev_max, pl.coarse_smem, opt.use_mg, pl.pdl);
 	sig += buf;
 	snprintf(buf, sizeof buf, "%p/%p/%p/%p/%p/%p|", (void *)pl.dp, (void *)pl.dst, (void *)pl.gl, (void *)pl.tbeg,
 			(void *)pl.tcnt, (void *)pl.partial);
@@ -2723,6 +2778,7 @@ int run_kind(simpois_ctx *ctx, Plan &pl, const MgOptions &opt)
 	// the squared 5-point V-cycle; MODE_PLAIN: per-sweep kernels (or no MG)
 	const int mode = !opt.use_mg || !pl.fused ? MODE_PLAIN : (K == 0 ? MODE_FUSED5 : MODE_BIH64);
 	const bool fused = mode == MODE_FUSED5;
+	pl.pdl = !pl.kt && pdl_enabled();
 	if (opt.use_graph && !pl.kt && !verbose()) {
 		bool done = false;
 		int r = run_device_loop<K>(ctx, pl, opt, mode, &done);

@@ -14,6 +14,8 @@ environment the reference ran with, and its planar output ``out``.
 * ``conv_*``  single-channel cases run to convergence with the reference
               recipe ``CG_EPS=rtol*||b|| simpois -s 1 -c -1`` (rtol 1e-7); the
               GPU solver must agree within 1e-4 relative max-abs.
+* ``trans.json`` iio's transformations on reading (IIO_TRANS, TRANS[...]:)
+              applied by the reference command to an all-known image.
 * ``amle_*``  the reference ``amle`` (src/amle.c) on one channel: neighbourhood
               sizes (AMLE_NN), iteration counts (AMLE_NITER), a mask file, an
               AMLE_INIT start image, all-known, all-NaN and 1-pixel images.
@@ -218,6 +220,43 @@ def io_cases():
     return len(res)
 
 
+TRANS_LISTS = ["flip=leftright", "flip=topdown", "flip=transpose", "flip=r90", "flip=r180", "flip=r270",
+               "flip=posetrans", "flip=Xy", "flip=yX", "flip=YX", "flip=xyz", "flip=yxz", "flip=zxy", "flip=zyx",
+               "flip=xzy", "flip=yzx", "x=2", "y=1", "w=4", "h=3", "x=1,y=1,w=3,h=2", "x=-2", "y=-1,h=7",
+               "flip=leftright,x=2,flip=transpose", "w=9", "pipe=cat", "bogus=3,flip=nothing"]
+
+
+def trans_cases():
+    """iio's transformations on reading (IIO_TRANS and the TRANS[...]:
+    prefix): an all-known image read by the reference command under each
+    list, with nothing to fill, written as npy (tests/golden/trans.json)."""
+    import subprocess
+    import tempfile
+    rng = np.random.default_rng(99)
+    img = (rng.random((5, 7, 3)) * 100).astype(np.float32)
+    res = {"in": img.ravel().tolist(), "shape": list(img.shape), "env": {}, "prefix": {}}
+    with tempfile.TemporaryDirectory() as td:
+        src = os.path.join(td, "in.npy")
+        np.save(src, img)
+        o = os.path.join(td, "o.npy")
+        e0 = {k: v for k, v in os.environ.items() if k not in ("PMSFAC", "PONLIT", "CG_EPS", "IIO_TRANS")}
+        for lst in TRANS_LISTS:
+            subprocess.run([O.REF_BIN, "-i", src, "-n", "0", "-o", o], env=dict(e0, IIO_TRANS=lst), check=True,
+                           capture_output=True)
+            a = np.load(o)
+            res["env"][lst] = {"shape": list(a.shape), "out": a.ravel().tolist()}
+        # the prefix, alone and together with IIO_TRANS (applied inside and outside)
+        for lst, env in (("flip=topdown", ""), ("x=1,w=5", ""), ("flip=leftright", "flip=transpose")):
+            ee = dict(e0, IIO_TRANS=env) if env else e0
+            subprocess.run([O.REF_BIN, "-i", f"TRANS[{lst}]:{src}", "-n", "0", "-o", o], env=ee, check=True,
+                           capture_output=True)
+            a = np.load(o)
+            res["prefix"][f"{lst}|{env}"] = {"shape": list(a.shape), "out": a.ravel().tolist()}
+    with open(os.path.join(OUT, "trans.json"), "w") as fh:
+        json.dump(res, fh)
+    return len(res["env"]) + len(res["prefix"])
+
+
 def mini_cases(rng):
     """The GS-only copy of the ftr viewers (ftr/minisimpois.c) from its own main."""
     k = 0
@@ -305,6 +344,9 @@ def amle_cli_cases():
 def main():
     if not O.have_reference():
         O.build(reference=True)
+    if sys.argv[1:] == ["trans"]:
+        print(f"wrote {trans_cases()} transformation cases into {OUT}")
+        return
     if sys.argv[1:] == ["amle"]:
         n = amle_cases(np.random.default_rng(5150))
         print(f"wrote {n} AMLE cases and {amle_cli_cases()} AMLE command cases into {OUT}")
@@ -316,8 +358,9 @@ def main():
     n4 = io_cases()
     n5 = mini_cases(np.random.default_rng(4242))
     n6 = amle_cases(np.random.default_rng(5150)) + amle_cli_cases()
+    n7 = trans_cases()
     print(f"wrote {n1} pin cases, {n2} converged cases, {n3} CLI cases, {n4} I/O cases, "
-          f"{n5} minisimpois cases and {n6} AMLE cases into {OUT}")
+          f"{n5} minisimpois cases, {n6} AMLE cases and {n7} transformation cases into {OUT}")
 
 
 if __name__ == "__main__":

@@ -206,3 +206,64 @@ def test_semantic_image_names(harness, tmp_path, name, shape, value):
 def test_bad_semantic_name_fails(harness, tmp_path):
     r = subprocess.run([harness, "read", "zero:axb", str(tmp_path / "o.npy")], capture_output=True, text=True)
     assert r.returncode != 0 and "bad semantical name" in r.stderr
+
+
+# iio's transformations on reading (iio.c:3796-3884, 5677-5705); the
+# reference command filled the cells a negative trim pads (NaN here), so those
+# are compared by position only
+_PADDED = {"x=-2": 30, "y=-1,h=7": 42, "w=9": 30}
+
+
+def _read_with(harness, tmp_path, name, env_list):
+    dst = str(tmp_path / "o.npy")
+    env = {k: v for k, v in os.environ.items() if k != "IIO_TRANS"}
+    if env_list:
+        env["IIO_TRANS"] = env_list
+    subprocess.run([harness, "read", name, dst], check=True, env=env)
+    return np.load(dst)
+
+
+def _trans_src(tmp_path):
+    d = _fixtures("trans.json")
+    src = str(tmp_path / "in.npy")
+    np.save(src, np.array(d["in"], np.float32).reshape(d["shape"]))
+    return d, src
+
+
+def _same_where_known(got, want, padded):
+    nan = np.isnan(got)
+    assert int(nan.sum()) == padded
+    assert np.array_equal(got[~nan], want[~nan])
+
+
+@pytest.mark.parametrize("lst", json.load(open(os.path.join(GOLDEN, "trans.json")))["env"].keys())
+def test_iio_trans_matches_reference(harness, tmp_path, lst):
+    d, src = _trans_src(tmp_path)
+    want = d["env"][lst]
+    got = _read_with(harness, tmp_path, src, lst)
+    assert list(got.shape) == want["shape"]
+    _same_where_known(got, np.array(want["out"], np.float32).reshape(want["shape"]), _PADDED.get(lst, 0))
+
+
+@pytest.mark.parametrize("key", json.load(open(os.path.join(GOLDEN, "trans.json")))["prefix"].keys())
+def test_trans_prefix_matches_reference(harness, tmp_path, key):
+    """TRANS[list]:name, alone and with IIO_TRANS (applied to the inner read
+    and again to the outer one)."""
+    d, src = _trans_src(tmp_path)
+    lst, env = key.split("|")
+    want = d["prefix"][key]
+    got = _read_with(harness, tmp_path, f"TRANS[{lst}]:{src}", env)
+    assert list(got.shape) == want["shape"]
+    assert np.array_equal(got, np.array(want["out"], np.float32).reshape(want["shape"]))
+
+
+def test_iio_trans_errors(harness, tmp_path):
+    _, src = _trans_src(tmp_path)
+    for lst in ("flip=XYZ", "x=7", "h=0"):
+        env = dict(os.environ, IIO_TRANS=lst)
+        r = subprocess.run([harness, "read", src, str(tmp_path / "o.npy")], capture_output=True, text=True, env=env)
+        assert r.returncode != 0, lst
+    # a failing pipe leaves the image as it was
+    got = _read_with(harness, tmp_path, src, "pipe=false")
+    d = _fixtures("trans.json")
+    assert np.array_equal(got, np.array(d["in"], np.float32).reshape(d["shape"]))
