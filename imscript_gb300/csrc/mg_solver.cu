@@ -1318,7 +1318,10 @@ __device__ __forceinline__ void own_cells(int x0, int y0, int cells[2][4])
 		for (int k = 0; k < 4; k++) cells[col][k] = g_cells.v[col][k][threadIdx.x];
 }
 
-// Half-sweep of colour col over the cells with ring >= lo.
+// Half-sweep of colour col over the cells with ring >= lo.  In the first
+// half-sweep from z = 0 (zero set) every neighbour is 0: the off-diagonal sum
+// is +0 and b - (+0) is b, so z = b / diag gives the same float.
+template <bool zero = false>
 __device__ __forceinline__ void sweep_cells(float *sz, const float *sb, const uint8_t *sc, const int cells[2][4],
 		int col, int lo)
 {
@@ -1329,8 +1332,12 @@ __device__ __forceinline__ void sweep_cells(float *sz, const float *sb, const ui
 		const int c = e & 2047;
 		const int code = sc[c];
 		if (!(code & 1)) continue;
-		const float off = off_code(sz, c, FR, code);
-		sz[c] = gs_div(sb[c] - off, diag_code(code));
+		if (zero) {
+			sz[c] = gs_div(sb[c], diag_code(code));
+		} else {
+			const float off = off_code(sz, c, FR, code);
+			sz[c] = gs_div(sb[c] - off, diag_code(code));
+		}
 	}
 }
 
@@ -1364,6 +1371,10 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 	const float a = upd ? (float)st[prob].alpha : 0.f;
 	const float *qv = pr.q;
 	const int x0 = t.y * SP_TILE - FH, y0 = t.z * SP_TILE - FH;
+	// the coarse cell this thread restricts to (16 x 16 per tile); its mask is
+	// loaded now, with the region, not after the sweeps
+	const int ci = t.y * (SP_TILE / 2) + (threadIdx.x & 15), cj = t.z * (SP_TILE / 2) + (threadIdx.x >> 4);
+	const bool cun = ci < C.w && cj < C.h && C.mask[(size_t)cj * C.w + ci];
 	// every load depends only on the coordinates, so all are in flight at once
 	if (L.tmb) {
 		// TMA: b as a 40 x 40 box at (x0, y0) straight into sb, the codes as a
@@ -1481,7 +1492,9 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 	__syncthreads();
 	// half-sweep s updates colour s&1 on the cells of ring >= s; at s = 0 every
 	// neighbour is 0, so the outermost ring needs no outside value
-	for (int s = 0; s < 2 * NU5; s++) {
+	sweep_cells<true>(sz, sb, sc, cells, 0, 0);
+	__syncthreads();
+	for (int s = 1; s < 2 * NU5; s++) {
 		sweep_cells(sz, sb, sc, cells, s & 1, s);
 		__syncthreads();
 	}
@@ -1490,9 +1503,8 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 		const Grp g = grp_of(t, L.w, L.h);
 		if (g.n) st4(L.z, g, sz + ((threadIdx.x >> 3) + FH) * FR + 4 * (threadIdx.x & 7) + FH);
 	}
-	// restriction: one coarse cell per thread (16 x 16 per tile)
-	const int ci = t.y * (SP_TILE / 2) + (threadIdx.x & 15), cj = t.z * (SP_TILE / 2) + (threadIdx.x >> 4);
-	if (ci < C.w && cj < C.h && C.mask[(size_t)cj * C.w + ci]) {
+	// restriction: one coarse cell per thread
+	if (cun) {
 		float acc = 0.f;
 		for (int bb = 0; bb < 2; bb++)
 			for (int aa = 0; aa < 2; aa++) {
