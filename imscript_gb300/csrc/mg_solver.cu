@@ -1300,6 +1300,19 @@ constexpr CellTable make_cell_table()
 
 __device__ const CellTable g_cells = make_cell_table();
 
+// Make the values a kernel's early-return test and its first region loads
+// need be loaded together, before the test, rather than each after the one
+// before it (one global round trip instead of several): an empty volatile asm
+// that takes them all as inputs stands before the test.
+__device__ __forceinline__ void touch(int v) { asm volatile("" ::"r"(v)); }
+__device__ __forceinline__ void touch(double v) { asm volatile("" ::"d"(v)); }
+__device__ __forceinline__ void touch(const void *v) { asm volatile("" ::"l"(v)); }
+template <typename... T>
+__device__ __forceinline__ void together(const T &...v)
+{
+	(touch(v), ...);
+}
+
 // Programmatic dependent launch.  A kernel launched with programmatic stream
 // serialisation may be scheduled while the kernel before it drains; it calls
 // grid_wait() before its first access to anything an earlier kernel wrote
@@ -1365,10 +1378,15 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 	grid_release();
 	const int prob = t.x;
 	const ProbDev &pr = P[prob];
-	if (!st[prob].inner_active || l >= pr.nfine) return;
+	// the problem's state and level table in one round trip (l + 1 < MAXLEV)
+	const int active = st[prob].inner_active, nf = pr.nfine, pending = st[prob].pending;
+	const double alpha = st[prob].alpha;
 	const LevelDev L = pr.lv[l], C = pr.lv[l + 1];
-	const bool upd = l == 0 && st[prob].pending;
-	const float a = upd ? (float)st[prob].alpha : 0.f;
+	together(active, nf, pending, alpha, L.w, L.h, L.b, L.code, L.z, L.tmb, L.tmc, L.mask, C.w, C.h, C.mask, C.b, pr.q,
+			pr.x, pr.xlo, pr.p, pr.p2, pr.b_alt);
+	if (!active || l >= nf) return;
+	const bool upd = l == 0 && pending;
+	const float a = upd ? (float)alpha : 0.f;
 	const float *qv = pr.q;
 	const int x0 = t.y * SP_TILE - FH, y0 = t.z * SP_TILE - FH;
 	// the coarse cell this thread restricts to (16 x 16 per tile); its mask is
@@ -1554,8 +1572,10 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_post5(const ProbDev *__restri
 	grid_release();
 	const int prob = t.x;
 	const ProbDev &pr = P[prob];
-	if (!st[prob].inner_active || l >= pr.nfine) return;
+	const int active = st[prob].inner_active, nf = pr.nfine;
 	const LevelDev L = pr.lv[l], C = pr.lv[l + 1];
+	together(active, nf, L.w, L.h, L.code, L.b, L.z, L.z2, C.w, C.mask, C.z2);
+	if (!active || l >= nf) return;
 	const int x0 = t.y * SP_TILE - FH, y0 = t.z * SP_TILE - FH;
 	if ((L.w & 3) == 0) {
 		// groups of 4 cells of a row: with w % 4 == 0 (and x0 % 4 == 0) a group
@@ -1967,10 +1987,13 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_spmv5(const ProbDev *__restri
 	grid_wait();
 	grid_release();
 	const int prob = t.x;
-	if (!st[prob].inner_active) return;
 	const ProbDev &pr = P[prob];
+	const int active = st[prob].inner_active;
+	const double beta64 = st[prob].beta;
 	const LevelDev L = pr.lv[0];
-	const float beta = (float)st[prob].beta;
+	together(active, beta64, L.w, L.h, L.code, L.z2, pr.p, pr.p2, pr.q);
+	if (!active) return;
+	const float beta = (float)beta64;
 	const float *pold = new_is_p2 ? pr.p : pr.p2;
 	float *pnew = new_is_p2 ? pr.p2 : pr.p;
 	FF pq = {0.f, 0.f};
