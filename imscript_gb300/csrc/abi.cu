@@ -373,6 +373,9 @@ int simpois_destroy(simpois_ctx *ctx)
 	if (ctx->io) cudaFree(ctx->io);
 	if (ctx->pinned) cudaFreeHost(ctx->pinned);
 	if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
+	if (ctx->aux_stream) cudaStreamDestroy(ctx->aux_stream);
+	if (ctx->ev_in) cudaEventDestroy(ctx->ev_in);
+	if (ctx->ev_out) cudaEventDestroy(ctx->ev_out);
 	for (cudaEvent_t e : ctx->evpool) cudaEventDestroy(e);
 	if (ctx->solve_exec) cudaGraphExecDestroy(ctx->solve_exec);
 	if (ctx->amle_exec) cudaGraphExecDestroy(ctx->amle_exec);
@@ -405,6 +408,58 @@ int simpois_solve_device(simpois_ctx *ctx, float *out, const float *in, const fl
 	return st;
 }
 
+// ---------------------------------------------- host entry point: direct I/O
+//
+// The converged schedule reads the data term f only at the unknowns, and the
+// output equals the input g at every known pixel.  With page-locked host
+// buffers the host entry point therefore moves, besides g itself, only the
+// 4-pixel groups of f and of the output that hold an unknown (read and
+// written in place by a kernel), and sends the output's known pixels back
+// while the solve runs (the host link is idle then).
+
+__global__ void k_fetch_rhs(const float4 *__restrict__ g, const float4 *__restrict__ hf, float4 *__restrict__ f,
+		size_t n4)
+{
+	for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
+		const float4 v = g[i];
+		const bool u = isnan(v.x) || isnan(v.y) || isnan(v.z) || isnan(v.w);
+		f[i] = u ? hf[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+	}
+}
+
+__global__ void k_put_unknowns(const float4 *__restrict__ g, const float4 *__restrict__ out,
+		float4 *__restrict__ hout, size_t n4)
+{
+	for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
+		const float4 v = g[i];
+		if (isnan(v.x) || isnan(v.y) || isnan(v.z) || isnan(v.w)) hout[i] = out[i];
+	}
+}
+
+// The device address of a page-locked host buffer, 16-byte aligned; null for
+// any other buffer.
+static void *direct_ptr(const void *p)
+{
+	if (!p || ((uintptr_t)p & 15)) return nullptr;
+	cudaPointerAttributes a;
+	if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+		cudaGetLastError();
+		return nullptr;
+	}
+	if (a.type != cudaMemoryTypeHost || !a.devicePointer || ((uintptr_t)a.devicePointer & 15)) return nullptr;
+	return a.devicePointer;
+}
+
+// SIMPOIS_NO_DIRECT_IO=1: the host entry point copies whole buffers
+static bool direct_io_enabled()
+{
+	static bool v = [] {
+		const char *e = getenv("SIMPOIS_NO_DIRECT_IO");
+		return !(e && atoi(e) > 0);
+	}();
+	return v;
+}
+
 int simpois_solve(simpois_ctx *ctx, float *out, const float *in, const float *dat, int w, int h, int pd,
 		const simpois_params *params, simpois_report *reports)
 {
@@ -420,11 +475,53 @@ int simpois_solve(simpois_ctx *ctx, float *out, const float *in, const float *da
 	float *din = (float *)ctx->io, *dout = (float *)(ctx->io + slot);
 	float *ddat = dat ? (float *)(ctx->io + 2 * slot) : nullptr;
 	cudaStream_t s = ctx->stream;
+	const bool converged = params && params->rtol > 0;   // the default is the reference schedule
+	float4 *hout = nullptr;
+	const float4 *hdat = nullptr;
+	if (converged && n % 4 == 0 && direct_io_enabled()) {
+		hout = (float4 *)direct_ptr(out);
+		hdat = dat ? (const float4 *)direct_ptr(dat) : nullptr;
+		if (dat && !hdat) hout = nullptr;
+	}
+	const bool direct = hout != nullptr;
+	if (direct && !ctx->aux_stream) {
+		SP_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking));
+		SP_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_in, cudaEventDisableTiming));
+		SP_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_out, cudaEventDisableTiming));
+	}
+	const int grid = 8 * (ctx->sm_count > 0 ? ctx->sm_count : 1);
 	SP_CUDA(ctx, cudaMemcpyAsync(din, in, bytes, cudaMemcpyHostToDevice, s));
-	if (dat) SP_CUDA(ctx, cudaMemcpyAsync(ddat, dat, bytes, cudaMemcpyHostToDevice, s));
+	if (direct) {
+		// the known pixels of the output are those of g: back while the solve runs
+		SP_CUDA(ctx, cudaEventRecord(ctx->ev_in, s));
+		SP_CUDA(ctx, cudaStreamWaitEvent(ctx->aux_stream, ctx->ev_in, 0));
+		SP_CUDA(ctx, cudaMemcpyAsync(out, din, bytes, cudaMemcpyDeviceToHost, ctx->aux_stream));
+		SP_CUDA(ctx, cudaEventRecord(ctx->ev_out, ctx->aux_stream));
+		if (dat) {
+			k_fetch_rhs<<<grid, 256, 0, s>>>((const float4 *)din, hdat, (float4 *)ddat, n / 4);
+			ctx->launches++;
+			const cudaError_t e = cudaGetLastError();
+			if (e != cudaSuccess) {
+				cudaStreamSynchronize(ctx->aux_stream);
+				return ctx_fail(ctx, SIMPOIS_ECUDA, "k_fetch_rhs: %s", cudaGetErrorString(e));
+			}
+		}
+	} else if (dat) {
+		SP_CUDA(ctx, cudaMemcpyAsync(ddat, dat, bytes, cudaMemcpyHostToDevice, s));
+	}
 	int st = simpois_solve_device(ctx, dout, din, ddat, w, h, pd, params, reports);
-	if (st != SIMPOIS_OK && st != SIMPOIS_NOT_CONVERGED && st != SIMPOIS_BREAKDOWN) return st;
-	SP_CUDA(ctx, cudaMemcpyAsync(out, dout, bytes, cudaMemcpyDeviceToHost, s));
+	if (st != SIMPOIS_OK && st != SIMPOIS_NOT_CONVERGED && st != SIMPOIS_BREAKDOWN) {
+		if (direct) cudaStreamSynchronize(ctx->aux_stream);   // the caller may free out
+		return st;
+	}
+	if (direct) {
+		SP_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_out, 0));
+		k_put_unknowns<<<grid, 256, 0, s>>>((const float4 *)din, (const float4 *)dout, hout, n / 4);
+		ctx->launches++;
+		SP_CUDA(ctx, cudaGetLastError());
+	} else {
+		SP_CUDA(ctx, cudaMemcpyAsync(out, dout, bytes, cudaMemcpyDeviceToHost, s));
+	}
 	SP_CUDA(ctx, cudaStreamSynchronize(s));
 	return st;
 }

@@ -35,6 +35,10 @@ struct simpois_ctx {
 	// staging for the host-pointer entry point
 	char *io = nullptr;
 	size_t io_cap = 0;
+	// its second stream (the output's known pixels go back while the solve
+	// runs) and the events that order it with `stream`
+	cudaStream_t aux_stream = nullptr;
+	cudaEvent_t ev_in = nullptr, ev_out = nullptr;
 
 	// kernel launches issued (graph replays count their kernel nodes)
 	long long launches = 0;

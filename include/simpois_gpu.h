@@ -131,7 +131,14 @@ const char *simpois_last_error(const simpois_ctx *ctx);
 
 /* Solve one planar w x h x pd image held in HOST memory (the work of
  * poisson_solver_separable, simpois.c:288-302).  dat may be NULL.  reports,
- * if not NULL, receives pd records.  Returns the worst channel status. */
+ * if not NULL, receives pd records.  Returns the worst channel status.
+ * With rtol > 0, w*h*pd a multiple of 4 and page-locked (cudaHostAlloc /
+ * cudaHostRegister), 16-byte aligned out and dat, the call moves only what
+ * the converged schedule needs: in whole; dat in the 4-pixel groups holding
+ * an unknown, read in place; out back whole while the solve runs (its known
+ * pixels are those of in), then its groups holding an unknown, written in
+ * place (SIMPOIS_NO_DIRECT_IO=1: whole-buffer copies).  On a failure status
+ * out may then hold the input. */
 int simpois_solve(simpois_ctx *ctx, float *out, const float *in,
 		const float *dat, int w, int h, int pd,
 		const simpois_params *params, simpois_report *reports);
