@@ -1148,32 +1148,6 @@ int handover_level(const int *lw, const int *lh, int nl, int cmax)
 	return nf;
 }
 
-// 5-point Gauss-Seidel update of region cell c (region side R), in place:
-// z = (b - off) / diag with off = -(sum of the unknown in-image neighbours),
-// the neighbours taken in split<0>'s order (E, W, S, N).
-__device__ __forceinline__ void gs5_cell(float *z, const float *b, const uint8_t *m, int c, int R,
-		int gi, int gj, int w, int h)
-{
-	float diag = 4.f, off = 0.f;
-	if (gi + 1 < w) { if (m[c + 1]) off -= z[c + 1]; } else diag -= 1.f;
-	if (gi > 0)     { if (m[c - 1]) off -= z[c - 1]; } else diag -= 1.f;
-	if (gj + 1 < h) { if (m[c + R]) off -= z[c + R]; } else diag -= 1.f;
-	if (gj > 0)     { if (m[c - R]) off -= z[c - R]; } else diag -= 1.f;
-	z[c] = gs_div(b[c] - off, diag);
-}
-
-// A z at region cell c, as split<0> then d*z + off
-__device__ __forceinline__ float az5_cell(const float *z, const uint8_t *m, int c, int R, int gi, int gj,
-		int w, int h)
-{
-	float diag = 4.f, off = 0.f;
-	if (gi + 1 < w) { if (m[c + 1]) off -= z[c + 1]; } else diag -= 1.f;
-	if (gi > 0)     { if (m[c - 1]) off -= z[c - 1]; } else diag -= 1.f;
-	if (gj + 1 < h) { if (m[c + R]) off -= z[c + R]; } else diag -= 1.f;
-	if (gj > 0)     { if (m[c - R]) off -= z[c - R]; } else diag -= 1.f;
-	return diag * z[c] + off;
-}
-
 // ------------------------------------------------------------------ TMA
 // Region loads of the tile kernels through the tensor memory accelerator: one
 // thread arms an mbarrier with the byte count and issues the 2-D tile copies;
@@ -1694,7 +1668,7 @@ __device__ __host__ inline CoarseLayout coarse_layout(const int *lw, const int *
 // One red-black half-sweep (colour) over a whole level held in shared memory;
 // the 1024 threads map to 32 x 32 (half-columns, rows) of the colour's cells.
 // The Gauss-Seidel update and A z of a cell from its cell code (the same
-// operations, in the same order, as gs5_cell and az5_cell).
+// operations, in the same order, as split<0>: E, W, S, N).
 __device__ __forceinline__ void gs5_code(float *z, const float *b, int code, int c, int w)
 {
 	z[c] = gs_div(b[c] - off_code(z, c, w, code), diag_code(code));
@@ -2496,7 +2470,6 @@ struct KTimer {
 constexpr double BPX_PRE5 = 1 + 4 + 4 + 0.25 + 1;         // mask, b, z; coarse mask, coarse b
 constexpr double BPX_POST5 = 1 + 4 + 4 + 1 + 0.25 + 4;    // mask, b, z, coarse z2, coarse mask; z2
 constexpr double BPX_SPMV5 = 1 + 4 + 4 + 4 + 4;           // mask, z2, p_old; p_new, q
-constexpr double BPX_XR = 1 + 4 + 4 + 4 + 4 + 4 + 4;      // mask, x, p, b, q; x, b
 constexpr double BPX_STEP = 4 + 4 + 4 + 4 + 4;            // k_pre5's PCG step: q, x, p; x, r
 constexpr double BPX_RESID64 = 1 + 8 + 4 + 4 + 4;         // mask, U, rhs; b, x
 constexpr double BPX_UADD = 1 + 8 + 4 + 8;                // mask, U, x; U
