@@ -1307,7 +1307,12 @@ __device__ __forceinline__ void own_cells(int x0, int y0, int cells[2][4])
 
 // Half-sweep of colour col over the cells with ring >= lo.  In the first
 // half-sweep from z = 0 (zero set) every neighbour is 0: the off-diagonal sum
-// is +0 and b - (+0) is b, so z = b / diag gives the same float.
+// is +0 and b - (+0) is b, so z = b / diag gives the same float.  In the
+// others (lo >= 1) every neighbour of an updated cell lies in the region, and
+// every neighbour off_code skips -- a known cell or one outside the image --
+// holds +0 in the region and is never written; x - (+0) is x for every float
+// (-0 and NaN included), so the four neighbours are subtracted without tests,
+// in off_code's order, with the same result.
 template <bool zero = false>
 __device__ __forceinline__ void sweep_cells(float *sz, const float *sb, const uint8_t *sc, const int cells[2][4],
 		int col, int lo)
@@ -1322,7 +1327,7 @@ __device__ __forceinline__ void sweep_cells(float *sz, const float *sb, const ui
 		if (zero) {
 			sz[c] = gs_div(sb[c], diag_code(code));
 		} else {
-			const float off = off_code(sz, c, FR, code);
+			const float off = (((0.f - sz[c + 1]) - sz[c - 1]) - sz[c + FR]) - sz[c - FR];
 			sz[c] = gs_div(sb[c] - off, diag_code(code));
 		}
 	}
