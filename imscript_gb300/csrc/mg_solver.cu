@@ -802,26 +802,43 @@ __global__ void k_spmv(const ProbDev *__restrict__ P, ProbState *st, const int4 
 	if (!st[prob].inner_active) return;
 	const ProbDev &pr = P[prob];
 	const LevelDev &L = pr.lv[0];
-	int i = tile_i(t);
 	FF pq = {0.f, 0.f};
-	for (int r = 0; r < SP_ROWS; r++) {
-		int j = tile_j(t, r);
-		if (i < pr.w && j < pr.h) {
-			size_t k = (size_t)j * pr.w + i;
+	if (K == 0 && (pr.w & 3) == 0) {
+		// k_spmv5's order: the 4 cells of a row group per thread, in row order
+		const Grp g = grp_of(t, pr.w, pr.h);
+		for (int e = 0; e < g.n; e++) {
+			const size_t k = g.k + e;
 			if (L.mask[k]) {
-				float pk = pr.p[k], qk;
-				if (K == 0) {
-					const int code = L.code[k];
-					const float *p = pr.p;
-					qk = a5_diff(pk, (code & 2) ? p[k + 1] : 0.f, (code & 4) ? p[k - 1] : 0.f,
-							(code & 8) ? p[k + pr.w] : 0.f, (code & 16) ? p[k - pr.w] : 0.f, code);
-				} else {
-					float d, o;
-					split<K>(L, pr.p, i, j, d, o);
-					qk = d * pk + o;
-				}
+				const int code = L.code[k];
+				const float *p = pr.p;
+				const float pk = p[k];
+				const float qk = a5_diff(pk, (code & 2) ? p[k + 1] : 0.f, (code & 4) ? p[k - 1] : 0.f,
+						(code & 8) ? p[k + pr.w] : 0.f, (code & 16) ? p[k - pr.w] : 0.f, code);
 				pr.q[k] = qk;
 				ff_add_prod(pq, pk, qk);
+			}
+		}
+	} else {
+		int i = tile_i(t);
+		for (int r = 0; r < SP_ROWS; r++) {
+			int j = tile_j(t, r);
+			if (i < pr.w && j < pr.h) {
+				size_t k = (size_t)j * pr.w + i;
+				if (L.mask[k]) {
+					float pk = pr.p[k], qk;
+					if (K == 0) {
+						const int code = L.code[k];
+						const float *p = pr.p;
+						qk = a5_diff(pk, (code & 2) ? p[k + 1] : 0.f, (code & 4) ? p[k - 1] : 0.f,
+								(code & 8) ? p[k + pr.w] : 0.f, (code & 16) ? p[k - pr.w] : 0.f, code);
+					} else {
+						float d, o;
+						split<K>(L, pr.p, i, j, d, o);
+						qk = d * pk + o;
+					}
+					pr.q[k] = qk;
+					ff_add_prod(pq, pk, qk);
+				}
 			}
 		}
 	}
@@ -1500,7 +1517,9 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 		const Grp g = grp_of(t, L.w, L.h);
 		if (g.n) st4(L.z, g, sz + ((threadIdx.x >> 3) + FH) * FR + 4 * (threadIdx.x & 7) + FH);
 	}
-	// restriction: one coarse cell per thread
+	// restriction: one coarse cell per thread.  A known child adds +0 to a sum
+	// that starts at +0 and so is never -0: it is skipped; an unknown one's
+	// neighbours are subtracted without tests (see sweep_cells)
 	if (cun) {
 		float acc = 0.f;
 		for (int bb = 0; bb < 2; bb++)
@@ -1509,7 +1528,10 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 				if (fi < L.w && fj < L.h) {
 					const int c = (fj - y0) * FR + (fi - x0);
 					const int code = sc[c];
-					acc += sb[c] - (diag_code(code) * sz[c] + off_code(sz, c, FR, code));
+					if (code & 1) {
+						const float off = (((0.f - sz[c + 1]) - sz[c - 1]) - sz[c + FR]) - sz[c - FR];
+						acc += sb[c] - (diag_code(code) * sz[c] + off);
+					}
 				}
 			}
 		C.b[(size_t)cj * C.w + ci] = 1.f * acc;
@@ -1960,7 +1982,6 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_spmv5(const ProbDev *__restri
 	constexpr int RW = SP_TILE + 8, RH = SP_TILE + 2;    // vector region: 40 x 34
 	__shared__ __align__(16) float sp[RW * RH];
 	__shared__ __align__(16) uint8_t sc[RW * RH];
-	__shared__ float2 spq[SP_TILE * SP_TILE];   // (p, q) of the unknown tile cells
 	__shared__ double sh[32];
 	const int4 t = tl[blockIdx.x];
 	grid_wait();
@@ -2001,7 +2022,8 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_spmv5(const ProbDev *__restri
 			}
 		}
 		__syncthreads();
-		// 4 cells of a row per thread (every neighbour is in the region)
+		// 4 cells of a row per thread (every neighbour is in the region); p.q
+		// summed over them in row order, as k_spmv does for w % 4 == 0
 		const int ty = threadIdx.x >> 3, tx = 4 * (threadIdx.x & 7);
 		const int gi = t.y * SP_TILE + tx, gj = t.z * SP_TILE + ty;
 		const int c = (ty + 1) * RW + tx + 4;
@@ -2014,17 +2036,14 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_spmv5(const ProbDev *__restri
 			if (code & 1) {
 				const int ce = c + e;
 				qk[e] = a5_diff(pk[e], sp[ce + 1], sp[ce - 1], sp[ce + RW], sp[ce - RW], code);
+				ff_add_prod(pq, pk[e], qk[e]);
 			}
-			spq[ty * SP_TILE + tx + e] = make_float2(pk[e], qk[e]);
 		}
 		if (gi < L.w && gj < L.h) {
 			const size_t k = (size_t)gj * L.w + gi;
 			*(float4 *)(pnew + k) = make_float4(pk[0], pk[1], pk[2], pk[3]);
 			*(float4 *)(pr.q + k) = make_float4(qk[0], qk[1], qk[2], qk[3]);
 		}
-		__syncthreads();
-		for (int q = threadIdx.x; q < SP_TILE * SP_TILE; q += SP_THREADS)
-			if (sc[((q >> 5) + 1) * RW + (q & 31) + 4] & 1) ff_add_prod(pq, spq[q].x, spq[q].y);
 	} else {
 		uint8_t *sm = sc;
 		const int x0 = t.y * SP_TILE - 1, y0 = t.z * SP_TILE - 1;
