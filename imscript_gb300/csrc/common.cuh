@@ -57,7 +57,9 @@ struct simpois_ctx {
 	// the last device-driven solve graph and the plan it was built for
 	cudaGraphExec_t solve_exec = nullptr;
 	std::string solve_sig;
-	long long solve_nodes_outer = 0, solve_nodes_inner = 0, solve_nodes_top = 0;
+	// kernel nodes of each problem group's refinement and PCG loop bodies
+	long long solve_nodes_outer[8] = {}, solve_nodes_inner[8] = {};
+	int solve_groups = 0;
 
 	// fused V-cycle hand-over size: fixed by the caller (0: none), and the
 	// autotuner's choice per batch shape

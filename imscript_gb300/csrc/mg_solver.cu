@@ -65,6 +65,7 @@
 namespace {
 
 constexpr int MAXLEV = 16;
+constexpr int GMAX = 8;               // problem groups of a solve graph
 constexpr int COARSE_MAX = 4;       // coarsest level: max(w, h) <= 4
 constexpr int COARSE_SWEEPS = 4;    // symmetric sweeps on the coarsest level (<= 4 x 4)
 constexpr int NU5 = 2;              // pre- and post-smoothing sweeps, 5-point
@@ -592,7 +593,7 @@ __global__ void __launch_bounds__(SP_THREADS) k_codes0(const ProbDev *__restrict
 // For level 0 also the per-problem tile ranges (tbeg, tcnt).
 __global__ void k_compact(const int4 *const *__restrict__ all, const int *const *__restrict__ flag,
 		const int *__restrict__ nall, int4 *const *__restrict__ act, int *__restrict__ nact,
-		int *__restrict__ tbeg, int *__restrict__ tcnt)
+		int *__restrict__ tbeg, int *__restrict__ tcnt, int *__restrict__ pcnt, int nprob)
 {
 	__shared__ int wsum[32];
 	__shared__ int carry;
@@ -613,6 +614,7 @@ __global__ void k_compact(const int4 *const *__restrict__ all, const int *const 
 		if (on) {
 			int4 t = all[l][k];
 			act[l][off] = t;
+			atomicAdd(pcnt + (size_t)l * nprob + t.x, 1);   // active tiles per level and problem
 			if (l == 0) {
 				atomicMin(tbeg + t.x, off);
 				atomicAdd(tcnt + t.x, 1);
@@ -1120,6 +1122,19 @@ bool verbose()
 	static bool v = [] {
 		const char *e = getenv("SIMPOIS_VERBOSE");
 		return e && atoi(e) > 0;
+	}();
+	return v;
+}
+
+// Problem groups of a batched fused 5-point solve, run as concurrent graph
+// branches (SIMPOIS_GROUPS, default 4; 1 keeps the whole batch in one).
+// Results are the same.
+int groups_max()
+{
+	static int v = [] {
+		const char *e = getenv("SIMPOIS_GROUPS");
+		const int g = e ? atoi(e) : 4;
+		return g < 1 ? 1 : (g > GMAX ? GMAX : g);
 	}();
 	return v;
 }
@@ -1803,7 +1818,7 @@ __device__ void warp_vcycle5(float *const *Z, float *const *B, const uint8_t *co
 // step first (x += alpha p, r -= alpha q in place, |r|^2 and the convergence
 // test of k_xr, summed in another order) and forms r.z and the PCG scalars.
 __global__ void __launch_bounds__(1024, 1) k_coarse5(const ProbDev *__restrict__ P, ProbState *st, Globals *gl,
-		int pcg, int use_p2)
+		int pcg, int use_p2, int p0)
 {
 	extern __shared__ __align__(16) unsigned char smem[];
 	__shared__ double sh[32];
@@ -1813,7 +1828,7 @@ __global__ void __launch_bounds__(1024, 1) k_coarse5(const ProbDev *__restrict__
 	__shared__ float *s_Z[MAXLEV], *s_B[MAXLEV];
 	__shared__ uint8_t *s_M[MAXLEV];
 	__shared__ const uint8_t *s_gm[MAXLEV];
-	const int prob = blockIdx.x;
+	const int prob = p0 + blockIdx.x;   // the launch covers problems p0 ..
 	grid_wait();
 	grid_release();
 	if (!st[prob].inner_active) return;
@@ -2425,7 +2440,37 @@ struct Plan {
 	// states (one synchronisation); the launch count is completed then
 	const Globals *hg = nullptr;
 	int pdl = 0;   // programmatic dependent launches between the V-cycle kernels
+	// problem groups: contiguous problem ranges solved as concurrent branches
+	// of the solve graph, each with its own loop counters (gls[g]) and its
+	// slice of every level's active tile list (stable compaction keeps a
+	// problem's tiles together); a view of one group is a Plan itself
+	int p0 = 0;                  // first problem of this view
+	int ngroups = 1;
+	int gp0[GMAX] = {}, gpn[GMAX] = {}, gnfine[GMAX] = {};
+	int gbeg[GMAX][MAXLEV] = {}, gcnt[GMAX][MAXLEV] = {};
+	Globals *gls = nullptr;      // GMAX loop-counter blocks (gl == gls: group 0)
+	int *tbeg_rel = nullptr;     // level-0 tile offsets relative to the group's first tile
+	int *pcnt = nullptr;         // active tiles per (level, problem)
 };
+
+// The view of problem group g: its problems, its tile-list slices, its loop
+// counters, its slice of the reduction partials.
+Plan group_view(const Plan &pl, int g)
+{
+	Plan v = pl;
+	v.n = pl.gpn[g];
+	v.p0 = pl.gp0[g];
+	v.nfine_max = pl.gnfine[g];
+	for (int l = 0; l < MAXLEV; l++) {
+		v.act[l] = pl.act[l] ? pl.act[l] + pl.gbeg[g][l] : nullptr;
+		v.nact[l] = pl.gcnt[g][l];
+	}
+	v.gl = pl.gls + g;
+	v.partial = pl.partial + 2 * (size_t)pl.gbeg[g][0];
+	v.tbeg = pl.tbeg_rel;
+	v.ngroups = 1;
+	return v;
+}
 
 // Launch with programmatic stream serialisation when pdl is set (the kernel
 // must call grid_wait() before its dependent accesses), else a plain launch.
@@ -2608,7 +2653,7 @@ void launch_vcycle_fused(const Plan &pl, cudaStream_t s, int pcg = 1, int use_p2
 	{
 		KT_BEGIN(pl, s);
 		launch_k(pl.pdl, k_coarse5, pl.n, 1024, pl.coarse_smem, s, (const ProbDev *)pl.dp, pl.dst, pl.gl, pcg,
-				use_p2); ++*pl.nl;
+				use_p2, pl.p0); ++*pl.nl;
 		KT_END(pl, s, "k_coarse5", pl.kt->cells() * BPC_COARSE5);
 	}
 	for (int l = pl.nfine_max - 1; l >= 0; l--) {
@@ -2677,6 +2722,15 @@ std::string plan_signature(const simpois_ctx *ctx, const Plan &pl, int K, int fu
 	snprintf(buf, sizeof buf, "%p/%d/%d/%d/%d/%d/%d/%d/%d|", (void *)ctx->arena, pl.n, K, (int)fused,
 			pl.nfine_max, pl.nlev_max, pl.coarse_smem, opt.use_mg, pl.pdl);
 	sig += buf;
+	const int ng = fused == MODE_FUSED5 ? pl.ngroups : 1;
+	for (int g = 0; g < ng && ng > 1; g++) {
+		snprintf(buf, sizeof buf, "g%d:%d+%d:%d|", g, pl.gp0[g], pl.gpn[g], pl.gnfine[g]);
+		sig += buf;
+		for (int l = 0; l < pl.nlev_max; l++) {
+			snprintf(buf, sizeof buf, "%d+%d,", pl.gbeg[g][l], pl.gcnt[g][l]);
+			sig += buf;
+		}
+	}
 	snprintf(buf, sizeof buf, "%p/%p/%p/%p/%p/%p|", (void *)pl.dp, (void *)pl.dst, (void *)pl.gl, (void *)pl.tbeg,
 			(void *)pl.tcnt, (void *)pl.partial);
 	sig += buf;
@@ -2693,86 +2747,118 @@ std::string plan_signature(const simpois_ctx *ctx, const Plan &pl, int K, int fu
 // inner solve runs.  Both loops are bounded (gmax) besides the per-problem
 // caps the kernels enforce.  Returns cudaErrorNotSupported-like failures to
 // the caller, which then drives the loops from the host.
+// Add one problem group's loops to the solve graph G: the refinement WHILE
+// node (no dependencies: groups run concurrently) with the PCG WHILE node in
+// its body.  n_outer / n_inner: kernel nodes of the two bodies.
 template <int K>
-cudaError_t build_solve_graph(simpois_ctx *ctx, Plan &pl, const MgOptions &opt, int mode)
+cudaError_t add_solve_loops(cudaGraph_t G, cudaStream_t cs, Plan &pl, const MgOptions &opt, int mode,
+		long long *n_outer, long long *n_inner)
 {
-	cudaStream_t cs = ctx->capture_stream;
 	const int nt = pl.nact[0];
-	cudaGraph_t G = nullptr;
-	cudaError_t e = cudaGraphCreate(&G, 0);
-	if (e != cudaSuccess) return e;
-	long long n0 = *pl.nl, n_outer = 0, n_inner = 0;
+	cudaError_t e;
 	cudaGraphConditionalHandle ho, hi;
 	cudaGraphNodeParams po = {};
 	cudaGraphNode_t node_o, node_i;
 	cudaGraph_t body_o = nullptr, body_i = nullptr;
-	do {
-		if ((e = cudaGraphConditionalHandleCreate(&ho, G, 1, cudaGraphCondAssignDefault)) != cudaSuccess) break;
-		po.type = cudaGraphNodeTypeConditional;
-		po.conditional.handle = ho;
-		po.conditional.type = cudaGraphCondTypeWhile;
-		po.conditional.size = 1;
-		if ((e = cudaGraphAddNode(&node_o, G, nullptr, nullptr, 0, &po)) != cudaSuccess) break;
-		body_o = po.conditional.phGraph_out[0];
-		// refinement body
-		if ((e = cudaStreamBeginCaptureToGraph(cs, body_o, nullptr, nullptr, 0,
-				cudaStreamCaptureModeThreadLocal)) != cudaSuccess) break;
-		cudaError_t ce = cudaGraphConditionalHandleCreate(&hi, body_o, 0, cudaGraphCondAssignDefault);
-		long long c0 = *pl.nl;
-		k_resid64<K><<<nt, SP_THREADS, 0, cs>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl);
-		++*pl.nl;
-		if (mode == MODE_FUSED5) {
-			launch_vcycle_fused(pl, cs);
-		} else if (mode == MODE_BIH64) {
-			launch_precond_bih(pl, cs);
+	if ((e = cudaGraphConditionalHandleCreate(&ho, G, 1, cudaGraphCondAssignDefault)) != cudaSuccess) return e;
+	po.type = cudaGraphNodeTypeConditional;
+	po.conditional.handle = ho;
+	po.conditional.type = cudaGraphCondTypeWhile;
+	po.conditional.size = 1;
+	if ((e = cudaGraphAddNode(&node_o, G, nullptr, nullptr, 0, &po)) != cudaSuccess) return e;
+	body_o = po.conditional.phGraph_out[0];
+	// refinement body
+	if ((e = cudaStreamBeginCaptureToGraph(cs, body_o, nullptr, nullptr, 0,
+			cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
+	cudaError_t ce = cudaGraphConditionalHandleCreate(&hi, body_o, 0, cudaGraphCondAssignDefault);
+	long long c0 = *pl.nl;
+	k_resid64<K><<<nt, SP_THREADS, 0, cs>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl);
+	++*pl.nl;
+	if (mode == MODE_FUSED5) {
+		launch_vcycle_fused(pl, cs);
+	} else if (mode == MODE_BIH64) {
+		launch_precond_bih(pl, cs);
+	} else {
+		launch_precond<K>(pl, opt, cs);
+		k_rz<<<nt, SP_THREADS, 0, cs>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl); ++*pl.nl;
+	}
+	const int gmax_inner = mode == MODE_BIH64 ? INNER_MAX13 + 4 : 4 * INNER_MAX;
+	k_setcond<<<1, 32, 0, cs>>>(hi, pl.gl, 0, 1, gmax_inner); ++*pl.nl;
+	cudaStreamCaptureStatus cst;
+	cudaGraph_t cg;
+	const cudaGraphNode_t *deps = nullptr;
+	size_t ndeps = 0;
+	if (ce == cudaSuccess) ce = cudaStreamGetCaptureInfo(cs, &cst, nullptr, &cg, &deps, nullptr, &ndeps);
+	cudaGraphNodeParams pi = {};
+	pi.type = cudaGraphNodeTypeConditional;
+	pi.conditional.handle = hi;
+	pi.conditional.type = cudaGraphCondTypeWhile;
+	pi.conditional.size = 1;
+	if (ce == cudaSuccess) ce = cudaGraphAddNode(&node_i, cg, deps, nullptr, ndeps, &pi);
+	if (ce == cudaSuccess) ce = cudaStreamUpdateCaptureDependencies(cs, &node_i, nullptr, 1,
+			cudaStreamSetCaptureDependencies);
+	if (mode != MODE_BIH64) {   // the FP64 biharmonic PCG updates U itself
+		k_uadd<<<nt, SP_THREADS, 0, cs>>>(pl.dp, pl.dst, pl.act[0]); ++*pl.nl;
+	}
+	k_setcond<<<1, 32, 0, cs>>>(ho, pl.gl, 1, 0, MAX_OUTER + 2); ++*pl.nl;
+	*n_outer = *pl.nl - c0;
+	e = cudaStreamEndCapture(cs, &body_o);
+	if (ce != cudaSuccess) e = ce;
+	if (e != cudaSuccess) return e;
+	body_i = pi.conditional.phGraph_out[0];
+	// PCG body
+	if ((e = cudaStreamBeginCaptureToGraph(cs, body_i, nullptr, nullptr, 0,
+			cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
+	c0 = *pl.nl;
+	if (mode == MODE_FUSED5)
+		launch_iteration_fused(pl, cs);
+	else if (mode == MODE_BIH64)
+		launch_iteration_bih(pl, cs);
+	else
+		launch_iteration<K>(pl, opt, cs);
+	k_setcond<<<1, 32, 0, cs>>>(hi, pl.gl, 0, 0, gmax_inner); ++*pl.nl;
+	*n_inner = *pl.nl - c0;
+	return cudaStreamEndCapture(cs, &body_i);
+}
+
+// Build the whole converged solve as one graph: per problem group (one group
+// unless the fused 5-point batch was split), two nested device-side WHILE
+// loops -- refinement steps (k_resid64, first V-cycle, the PCG loop, U += x)
+// while a problem of the group is still refining, and PCG iterations while a
+// problem's inner solve runs.  The groups' loops are independent branches, so
+// one group's latency-bound coarse levels overlap another's fine-level work.
+// Both loops are bounded (gmax) besides the per-problem caps the kernels
+// enforce.  Returns the CUDA error of a failed build; the caller then drives
+// the loops from the host.
+template <int K>
+cudaError_t build_solve_graph(simpois_ctx *ctx, Plan &pl, const MgOptions &opt, int mode)
+{
+	cudaGraph_t G = nullptr;
+	cudaError_t e = cudaGraphCreate(&G, 0);
+	if (e != cudaSuccess) return e;
+	const long long n0 = *pl.nl;
+	const int ng = mode == MODE_FUSED5 ? pl.ngroups : 1;
+	long long no[GMAX] = {}, ni[GMAX] = {};
+	for (int g = 0; g < ng && e == cudaSuccess; g++) {
+		if (ng > 1) {
+			Plan v = group_view(pl, g);
+			e = add_solve_loops<K>(G, ctx->capture_stream, v, opt, mode, no + g, ni + g);
 		} else {
-			launch_precond<K>(pl, opt, cs);
-			k_rz<<<nt, SP_THREADS, 0, cs>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl); ++*pl.nl;
+			e = add_solve_loops<K>(G, ctx->capture_stream, pl, opt, mode, no + g, ni + g);
 		}
-		const int gmax_inner = mode == MODE_BIH64 ? INNER_MAX13 + 4 : 4 * INNER_MAX;
-		k_setcond<<<1, 32, 0, cs>>>(hi, pl.gl, 0, 1, gmax_inner); ++*pl.nl;
-		cudaStreamCaptureStatus cst;
-		cudaGraph_t cg;
-		const cudaGraphNode_t *deps = nullptr;
-		size_t ndeps = 0;
-		if (ce == cudaSuccess) ce = cudaStreamGetCaptureInfo(cs, &cst, nullptr, &cg, &deps, nullptr, &ndeps);
-		cudaGraphNodeParams pi = {};
-		pi.type = cudaGraphNodeTypeConditional;
-		pi.conditional.handle = hi;
-		pi.conditional.type = cudaGraphCondTypeWhile;
-		pi.conditional.size = 1;
-		if (ce == cudaSuccess) ce = cudaGraphAddNode(&node_i, cg, deps, nullptr, ndeps, &pi);
-		if (ce == cudaSuccess) ce = cudaStreamUpdateCaptureDependencies(cs, &node_i, nullptr, 1,
-				cudaStreamSetCaptureDependencies);
-		if (mode != MODE_BIH64) {   // the FP64 biharmonic PCG updates U itself
-			k_uadd<<<nt, SP_THREADS, 0, cs>>>(pl.dp, pl.dst, pl.act[0]); ++*pl.nl;
-		}
-		k_setcond<<<1, 32, 0, cs>>>(ho, pl.gl, 1, 0, MAX_OUTER + 2); ++*pl.nl;
-		n_outer = *pl.nl - c0;
-		e = cudaStreamEndCapture(cs, &body_o);
-		if (ce != cudaSuccess) e = ce;
-		if (e != cudaSuccess) break;
-		body_i = pi.conditional.phGraph_out[0];
-		// PCG body
-		if ((e = cudaStreamBeginCaptureToGraph(cs, body_i, nullptr, nullptr, 0,
-				cudaStreamCaptureModeThreadLocal)) != cudaSuccess) break;
-		c0 = *pl.nl;
-		if (mode == MODE_FUSED5)
-			launch_iteration_fused(pl, cs);
-		else if (mode == MODE_BIH64)
-			launch_iteration_bih(pl, cs);
-		else
-			launch_iteration<K>(pl, opt, cs);
-		k_setcond<<<1, 32, 0, cs>>>(hi, pl.gl, 0, 0, gmax_inner); ++*pl.nl;
-		n_inner = *pl.nl - c0;
-		if ((e = cudaStreamEndCapture(cs, &body_i)) != cudaSuccess) break;
+	}
+	if (e == cudaSuccess) {
 		cudaGraphExec_t ex = nullptr;
-		if ((e = cudaGraphInstantiate(&ex, G, 0)) != cudaSuccess) break;
-		if (ctx->solve_exec) cudaGraphExecDestroy(ctx->solve_exec);
-		ctx->solve_exec = ex;
-		ctx->solve_nodes_outer = n_outer;
-		ctx->solve_nodes_inner = n_inner;
-	} while (0);
+		if ((e = cudaGraphInstantiate(&ex, G, 0)) == cudaSuccess) {
+			if (ctx->solve_exec) cudaGraphExecDestroy(ctx->solve_exec);
+			ctx->solve_exec = ex;
+			ctx->solve_groups = ng;
+			for (int g = 0; g < ng; g++) {
+				ctx->solve_nodes_outer[g] = no[g];
+				ctx->solve_nodes_inner[g] = ni[g];
+			}
+		}
+	}
 	*pl.nl = n0;
 	cudaGraphDestroy(G);
 	if (e != cudaSuccess) cudaGetLastError();
@@ -2793,7 +2879,7 @@ int run_device_loop(simpois_ctx *ctx, Plan &pl, const MgOptions &opt, int mode, 
 	cudaStream_t s = ctx->stream;
 	SP_CUDA(ctx, cudaGraphLaunch(ctx->solve_exec, s));
 	Globals *hg = (Globals *)ctx->pinned;   // read with the final states
-	SP_CUDA(ctx, cudaMemcpyAsync(hg, pl.gl, sizeof(Globals), cudaMemcpyDeviceToHost, s));
+	SP_CUDA(ctx, cudaMemcpyAsync(hg, pl.gls, sizeof(Globals) * ctx->solve_groups, cudaMemcpyDeviceToHost, s));
 	pl.hg = hg;
 	*done = true;
 	return SIMPOIS_OK;
@@ -3051,7 +3137,8 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	}
 	size_t o_dp = Lo.take(sizeof(ProbDev) * n);
 	size_t o_st = Lo.take(sizeof(ProbState) * n);
-	size_t o_gl = Lo.take(sizeof(Globals));
+	size_t o_gl = Lo.take(sizeof(Globals) * GMAX);
+	size_t o_pcnt = Lo.take(sizeof(int) * MAXLEV * n), o_trel = Lo.take(sizeof(int) * n);
 	size_t o_all[MAXLEV], o_act[MAXLEV], o_flag[MAXLEV];
 	for (int l = 0; l < pl.nlev_max; l++) {
 		pl.nall[l] = (int)lists[l].size();
@@ -3077,13 +3164,14 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	char *A = ctx->arena;
 
 	// host images of the device tables, staged in pinned memory
-	size_t stage_bytes = sizeof(ProbDev) * n + sizeof(ProbState) * n + sizeof(Globals);
+	size_t stage_bytes = sizeof(ProbDev) * n + sizeof(ProbState) * n + sizeof(Globals) * GMAX;
 	for (int l = 0; l < pl.nlev_max; l++) stage_bytes += sizeof(int4) * lists[l].size();
 	stage_bytes += 64 * MAXLEV + sizeof(void *) * 3 * n + sizeof(int) * n + 16 * (MAXLEV + 16) + 4096;
 	stage_bytes += sizeof(CUtensorMap) * nmaps + 128;
-	rc = ctx_pinned_reserve(ctx, stage_bytes + 256);
+	stage_bytes += sizeof(int) * (MAXLEV + 1) * n + 64;   // per-problem tile counts, group offsets
+	rc = ctx_pinned_reserve(ctx, stage_bytes + 256 * GMAX);
 	if (rc) return rc;
-	char *stage = ctx->pinned + 256;  // the first 256 bytes hold read-back scalars
+	char *stage = ctx->pinned + 256 * GMAX;  // the first bytes hold read-back scalars
 
 	for (int k = 0; k < n; k++) {
 		ProbDev &d = pl.hp[k];
@@ -3145,7 +3233,10 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	}
 	pl.dp = (ProbDev *)(A + o_dp);
 	pl.dst = (ProbState *)(A + o_st);
-	pl.gl = (Globals *)(A + o_gl);
+	pl.gls = (Globals *)(A + o_gl);
+	pl.gl = pl.gls;
+	pl.pcnt = (int *)(A + o_pcnt);
+	pl.tbeg_rel = (int *)(A + o_trel);
 	pl.tbeg = (int *)(A + o_tbeg);
 	pl.tcnt = (int *)(A + o_tcnt);
 	pl.partial = (double *)(A + o_part);
@@ -3176,12 +3267,13 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 		hst[k].status = SIMPOIS_OK;
 		hst[k].max_iter = opt.max_iter > 0 ? opt.max_iter : 500;
 	}
-	Globals hg;
-	memset(&hg, 0, sizeof(hg));
+	std::vector<Globals> hg(GMAX);
+	memset(hg.data(), 0, sizeof(Globals) * GMAX);
 	SP_CUDA(ctx, put(pl.dp, pl.hp.data(), sizeof(ProbDev) * n));
 	if (nmaps) SP_CUDA(ctx, put(A + o_tmap, maps.data(), sizeof(CUtensorMap) * nmaps));
 	SP_CUDA(ctx, put(pl.dst, hst.data(), sizeof(ProbState) * n));
-	SP_CUDA(ctx, put(pl.gl, &hg, sizeof(hg)));
+	SP_CUDA(ctx, put(pl.gls, hg.data(), sizeof(Globals) * GMAX));
+	SP_CUDA(ctx, cudaMemsetAsync(pl.pcnt, 0, sizeof(int) * MAXLEV * n, s));
 	for (int l = 0; l < pl.nlev_max; l++)
 		SP_CUDA(ctx, put(pl.all[l], lists[l].data(), sizeof(int4) * lists[l].size()));
 	SP_CUDA(ctx, put(pl.dnall, pl.nall, sizeof(int) * MAXLEV));
@@ -3207,13 +3299,66 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	for (int l = 1; l < pl.nlev_max; l++) {
 		k_mask_down<<<pl.nall[l], SP_THREADS, 0, s>>>(pl.dp, pl.all[l], l, pl.flag[l]); ++*pl.nl;
 	}
-	k_compact<<<pl.nlev_max, 1024, 0, s>>>(pl.dall, pl.dflag, pl.dnall, pl.dact, pl.dnact, pl.tbeg, pl.tcnt); ++*pl.nl;
+	k_compact<<<pl.nlev_max, 1024, 0, s>>>(pl.dall, pl.dflag, pl.dnall, pl.dact, pl.dnact, pl.tbeg, pl.tcnt,
+			pl.pcnt, n); ++*pl.nl;
 	k_init_counts<<<1, 256, 0, s>>>(pl.dst, pl.tcnt, n, pl.gl); ++*pl.nl;
 	SP_LAUNCH_CHECK(ctx);
 	int *hn = (int *)ctx->pinned;
 	SP_CUDA(ctx, cudaMemcpyAsync(hn, pl.dnact, sizeof(int) * MAXLEV, cudaMemcpyDeviceToHost, s));
+	int *hpc = (int *)stage;   // the uploads above are done with the staging by now (stream order)
+	const bool grouped = n > 1 && groups_max() > 1 && opt.use_graph && !opt.ktimer && !verbose() && opt.use_mg &&
+			pl.fused && K == 0;
+	if (grouped)
+		SP_CUDA(ctx, cudaMemcpyAsync(hpc, pl.pcnt, sizeof(int) * MAXLEV * n, cudaMemcpyDeviceToHost, s));
 	SP_CUDA(ctx, cudaStreamSynchronize(s));
 	for (int l = 0; l < pl.nlev_max; l++) pl.nact[l] = hn[l];
+	pl.ngroups = 1;
+	pl.gp0[0] = 0;
+	pl.gpn[0] = n;
+	pl.gnfine[0] = pl.nfine_max;
+	for (int l = 0; l < MAXLEV; l++) pl.gcnt[0][l] = pl.nact[l];
+	if (grouped) {
+		// contiguous problem ranges with about equal level-0 active tiles
+		const int G = std::min(n, groups_max());
+		long long tot = 0, acc = 0;
+		for (int k = 0; k < n; k++) tot += hpc[k];
+		int g = 0;
+		pl.gpn[0] = 0;
+		for (int k = 0; k < n; k++) {
+			acc += hpc[k];
+			pl.gpn[g]++;
+			if (g + 1 < G && k + 1 < n && acc * G >= tot * (g + 1)) {
+				g++;
+				pl.gp0[g] = k + 1;
+				pl.gpn[g] = 0;
+			}
+		}
+		pl.ngroups = g + 1;
+		int *hrel = hpc + MAXLEV * n;
+		for (int gg = 0; gg < pl.ngroups; gg++) {
+			pl.gnfine[gg] = 0;
+			for (int l = 0; l < MAXLEV; l++) {
+				int b = 0, c = 0;
+				for (int k = 0; k < pl.gp0[gg]; k++) b += l < pl.nlev_max ? hpc[(size_t)l * n + k] : 0;
+				for (int k = pl.gp0[gg]; k < pl.gp0[gg] + pl.gpn[gg]; k++)
+					c += l < pl.nlev_max ? hpc[(size_t)l * n + k] : 0;
+				pl.gbeg[gg][l] = b;
+				pl.gcnt[gg][l] = c;
+			}
+			int r = 0;
+			for (int k = pl.gp0[gg]; k < pl.gp0[gg] + pl.gpn[gg]; k++) {
+				hrel[k] = r;   // a problem's level-0 tiles from its group's first
+				r += hpc[k];
+				pl.gnfine[gg] = std::max(pl.gnfine[gg], pl.hp[k].nfine);
+			}
+		}
+		SP_CUDA(ctx, cudaMemcpyAsync(pl.tbeg_rel, hrel, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+		for (int gg = 0; gg < pl.ngroups; gg++) {
+			k_init_counts<<<1, 256, 0, s>>>(pl.dst + pl.gp0[gg], pl.tcnt + pl.gp0[gg], pl.gpn[gg], pl.gls + gg);
+			++*pl.nl;
+		}
+		SP_LAUNCH_CHECK(ctx);
+	}
 
 	KTimer kt;
 	if (opt.ktimer) {
@@ -3248,12 +3393,15 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	}
 	SP_LAUNCH_CHECK(ctx);
 	ProbState *hs = (ProbState *)stage;
-	int *htma = (int *)(stage + ((sizeof(ProbState) * n + 15) / 16 * 16));
+	Globals *hgl = (Globals *)(stage + ((sizeof(ProbState) * n + 15) / 16 * 16));
 	SP_CUDA(ctx, cudaMemcpyAsync(hs, pl.dst, sizeof(ProbState) * n, cudaMemcpyDeviceToHost, s));
-	SP_CUDA(ctx, cudaMemcpyAsync(htma, &pl.gl->tma_timeout, sizeof(int), cudaMemcpyDeviceToHost, s));
+	SP_CUDA(ctx, cudaMemcpyAsync(hgl, pl.gls, sizeof(Globals) * GMAX, cudaMemcpyDeviceToHost, s));
 	SP_CUDA(ctx, cudaStreamSynchronize(s));
-	if (pl.hg) *pl.nl += ctx->solve_nodes_outer * pl.hg->n_outer + ctx->solve_nodes_inner * pl.hg->n_inner;
-	if (*htma) return ctx_fail(ctx, SIMPOIS_ECUDA, "a TMA region load did not complete in time");
+	if (pl.hg)
+		for (int g = 0; g < ctx->solve_groups; g++)
+			*pl.nl += ctx->solve_nodes_outer[g] * pl.hg[g].n_outer + ctx->solve_nodes_inner[g] * pl.hg[g].n_inner;
+	for (int g = 0; g < GMAX; g++)
+		if (hgl[g].tma_timeout) return ctx_fail(ctx, SIMPOIS_ECUDA, "a TMA region load did not complete in time");
 	for (int k = 0; k < n; k++) {
 		rep[k].status = hs[k].status;
 		rep[k].unknowns = hs[k].nunknown;
