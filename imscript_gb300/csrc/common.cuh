@@ -58,7 +58,7 @@ struct simpois_ctx {
 	cudaGraphExec_t solve_exec = nullptr;
 	std::string solve_sig;
 	// kernel nodes of each problem group's refinement and PCG loop bodies
-	long long solve_nodes_outer[8] = {}, solve_nodes_inner[8] = {};
+	long long solve_nodes_outer[16] = {}, solve_nodes_inner[16] = {};
 	int solve_groups = 0;
 
 	// fused V-cycle hand-over size: fixed by the caller (0: none), and the

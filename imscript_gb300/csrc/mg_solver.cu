@@ -65,7 +65,7 @@
 namespace {
 
 constexpr int MAXLEV = 16;
-constexpr int GMAX = 8;               // problem groups of a solve graph
+constexpr int GMAX = 16;              // problem groups of a solve graph (the context's node tables)
 constexpr int COARSE_MAX = 4;       // coarsest level: max(w, h) <= 4
 constexpr int COARSE_SWEEPS = 4;    // symmetric sweeps on the coarsest level (<= 4 x 4)
 constexpr int NU5 = 2;              // pre- and post-smoothing sweeps, 5-point
@@ -1127,13 +1127,14 @@ bool verbose()
 }
 
 // Problem groups of a batched fused 5-point solve, run as concurrent graph
-// branches (SIMPOIS_GROUPS, default 4; 1 keeps the whole batch in one).
-// Results are the same.
+// branches (SIMPOIS_GROUPS, default 8 -- measured best against 4 and 16 on
+// 256 uneven instances and on 32 images of 1024^2; 1 keeps the whole batch
+// in one).  Results are the same.
 int groups_max()
 {
 	static int v = [] {
 		const char *e = getenv("SIMPOIS_GROUPS");
-		const int g = e ? atoi(e) : 4;
+		const int g = e ? atoi(e) : 8;
 		return g < 1 ? 1 : (g > GMAX ? GMAX : g);
 	}();
 	return v;
