@@ -2418,7 +2418,6 @@ __global__ void k_dense_resid(const float *__restrict__ u, const float *__restri
 
 struct Plan {
 	int n = 0, nlev_max = 0, kind_mask = 0;
-	std::vector<ProbDev> hp;
 	ProbDev *dp = nullptr;
 	ProbState *dst = nullptr;
 	Globals *gl = nullptr;
@@ -3059,7 +3058,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	Plan pl;
 	pl.nl = &ctx->launches;
 	pl.n = n;
-	pl.hp.resize(n);
+	std::vector<ProbDev> hp(n);   // host image of the problem table
 	int kinds = 0;
 	Layout Lo;
 	std::vector<size_t> off_mask[MAXLEV], off_code[MAXLEV], off_b[MAXLEV], off_z[MAXLEV], off_z2[MAXLEV];
@@ -3071,7 +3070,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 		const MgProblem &q = probs[k];
 		int lw[MAXLEV], lh[MAXLEV];
 		int nl = level_dims(q.w, q.h, lw, lh);
-		ProbDev &d = pl.hp[k];
+		ProbDev &d = hp[k];
 		memset(&d, 0, sizeof(d));
 		d.nlev = nl;
 		d.kind = q.kind;
@@ -3156,8 +3155,8 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	// TMA maps (b and code) of the tile levels whose rows are 16-byte multiples
 	int nmaps = 0;
 	for (int k = 0; k < n && opt.tma; k++)
-		for (int l = 0; l < pl.hp[k].nfine; l++)
-			if (pl.hp[k].lv[l].w % 16 == 0) nmaps += l == 0 ? 3 : 2;   // level 0: also b_alt
+		for (int l = 0; l < hp[k].nfine; l++)
+			if (hp[k].lv[l].w % 16 == 0) nmaps += l == 0 ? 3 : 2;   // level 0: also b_alt
 	size_t o_tmap = Lo.take(sizeof(CUtensorMap) * std::max(1, nmaps), 128);
 	size_t total = Lo.off;
 	int rc = ctx_arena_reserve(ctx, total);
@@ -3175,7 +3174,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	char *stage = ctx->pinned + 256 * GMAX;  // the first bytes hold read-back scalars
 
 	for (int k = 0; k < n; k++) {
-		ProbDev &d = pl.hp[k];
+		ProbDev &d = hp[k];
 		const MgProblem &q = probs[k];
 		d.g = q.g;
 		d.out = q.out;
@@ -3215,7 +3214,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 		CUtensorMap *dmaps = (CUtensorMap *)(A + o_tmap);
 		int im = 0;
 		for (int k = 0; k < n && opt.tma; k++) {
-			ProbDev &d = pl.hp[k];
+			ProbDev &d = hp[k];
 			for (int l = 0; l < d.nfine; l++) {
 				LevelDev &L = d.lv[l];
 				if (L.w % 16 != 0) continue;
@@ -3270,7 +3269,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	}
 	std::vector<Globals> hg(GMAX);
 	memset(hg.data(), 0, sizeof(Globals) * GMAX);
-	SP_CUDA(ctx, put(pl.dp, pl.hp.data(), sizeof(ProbDev) * n));
+	SP_CUDA(ctx, put(pl.dp, hp.data(), sizeof(ProbDev) * n));
 	if (nmaps) SP_CUDA(ctx, put(A + o_tmap, maps.data(), sizeof(CUtensorMap) * nmaps));
 	SP_CUDA(ctx, put(pl.dst, hst.data(), sizeof(ProbState) * n));
 	SP_CUDA(ctx, put(pl.gls, hg.data(), sizeof(Globals) * GMAX));
@@ -3350,7 +3349,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 			for (int k = pl.gp0[gg]; k < pl.gp0[gg] + pl.gpn[gg]; k++) {
 				hrel[k] = r;   // a problem's level-0 tiles from its group's first
 				r += hpc[k];
-				pl.gnfine[gg] = std::max(pl.gnfine[gg], pl.hp[k].nfine);
+				pl.gnfine[gg] = std::max(pl.gnfine[gg], hp[k].nfine);
 			}
 		}
 		SP_CUDA(ctx, cudaMemcpyAsync(pl.tbeg_rel, hrel, sizeof(int) * n, cudaMemcpyHostToDevice, s));
@@ -3376,7 +3375,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 			for (const int4 &t : h) kt.tiles[(size_t)l * n + t.x]++;
 		}
 		for (int k = 0; k < n; k++) {
-			const LevelDev &c = pl.hp[k].lv[pl.hp[k].nfine];
+			const LevelDev &c = hp[k].lv[hp[k].nfine];
 			kt.coarse_cells[k] = c.w * c.h;
 		}
 		pl.kt = &kt;
