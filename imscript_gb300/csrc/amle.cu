@@ -170,6 +170,18 @@ __global__ void k_amle_init(AmleArgs a)
 // the same values outside the tiles with unknowns, which no launch touches.
 // NN > 0: the neighbourhood size known at compile time (the loop over the
 // neighbours unrolls); NN == 0: a.nn at run time.
+// (wmx v_min + wmn v_max) / (wmx + wmn), the reference's midpoint.  The
+// weights are 1, 2, 5, 10 or 13, so a denominator of 2 or 4 is a power of
+// two: multiplying by its reciprocal gives the same float as dividing.
+__device__ __forceinline__ float amle_mid(float mn, float mx, float wmn, float wmx)
+{
+	const float num = __fadd_rn(__fmul_rn(wmx, mn), __fmul_rn(wmn, mx));
+	const float den = __fadd_rn(wmx, wmn);
+	if (den == 2.f) return __fmul_rn(num, 0.5f);
+	if (den == 4.f) return __fmul_rn(num, 0.25f);
+	return __fdiv_rn(num, den);
+}
+
 template <int NN>
 __global__ void __launch_bounds__(SP_THREADS) k_amle_fused(AmleArgs a, const float *__restrict__ sinf,
 		const float *__restrict__ ssup, float *__restrict__ dinf, float *__restrict__ dsup, int r, int s0, int S)
@@ -246,8 +258,14 @@ __global__ void __launch_bounds__(SP_THREADS) k_amle_fused(AmleArgs a, const flo
 					if (v1 > mx1) { mx1 = v1; wmx1 = wt; }
 				}
 			}
-			zi[q] = __fdiv_rn(__fadd_rn(__fmul_rn(wmx0, mn0), __fmul_rn(wmn0, mx0)), __fadd_rn(wmx0, wmn0));
-			zs[q] = __fdiv_rn(__fadd_rn(__fmul_rn(wmx1, mn1), __fmul_rn(wmn1, mx1)), __fadd_rn(wmx1, wmn1));
+			if (NN == 4 && !first) {
+				// the 4-neighbourhood weighs every neighbour 1: (v_min + v_max) / 2
+				zi[q] = __fmul_rn(__fadd_rn(mn0, mx0), 0.5f);
+				zs[q] = __fmul_rn(__fadd_rn(mn1, mx1), 0.5f);
+			} else {
+				zi[q] = amle_mid(mn0, mx0, wmn0, wmx0);
+				zs[q] = amle_mid(mn1, mx1, wmn1, wmx1);
+			}
 		}
 		__syncthreads();
 	}
