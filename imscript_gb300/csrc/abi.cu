@@ -376,6 +376,7 @@ int simpois_destroy(simpois_ctx *ctx)
 	if (ctx->aux_stream) cudaStreamDestroy(ctx->aux_stream);
 	if (ctx->ev_in) cudaEventDestroy(ctx->ev_in);
 	if (ctx->ev_out) cudaEventDestroy(ctx->ev_out);
+	if (ctx->ev_rhs) cudaEventDestroy(ctx->ev_rhs);
 	for (cudaEvent_t e : ctx->evpool) cudaEventDestroy(e);
 	if (ctx->solve_exec) cudaGraphExecDestroy(ctx->solve_exec);
 	if (ctx->amle_exec) cudaGraphExecDestroy(ctx->amle_exec);
@@ -488,28 +489,37 @@ int simpois_solve(simpois_ctx *ctx, float *out, const float *in, const float *da
 		SP_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking));
 		SP_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_in, cudaEventDisableTiming));
 		SP_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_out, cudaEventDisableTiming));
+		SP_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_rhs, cudaEventDisableTiming));
 	}
 	const int grid = 8 * (ctx->sm_count > 0 ? ctx->sm_count : 1);
 	SP_CUDA(ctx, cudaMemcpyAsync(din, in, bytes, cudaMemcpyHostToDevice, s));
 	if (direct) {
-		// the known pixels of the output are those of g: back while the solve runs
+		// on the second stream, once g is in: the data term's groups that hold
+		// an unknown (overlapping the solve's setup, which does not read f),
+		// then the output's known pixels -- those of g -- while the solve runs
 		SP_CUDA(ctx, cudaEventRecord(ctx->ev_in, s));
 		SP_CUDA(ctx, cudaStreamWaitEvent(ctx->aux_stream, ctx->ev_in, 0));
-		SP_CUDA(ctx, cudaMemcpyAsync(out, din, bytes, cudaMemcpyDeviceToHost, ctx->aux_stream));
-		SP_CUDA(ctx, cudaEventRecord(ctx->ev_out, ctx->aux_stream));
 		if (dat) {
-			k_fetch_rhs<<<grid, 256, 0, s>>>((const float4 *)din, hdat, (float4 *)ddat, n / 4);
+			k_fetch_rhs<<<grid, 256, 0, ctx->aux_stream>>>((const float4 *)din, hdat, (float4 *)ddat, n / 4);
 			ctx->launches++;
 			const cudaError_t e = cudaGetLastError();
 			if (e != cudaSuccess) {
 				cudaStreamSynchronize(ctx->aux_stream);
 				return ctx_fail(ctx, SIMPOIS_ECUDA, "k_fetch_rhs: %s", cudaGetErrorString(e));
 			}
+			SP_CUDA(ctx, cudaEventRecord(ctx->ev_rhs, ctx->aux_stream));
+			ctx->rhs_pending = ctx->ev_rhs;
 		}
+		SP_CUDA(ctx, cudaMemcpyAsync(out, din, bytes, cudaMemcpyDeviceToHost, ctx->aux_stream));
+		SP_CUDA(ctx, cudaEventRecord(ctx->ev_out, ctx->aux_stream));
 	} else if (dat) {
 		SP_CUDA(ctx, cudaMemcpyAsync(ddat, dat, bytes, cudaMemcpyHostToDevice, s));
 	}
 	int st = simpois_solve_device(ctx, dout, din, ddat, w, h, pd, params, reports);
+	if (ctx->rhs_pending) {   // a solve that stopped before its loops
+		cudaStreamWaitEvent(s, ctx->rhs_pending, 0);
+		ctx->rhs_pending = nullptr;
+	}
 	if (st != SIMPOIS_OK && st != SIMPOIS_NOT_CONVERGED && st != SIMPOIS_BREAKDOWN) {
 		if (direct) cudaStreamSynchronize(ctx->aux_stream);   // the caller may free out
 		return st;

@@ -38,7 +38,11 @@ struct simpois_ctx {
 	// its second stream (the output's known pixels go back while the solve
 	// runs) and the events that order it with `stream`
 	cudaStream_t aux_stream = nullptr;
-	cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+	cudaEvent_t ev_in = nullptr, ev_out = nullptr, ev_rhs = nullptr;
+	// set while the data term is still arriving on aux_stream: the next
+	// converged solve waits for it before its first read of f (its setup
+	// does not read f)
+	cudaEvent_t rhs_pending = nullptr;
 
 	// kernel launches issued (graph replays count their kernel nodes)
 	long long launches = 0;

@@ -3380,6 +3380,10 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 		}
 		pl.kt = &kt;
 	}
+	if (ctx->rhs_pending) {   // the data term is still arriving: the loops read it
+		SP_CUDA(ctx, cudaStreamWaitEvent(s, ctx->rhs_pending, 0));
+		ctx->rhs_pending = nullptr;
+	}
 	rc = K == 0 ? run_kind<0>(ctx, pl, opt) : run_kind<1>(ctx, pl, opt);
 	if (rc) return rc;
 	if (pl.kt) kt_collect(ctx, kt);
