@@ -232,6 +232,54 @@ static int read_asc(raw_image *x, const unsigned char *b, size_t n)
 	return 0;
 }
 
+/* ---- CSV and TXT: one image row per line, samples separated by commas
+ * (CSV) or spaces (TXT); height = newlines, width = separators / height + 1,
+ * samples parsed in order, any missing ones 0 (iio.c:2992-3071) */
+static int read_text(raw_image *x, const unsigned char *b, size_t n, char sep)
+{
+	size_t h = 0, ns = 0;
+	for (size_t i = 0; i < n; i++) {
+		h += b[i] == '\n';
+		ns += b[i] == (unsigned char)sep;
+	}
+	if (h == 0) return 1;
+	const size_t w = ns / h + 1;
+	char *s = xcalloc(n + 1, 1);
+	x->v = xcalloc(w * h, sizeof(double));
+	if (!s || !x->v) { free(s); return 2; }
+	memcpy(s, b, n);
+	const char delim[3] = {sep, '\n', 0};
+	char *save = NULL, *tok = strtok_r(s, delim, &save);
+	for (size_t k = 0; k < w * h && tok; k++, tok = strtok_r(NULL, delim, &save)) x->v[k] = (float)atof(tok);
+	free(s);
+	x->w = (int)w; x->h = (int)h; x->pd = 1; x->type = T_F32;
+	return 0;
+}
+
+/* The text formats as iio tells them apart (iio.c:5260-5300, 5347-5400): on
+ * the first 256 bytes (all of a shorter file), CSV when every byte is a
+ * digit, ".e+-,", "naifNAIF" or a newline; else, when every byte is a digit,
+ * ".eE+- ", "naifNAIF" or a newline, TXT when the first line does not hold
+ * exactly three spaces or the second holds as many, else ASC when the first
+ * line is "w h 1 pd".  0 = none of them. */
+enum { TXT_NONE, TXT_CSV, TXT_TXT, TXT_ASC };
+static int text_format(const unsigned char *b, size_t n)
+{
+	const size_t m = n < 256 ? n : 256;
+	char head[257] = {0};
+	memcpy(head, b, m);
+	if (strspn(head, "0123456789.e+-,naifNAIF\n") == m) return TXT_CSV;
+	if (strspn(head, "0123456789.eE+- naifNAIF\n") != m) return TXT_NONE;
+	int a = 0, c = 0;
+	size_t i = 0;
+	for (; i < m && head[i] != '\n'; i++) a += head[i] == ' ';
+	for (i++; i < m && head[i] != '\n'; i++) c += head[i] == ' ';
+	if (a != 3 || a == c) return TXT_TXT;
+	int t[4];
+	if (sscanf(head, "%d %d %d %d", t, t + 1, t + 2, t + 3) == 4 && t[2] == 1) return TXT_ASC;
+	return TXT_NONE;
+}
+
 /* iio's semantic names (iio.c:5604-5633): "zero:WxH[,pd]" and "one:WxH[,pd]"
  * (byte samples), "constant:V:WxH" (one float channel); 1 when `name` is
  * one (x filled, or a message on a malformed one), 0 otherwise. */
@@ -549,13 +597,11 @@ static int read_core(const char *name, raw_image *x)
 	else if (n >= 2 && b[0] == 'P' && (b[1] == 'f' || b[1] == 'F')) r = read_pfm(x, b, n);
 	else if (n >= 2 && b[0] == 'P' && strchr("2356", b[1])) r = read_pnm(x, b, n);
 	else {
-		int t[4];
-		char head[256] = {0};
-		memcpy(head, b, n < 255 ? n : 255);
-		if (sscanf(head, "%d %d %d %d", t, t + 1, t + 2, t + 3) == 4 && t[2] == 1)
-			r = read_asc(x, b, n);
-		else
-			fprintf(stderr, "imageio: unrecognized format of \"%s\"\n", name);
+		const int tf = text_format(b, n);
+		if (tf == TXT_CSV) r = read_text(x, b, n, ',');
+		else if (tf == TXT_TXT) r = read_text(x, b, n, ' ');
+		else if (tf == TXT_ASC) r = read_asc(x, b, n);
+		else fprintf(stderr, "imageio: unrecognized format of \"%s\"\n", name);
 	}
 	free(b);
 	if (r) fprintf(stderr, "imageio: could not read image \"%s\"\n", name);

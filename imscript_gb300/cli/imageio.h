@@ -10,8 +10,9 @@
  *    list as well (iio.c:3796-3884, 5677-5705): flips and reorientations,
  *    trims (negative ones pad with NaN), a pipe through a shell command;
  *  - the input format is sniffed from the first bytes: NumPy .npy (1.0,
- *    every numeric dtype), PFM ("Pf"/"PF"), PNM ("P2","P3","P5","P6") and the
- *    ASC text format ("w h 1 pd" header, planar samples);
+ *    every numeric dtype), PFM ("Pf"/"PF"), PNM ("P2","P3","P5","P6"), and
+ *    the text formats told apart as iio does -- CSV and TXT (one row per
+ *    line, commas or spaces) and ASC ("w h 1 pd" header, planar samples);
  *  - the output format follows the file-name suffix: .pfm (1 or 3 channels),
  *    .ppm/.pgm (1 or 3 channels, ASCII integers), .asc, .npy; any other name,
  *    and a stdout that is not a terminal, get NumPy .npy.  A terminal stdout

@@ -16,6 +16,7 @@ environment the reference ran with, and its planar output ``out``.
               GPU solver must agree within 1e-4 relative max-abs.
 * ``trans.json`` iio's transformations on reading (IIO_TRANS, TRANS[...]:)
               applied by the reference command to an all-known image.
+* ``text.json`` CSV / TXT / ASC-looking text images as the reference reads them.
 * ``amle_*``  the reference ``amle`` (src/amle.c) on one channel: neighbourhood
               sizes (AMLE_NN), iteration counts (AMLE_NITER), a mask file, an
               AMLE_INIT start image, all-known, all-NaN and 1-pixel images.
@@ -257,6 +258,37 @@ def trans_cases():
     return len(res["env"]) + len(res["prefix"])
 
 
+def text_cases():
+    """Text images as the reference command reads them (CSV, TXT, and a TXT
+    whose first line looks like an ASC header), all-known, nothing to fill,
+    written as npy (tests/golden/text.json).  Every file is at least 256
+    bytes: the reference's format sniffing reads that many."""
+    import subprocess
+    import tempfile
+    rng = np.random.default_rng(31)
+    a = (rng.standard_normal((9, 7)) * 50).astype(np.float32)
+    files = {
+        "csv": "\n".join(",".join(f"{v:.6g}" for v in row) for row in a) + "\n",
+        "txt": "\n".join(" ".join(f"{v:.6g}" for v in row) for row in a) + "\n",
+        "txt_like_asc": "3 5 1 2\n" + "\n".join(" ".join(f"{v:.5g}" for v in row[:4]) for row in a) + "\n",
+        "csv_exp": "\n".join(",".join(f"{v:.3e}" for v in row) for row in a) + "\n",
+        "txt_uneven": "\n".join(" ".join(f"{v:.6g}" for v in row[: 7 - (k % 2)]) for k, row in enumerate(a)) + "\n",
+    }
+    res = {}
+    with tempfile.TemporaryDirectory() as td:
+        o = os.path.join(td, "o.npy")
+        for k, text in files.items():
+            assert len(text) >= 256, (k, len(text))
+            src = os.path.join(td, k)
+            open(src, "w").write(text)
+            subprocess.run([O.REF_BIN, "-i", src, "-n", "0", "-o", o], check=True, capture_output=True)
+            out = np.load(o)
+            res[k] = {"text": text, "shape": list(out.shape), "out": out.ravel().tolist()}
+    with open(os.path.join(OUT, "text.json"), "w") as fh:
+        json.dump(res, fh)
+    return len(res)
+
+
 def mini_cases(rng):
     """The GS-only copy of the ftr viewers (ftr/minisimpois.c) from its own main."""
     k = 0
@@ -344,6 +376,9 @@ def amle_cli_cases():
 def main():
     if not O.have_reference():
         O.build(reference=True)
+    if sys.argv[1:] == ["text"]:
+        print(f"wrote {text_cases()} text-format cases into {OUT}")
+        return
     if sys.argv[1:] == ["trans"]:
         print(f"wrote {trans_cases()} transformation cases into {OUT}")
         return
@@ -358,7 +393,7 @@ def main():
     n4 = io_cases()
     n5 = mini_cases(np.random.default_rng(4242))
     n6 = amle_cases(np.random.default_rng(5150)) + amle_cli_cases()
-    n7 = trans_cases()
+    n7 = trans_cases() + text_cases()
     print(f"wrote {n1} pin cases, {n2} converged cases, {n3} CLI cases, {n4} I/O cases, "
           f"{n5} minisimpois cases, {n6} AMLE cases and {n7} transformation cases into {OUT}")
 

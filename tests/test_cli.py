@@ -267,3 +267,26 @@ def test_iio_trans_errors(harness, tmp_path):
     got = _read_with(harness, tmp_path, src, "pipe=false")
     d = _fixtures("trans.json")
     assert np.array_equal(got, np.array(d["in"], np.float32).reshape(d["shape"]))
+
+
+@pytest.mark.parametrize("key", json.load(open(os.path.join(GOLDEN, "text.json"))).keys())
+def test_text_formats_match_reference(harness, tmp_path, key):
+    """CSV, TXT and an ASC-looking TXT read as the reference reads them
+    (iio.c:2992-3071, 5260-5400)."""
+    d = _fixtures("text.json")[key]
+    src = str(tmp_path / key)
+    open(src, "w").write(d["text"])
+    got = _read_with(harness, tmp_path, src, "")
+    assert list(got.shape) == d["shape"]
+    assert np.array_equal(got.view(np.uint32), np.array(d["out"], np.float32).reshape(d["shape"]).view(np.uint32))
+
+
+@pytest.mark.parametrize("ext", ["csv", "txt", "asc"])
+def test_text_writers_read_back(harness, tmp_path, ext):
+    rng = np.random.default_rng(3)
+    a = (rng.standard_normal((12, 9, 1)) * 30).astype(np.float32)
+    src, dst, back = str(tmp_path / "a.npy"), str(tmp_path / f"a.{ext}"), str(tmp_path / "b.npy")
+    np.save(src, a)
+    subprocess.run([harness, "write", src, dst], check=True)
+    subprocess.run([harness, "read", dst, back], check=True)
+    assert np.array_equal(np.load(back).reshape(a.shape), a)
