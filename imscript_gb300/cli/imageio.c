@@ -472,6 +472,164 @@ static int flip(raw_image *x, const char *s)
 
 static int read_core(const char *name, raw_image *x);
 
+/* ---- RAW: headerless binary samples described by a list of one-letter
+ * fields, "RAW[w640,h480,p3,tuint16,e1]:file" or the IIO_RAW variable
+ * (iio.c:3597-3777).  w, h, p (or d): sizes; o: header bytes; t: sample
+ * type; e: swap bytes; i, y: image index and bytes between images; r: two-
+ * letter orientation; b: ignored.  A value "@pos[/size]" is an integer read
+ * from the file at byte pos (size 1, 2, 4 unsigned, negative signed; -4 by
+ * default).  Missing sizes and offset are estimated from the file size. */
+static int raw_type(const char *t, int *type, int *ss)
+{
+	char u[16] = {0};
+	for (int i = 0; t[i] && i < 15; i++) u[i] = (char)toupper((unsigned char)t[i]);
+	static const struct { const char *n; int t, s; } tab[] = {
+		{"INT8", T_I8, 1}, {"UINT8", T_U8, 1}, {"CHAR", T_U8, 1}, {"INT16", T_I16, 2}, {"SHORT", T_I16, 2},
+		{"UINT16", T_U16, 2}, {"INT32", T_I32, 4}, {"INT", T_I32, 4}, {"UINT32", T_U32, 4},
+		{"INT64", T_I64, 8}, {"LONG", T_I64, 8}, {"LONGLONG", T_I64, 8}, {"UINT64", T_U64, 8},
+		{"FLOAT", T_F32, 4}, {"DOUBLE", T_F64, 8}};
+	for (size_t k = 0; k < sizeof tab / sizeof *tab; k++)
+		if (!strcmp(u, tab[k].n)) {
+			*type = tab[k].t;
+			*ss = tab[k].s;
+			return 0;
+		}
+	fprintf(stderr, "imageio: unrecognized typename \"%s\"\n", t);
+	return 1;
+}
+
+static void swap_bytes(unsigned char *p, size_t words, int size)
+{
+	for (size_t k = 0; k < words; k++, p += size)
+		for (int a = 0, b = size - 1; a < b; a++, b--) {
+			unsigned char t = p[a];
+			p[a] = p[b];
+			p[b] = t;
+		}
+}
+
+/* an integer field of the file (the reference swaps it in place) */
+static int raw_field(unsigned char *d, size_t n, const char *tok, int swap, int *v)
+{
+	int pos, size = -4;
+	if (sscanf(tok, "%d/%d", &pos, &size) != 2 && sscanf(tok, "%d", &pos) != 1) {
+		*v = 0;
+		return 0;
+	}
+	const int as = size < 0 ? -size : size;
+	if (pos < 0 || (size_t)(as + pos) > n || (as != 1 && as != 2 && as != 4)) {
+		fprintf(stderr, "imageio: can not read field beyond data size\n");
+		return 1;
+	}
+	unsigned char *p = d + pos;
+	if (swap && as > 1) swap_bytes(p, 1, as);
+	uint32_t u = 0;
+	memcpy(&u, p, as);   /* little-endian host */
+	switch (size) {
+	case 1: *v = (uint8_t)u; break;
+	case 2: *v = (uint16_t)u; break;
+	case 4: *v = (int)u; break;
+	case -1: *v = (int8_t)u; break;
+	case -2: *v = (int16_t)u; break;
+	default: *v = (int32_t)u; break;
+	}
+	return 0;
+}
+
+static int read_raw_spec(const char *spec, const char *file, raw_image *x)
+{
+	FILE *f = strcmp(file, "-") ? fopen(file, "rb") : stdin;
+	if (!f) {
+		fprintf(stderr, "imageio: can not open file \"%s\" in mode \"r\"\n", file);
+		return 1;
+	}
+	size_t n = 0;
+	unsigned char *d = slurp(f, &n);
+	if (f != stdin) fclose(f);
+	if (!d) return 1;
+	char *desc = malloc(strlen(spec) + 1);
+	if (!desc) { free(d); return 1; }
+	strcpy(desc, spec);
+	long w = -1, h = -1, pd = 1, off = -1, index = 0, frame = 0;
+	int swap = 0, type = T_U8, ss = 1, orient = 0, r = 0;
+	for (char *tok = desc; tok && !r;) {
+		char *next = strchr(tok, ',');
+		if (next) *next++ = 0;
+		if (*tok) {
+			int v = 0;
+			if (tok[1] == '@') r = raw_field(d, n, tok + 2, swap, &v);
+			else v = atoi(tok + 1);
+			switch (*tok) {
+			case 'w': w = v; break;
+			case 'h': h = v; break;
+			case 'd': case 'p': pd = v; break;
+			case 'o': off = v; break;
+			case 'e': swap = v; break;
+			case 'i': index = v; break;
+			case 'y': frame = v; break;
+			case 't': r = raw_type(tok + 1, &type, &ss); break;
+			case 'r': orient = tok[1] ? tok[1] + 256 * tok[2] : 0; break;
+			default: break;
+			}
+		}
+		tok = next;
+	}
+	free(desc);
+	if (r) { free(d); return r; }
+	const long fs = (long)n, px = pd * ss;
+	if (off < 0 && w > 0 && h > 0) off = fs - w * h * px;
+	if (w < 0 && off > 0 && h > 0) w = (fs - off) / (h * px);
+	if (h < 0 && off > 0 && w > 0) h = (fs - off) / (w * px);
+	if (off < 0) off = 0;
+	if (h < 0 && w > 0) h = fs / (w * px);
+	if (w < 0 && h > 0) w = fs / (h * px);
+	if (off < 0 || w <= 0 || h <= 0 || pd <= 0) {
+		fprintf(stderr, "imageio: could not determine width, height and offset (got %ld,%ld,%ld)\n", w, h, off);
+		free(d);
+		return 1;
+	}
+	off += frame + index * (frame + w * h * px);
+	const size_t ns = (size_t)w * h * pd;
+	if ((size_t)off + ns * ss > n) {
+		fprintf(stderr, "imageio: raw file is not large enough\n");
+		free(d);
+		return 1;
+	}
+	unsigned char *p = d + off;
+	/* the reference swaps 2-byte samples, and 4-byte words -- one per
+	 * sample, so only the first half of 8-byte samples -- for wider ones */
+	if (swap && ss == 2) swap_bytes(p, ns, 2);
+	if (swap && ss >= 4) swap_bytes(p, ns, 4);
+	x->v = xcalloc(ns, sizeof(double));
+	if (!x->v) { free(d); return 1; }
+	for (size_t k = 0; k < ns; k++) {
+		const unsigned char *q = p + k * ss;
+		switch (type) {
+		case T_U8: x->v[k] = q[0]; break;
+		case T_I8: x->v[k] = (int8_t)q[0]; break;
+		case T_U16: { uint16_t v; memcpy(&v, q, 2); x->v[k] = v; break; }
+		case T_I16: { int16_t v; memcpy(&v, q, 2); x->v[k] = v; break; }
+		case T_U32: { uint32_t v; memcpy(&v, q, 4); x->v[k] = v; break; }
+		case T_I32: { int32_t v; memcpy(&v, q, 4); x->v[k] = v; break; }
+		case T_U64: { uint64_t v; memcpy(&v, q, 8); x->v[k] = (double)v; break; }
+		case T_I64: { int64_t v; memcpy(&v, q, 8); x->v[k] = (double)v; break; }
+		case T_F32: { float v; memcpy(&v, q, 4); x->v[k] = v; break; }
+		default: { double v; memcpy(&v, q, 8); x->v[k] = v; break; }
+		}
+	}
+	free(d);
+	x->w = (int)w; x->h = (int)h; x->pd = (int)pd; x->type = type;
+	return orient ? reorient(x, orient & 0xff, orient >> 8) : 0;
+}
+
+/* "RAW[spec]:name" (iio.c:3597-3605): the colon after the closing bracket */
+static const char *raw_prefix(const char *name)
+{
+	if (name != strstr(name, "RAW[")) return NULL;
+	const char *colon = strchr(name, ':');
+	return colon && colon[-1] == ']' ? colon : NULL;
+}
+
 /* Filter the image through a shell command: the image goes to the command's
  * standard input as a file, its standard output is read back as the image,
  * IIO_TRANS unset for it (iio.c:3826-3852); a command that fails leaves the
@@ -567,10 +725,21 @@ static int read_raw(const char *name, raw_image *x)
 {
 	int rc;
 	if (semantic_name(name, x, &rc)) return rc;
-	const char *colon = trans_prefix(name);
+	const char *colon = trans_prefix(name), *rcolon = raw_prefix(name);
+	const char *iio_raw = getenv("IIO_RAW");
 	if (colon) {
 		rc = read_raw(colon + 1, x);
 		if (!rc) rc = trans_apply(x, name + 6);
+	} else if (rcolon) {
+		const size_t len = (size_t)(rcolon - name) - 5;   /* between "RAW[" and "]:" */
+		char *spec = malloc(len + 1);
+		if (!spec) return 1;
+		memcpy(spec, name + 4, len);
+		spec[len] = 0;
+		rc = read_raw_spec(spec, rcolon + 1, x);
+		free(spec);
+	} else if (iio_raw && strcmp(name, "-")) {
+		rc = read_raw_spec(iio_raw, name, x);   /* IIO_RAW: every file is raw (iio.c:3777-3795) */
 	} else {
 		rc = read_core(name, x);
 	}
@@ -593,7 +762,8 @@ static int read_core(const char *name, raw_image *x)
 	if (f != stdin) fclose(f);
 	if (!b) return 1;
 	int r = 1;
-	if (n >= 4 && b[0] == 0x93 && b[1] == 'N' && b[2] == 'U' && b[3] == 'M') r = read_npy(x, b, n);
+	if (getenv("IIO_TXT")) r = read_text(x, b, n, ' ');   /* IIO_TXT: every file is TXT */
+	else if (n >= 4 && b[0] == 0x93 && b[1] == 'N' && b[2] == 'U' && b[3] == 'M') r = read_npy(x, b, n);
 	else if (n >= 2 && b[0] == 'P' && (b[1] == 'f' || b[1] == 'F')) r = read_pfm(x, b, n);
 	else if (n >= 2 && b[0] == 'P' && strchr("2356", b[1])) r = read_pnm(x, b, n);
 	else {

@@ -9,6 +9,10 @@
  *    transformations in IIO_TRANS, and a name "TRANS[list]:file" gets that
  *    list as well (iio.c:3796-3884, 5677-5705): flips and reorientations,
  *    trims (negative ones pad with NaN), a pipe through a shell command;
+ *  - "RAW[fields]:file" reads headerless binary samples (sizes, header,
+ *    type, byte swap, orientation, image index, fields read from the file),
+ *    and so does every file while IIO_RAW holds the fields; IIO_TXT reads
+ *    every file as TXT (iio.c:3597-3795, 5164-5180);
  *  - the input format is sniffed from the first bytes: NumPy .npy (1.0,
  *    every numeric dtype), PFM ("Pf"/"PF"), PNM ("P2","P3","P5","P6"), and
  *    the text formats told apart as iio does -- CSV and TXT (one row per

@@ -17,6 +17,8 @@ environment the reference ran with, and its planar output ``out``.
 * ``trans.json`` iio's transformations on reading (IIO_TRANS, TRANS[...]:)
               applied by the reference command to an all-known image.
 * ``text.json`` CSV / TXT / ASC-looking text images as the reference reads them.
+* ``raw.json``  headerless binary images (RAW[...]:file, IIO_RAW) as the reference
+              reads them.
 * ``amle_*``  the reference ``amle`` (src/amle.c) on one channel: neighbourhood
               sizes (AMLE_NN), iteration counts (AMLE_NITER), a mask file, an
               AMLE_INIT start image, all-known, all-NaN and 1-pixel images.
@@ -289,6 +291,51 @@ def text_cases():
     return len(res)
 
 
+def raw_cases():
+    """Headerless binary images named RAW[...]:file, and read through
+    IIO_RAW, as the reference command reads them (all-known, nothing to
+    fill, written as npy: tests/golden/raw.json)."""
+    import subprocess
+    import tempfile
+    rng = np.random.default_rng(17)
+    f32 = (rng.standard_normal(7 * 5) * 40).astype("<f4").tobytes()
+    u8 = rng.integers(0, 256, 7 * 5 * 3, dtype=np.uint8).tobytes()
+    u16be = rng.integers(0, 65536, 6 * 4, dtype=np.uint16).astype(">u2").tobytes()
+    i16 = bytes(range(16)) + rng.integers(-3000, 3000, 4 * 3, dtype=np.int16).astype("<i2").tobytes()
+    i32 = bytes(8) + rng.integers(-99999, 99999, 6 * 5, dtype=np.int32).astype("<i4").tobytes()
+    f64 = (rng.standard_normal(5 * 4 * 2) * 9).astype("<f8").tobytes()
+    stack = (rng.standard_normal(3 * 2 * 3) * 5).astype("<f4").tobytes()
+    fields = np.array([6, 5], "<u2").tobytes() + bytes(4) + rng.integers(0, 256, 30, dtype=np.uint8).tobytes()
+    f32be = (rng.standard_normal(4 * 3) * 7).astype(">f4").tobytes()
+    cases = [("f32", "w7,h5,tfloat", f32), ("u8_rgb", "w7,h5,p3,tuint8", u8),
+             ("u16_be_h_estimated", "w6,tuint16,e1", u16be), ("i16_header", "w4,h3,o16,tint16", i16),
+             ("i32_w_estimated", "h5,o8,tint32", i32), ("f64_2ch", "w5,h4,p2,tdouble", f64),
+             ("u8_orient", "w7,h5,p3,tUINT8,rYx", u8), ("f32_stack_index", "w3,h2,o0,tfloat,i2", stack),
+             ("fields_from_file", "w@0/2,h@2/2,o8,tuint8", fields), ("f32_be", "w4,h3,tfloat,e1", f32be)]
+    res = {}
+    with tempfile.TemporaryDirectory() as td:
+        o = os.path.join(td, "o.npy")
+        env0 = {k: v for k, v in os.environ.items() if k not in ("IIO_RAW", "IIO_TRANS", "IIO_TXT")}
+        for key, spec, data in cases:
+            src = os.path.join(td, key + ".bin")
+            open(src, "wb").write(data)
+            subprocess.run([O.REF_BIN, "-i", f"RAW[{spec}]:{src}", "-n", "0", "-o", o], check=True,
+                           capture_output=True, env=env0)
+            out = np.load(o)
+            res[key] = {"spec": spec, "data": list(data), "shape": list(out.shape), "out": out.ravel().tolist()}
+        # IIO_RAW: a plain file name read as raw
+        src = os.path.join(td, "plain.bin")
+        open(src, "wb").write(f32)
+        subprocess.run([O.REF_BIN, "-i", src, "-n", "0", "-o", o], check=True, capture_output=True,
+                       env=dict(env0, IIO_RAW="w5,h7,tfloat"))
+        out = np.load(o)
+        res["iio_raw_env"] = {"spec": "", "env": "w5,h7,tfloat", "data": list(f32), "shape": list(out.shape),
+                              "out": out.ravel().tolist()}
+    with open(os.path.join(OUT, "raw.json"), "w") as fh:
+        json.dump(res, fh)
+    return len(res)
+
+
 def mini_cases(rng):
     """The GS-only copy of the ftr viewers (ftr/minisimpois.c) from its own main."""
     k = 0
@@ -376,6 +423,9 @@ def amle_cli_cases():
 def main():
     if not O.have_reference():
         O.build(reference=True)
+    if sys.argv[1:] == ["raw"]:
+        print(f"wrote {raw_cases()} raw-image cases into {OUT}")
+        return
     if sys.argv[1:] == ["text"]:
         print(f"wrote {text_cases()} text-format cases into {OUT}")
         return
@@ -393,7 +443,7 @@ def main():
     n4 = io_cases()
     n5 = mini_cases(np.random.default_rng(4242))
     n6 = amle_cases(np.random.default_rng(5150)) + amle_cli_cases()
-    n7 = trans_cases() + text_cases()
+    n7 = trans_cases() + text_cases() + raw_cases()
     print(f"wrote {n1} pin cases, {n2} converged cases, {n3} CLI cases, {n4} I/O cases, "
           f"{n5} minisimpois cases, {n6} AMLE cases and {n7} transformation cases into {OUT}")
 

@@ -290,3 +290,32 @@ def test_text_writers_read_back(harness, tmp_path, ext):
     subprocess.run([harness, "write", src, dst], check=True)
     subprocess.run([harness, "read", dst, back], check=True)
     assert np.array_equal(np.load(back).reshape(a.shape), a)
+
+
+@pytest.mark.parametrize("key", json.load(open(os.path.join(GOLDEN, "raw.json"))).keys())
+def test_raw_images_match_reference(harness, tmp_path, key):
+    """Headerless binary images, RAW[fields]:file or IIO_RAW (iio.c:3597-3795):
+    sizes, header, sample types, byte swaps, orientation, image index and
+    fields read from the file, as the reference reads them."""
+    d = _fixtures("raw.json")[key]
+    src = str(tmp_path / "img.bin")
+    open(src, "wb").write(bytes(d["data"]))
+    dst = str(tmp_path / "o.npy")
+    env = {k: v for k, v in os.environ.items() if k not in ("IIO_RAW", "IIO_TRANS", "IIO_TXT")}
+    if d.get("env"):
+        env["IIO_RAW"] = d["env"]
+        name = src
+    else:
+        name = f"RAW[{d['spec']}]:{src}"
+    subprocess.run([harness, "read", name, dst], check=True, env=env)
+    got = np.load(dst)
+    assert list(got.shape) == d["shape"]
+    assert np.array_equal(got.view(np.uint32), np.array(d["out"], np.float32).reshape(d["shape"]).view(np.uint32))
+
+
+def test_raw_too_small_fails(harness, tmp_path):
+    src = str(tmp_path / "img.bin")
+    open(src, "wb").write(bytes(10))
+    r = subprocess.run([harness, "read", f"RAW[w4,h4,tfloat,o0]:{src}", str(tmp_path / "o.npy")],
+                       capture_output=True, text=True)
+    assert r.returncode != 0 and "not large enough" in r.stderr
