@@ -232,6 +232,50 @@ static int read_asc(raw_image *x, const unsigned char *b, size_t n)
 	return 0;
 }
 
+/* ---- FLO (Middlebury flow: "PIEH", width, height, interleaved float
+ * pairs) and JUV ("#UV {" text header padded to 255 bytes, then the u plane
+ * and the v plane), 2 channels (iio.c:2619-2654) */
+static int read_flo(raw_image *x, const unsigned char *b, size_t n)
+{
+	uint32_t w, h;
+	if (n < 12) return 1;
+	memcpy(&w, b + 4, 4);
+	memcpy(&h, b + 8, 4);
+	const size_t ns = (size_t)w * h * 2;
+	if (n < 12 + 4 * ns) return 1;
+	x->v = xcalloc(ns, sizeof(double));
+	if (!x->v) return 2;
+	for (size_t k = 0; k < ns; k++) {
+		float v;
+		memcpy(&v, b + 12 + 4 * k, 4);
+		x->v[k] = v;
+	}
+	x->w = (int)w; x->h = (int)h; x->pd = 2; x->type = T_F32;
+	return 0;
+}
+
+static int read_juv(raw_image *x, const unsigned char *b, size_t n)
+{
+	char head[256] = {0};
+	int w, h;
+	if (n < 255) return 1;
+	memcpy(head, b, 255);
+	if (sscanf(head, "#UV {\n dimx %d dimy %d\n}\n", &w, &h) != 2 || w <= 0 || h <= 0) return 1;
+	const size_t np = (size_t)w * h;
+	if (n < 255 + 8 * np) return 1;
+	x->v = xcalloc(2 * np, sizeof(double));
+	if (!x->v) return 2;
+	for (size_t i = 0; i < np; i++) {
+		float u, v;
+		memcpy(&u, b + 255 + 4 * i, 4);
+		memcpy(&v, b + 255 + 4 * (np + i), 4);
+		x->v[2 * i] = u;
+		x->v[2 * i + 1] = v;
+	}
+	x->w = w; x->h = h; x->pd = 2; x->type = T_F32;
+	return 0;
+}
+
 /* ---- CSV and TXT: one image row per line, samples separated by commas
  * (CSV) or spaces (TXT); height = newlines, width = separators / height + 1,
  * samples parsed in order, any missing ones 0 (iio.c:2992-3071) */
@@ -766,6 +810,8 @@ static int read_core(const char *name, raw_image *x)
 	else if (n >= 4 && b[0] == 0x93 && b[1] == 'N' && b[2] == 'U' && b[3] == 'M') r = read_npy(x, b, n);
 	else if (n >= 2 && b[0] == 'P' && (b[1] == 'f' || b[1] == 'F')) r = read_pfm(x, b, n);
 	else if (n >= 2 && b[0] == 'P' && strchr("2356", b[1])) r = read_pnm(x, b, n);
+	else if (n >= 4 && !memcmp(b, "PIEH", 4)) r = read_flo(x, b, n);
+	else if (n >= 3 && !memcmp(b, "#UV", 3)) r = read_juv(x, b, n);
 	else {
 		const int tf = text_format(b, n);
 		if (tf == TXT_CSV) r = read_text(x, b, n, ',');
@@ -844,9 +890,39 @@ static int close_out(FILE *f)
 	return fclose(f) ? 1 : 0;
 }
 
+/* one row of w samples a line ("%.9g", spaces); a single row or column of
+ * pd-vectors one pixel a line (iio.c:4277-4304) */
+static void write_txt(FILE *f, const float *v, int w, size_t ns, int pd)
+{
+	const size_t rw = pd == 1 ? (size_t)w : (size_t)pd;
+	for (size_t k = 0; k < ns; k++) fprintf(f, "%.9g%c", v[k], (k + 1) % rw ? ' ' : '\n');
+}
+
 int imgio_write_split(const char *name, const float *x, int w, int h, int pd)
 {
 	size_t np = (size_t)w * h, ns = np * pd;
+	/* "TXT:name" and "RAW:name" (iio.c:6292-6307) */
+	const int txt_prefix = name == strstr(name, "TXT:"), raw_prefix_w = name == strstr(name, "RAW:");
+	if ((txt_prefix || raw_prefix_w) && strlen(name) > 4) {
+		if (txt_prefix && !(pd == 1 || w == 1 || h == 1)) {
+			fprintf(stderr, "imageio: TXT needs one channel, or one row or column\n");
+			return 1;
+		}
+		float *v = malloc(sizeof(float) * (ns ? ns : 1));
+		if (!v) return 1;
+		for (size_t i = 0; i < np; i++)
+			for (int l = 0; l < pd; l++) v[i * pd + l] = x[np * l + i];
+		FILE *f = open_out(name + 4);
+		int rc = !f;
+		if (f) {
+			if (txt_prefix) write_txt(f, v, w, ns, pd);
+			else rc = fwrite(v, sizeof(float), ns, f) != ns;
+			rc |= close_out(f);
+		}
+		free(v);
+		if (rc) fprintf(stderr, "imageio: error writing \"%s\"\n", name + 4);
+		return rc;
+	}
 	if (!strcmp(name, "-") && isatty(1)) {
 		printf("IMAGE %dx%d,%d float\n", w, h, pd);
 		return 0;
@@ -858,7 +934,19 @@ int imgio_write_split(const char *name, const float *x, int w, int h, int pd)
 	int rc = 0;
 	FILE *f = open_out(name);
 	if (!f) { free(v); return 1; }
-	if ((suffix(name, ".pfm")) && (pd == 1 || pd == 3)) {
+	if (suffix(name, ".uv") && pd == 2) {
+		/* JUV: a 255-byte text header (the text, its NUL, spaces), u, v */
+		char head[255];
+		memset(head, ' ', sizeof head);
+		snprintf(head, sizeof head, "#UV {\n dimx %d dimy %d\n}\n", w, h);
+		rc = fwrite(head, 1, 255, f) != 255;
+		rc |= fwrite(x, sizeof(float), ns, f) != ns;   /* the planes: u then v */
+	} else if (suffix(name, ".flo") && pd == 2) {
+		const uint32_t dims[2] = {(uint32_t)w, (uint32_t)h};
+		rc = fwrite("PIEH", 1, 4, f) != 4;
+		rc |= fwrite(dims, 4, 2, f) != 2;
+		rc |= fwrite(v, sizeof(float), ns, f) != ns;
+	} else if ((suffix(name, ".pfm")) && (pd == 1 || pd == 3)) {
 		fprintf(f, "P%c\n%d %d\n%g\n", pd > 1 ? 'F' : 'f', w, h, -1.0);
 		rc = fwrite(v, sizeof(float), ns, f) != ns;
 	} else if ((suffix(name, ".ppm") || suffix(name, ".pgm")) && (pd == 1 || pd == 3)) {
@@ -867,10 +955,9 @@ int imgio_write_split(const char *name, const float *x, int w, int h, int pd)
 	} else if (suffix(name, ".csv") && pd == 1) {
 		for (size_t k = 0; k < ns; k++) fprintf(f, "%.9g%c", v[k], (k + 1) % w ? ',' : '\n');
 	} else if (suffix(name, ".txt") && (pd == 1 || w == 1 || h == 1)) {
-		/* rows of w samples; a single row or column of pd-vectors is
-		 * written one pixel per line */
-		size_t rw = pd == 1 ? (size_t)w : (size_t)pd;
-		for (size_t k = 0; k < ns; k++) fprintf(f, "%.9g%c", v[k], (k + 1) % rw ? ' ' : '\n');
+		write_txt(f, v, w, ns, pd);
+	} else if (suffix(name, ".raw")) {
+		rc = fwrite(v, sizeof(float), ns, f) != ns;   /* the samples, interleaved */
 	} else if (suffix(name, ".asc")) {
 		fprintf(f, "%d %d 1 %d\n", w, h, pd);
 		for (size_t k = 0; k < ns; k++) fprintf(f, "%.9g\n", x[k]);   /* planar */

@@ -17,10 +17,12 @@
  *    every numeric dtype), PFM ("Pf"/"PF"), PNM ("P2","P3","P5","P6"), and
  *    the text formats told apart as iio does -- CSV and TXT (one row per
  *    line, commas or spaces) and ASC ("w h 1 pd" header, planar samples);
- *  - the output format follows the file-name suffix: .pfm (1 or 3 channels),
- *    .ppm/.pgm (1 or 3 channels, ASCII integers), .asc, .npy; any other name,
- *    and a stdout that is not a terminal, get NumPy .npy.  A terminal stdout
- *    gets the one-line "IMAGE wxh,pd float" summary.
+ *  - the output format follows the file-name suffix: .uv and .flo (2
+ *    channels), .pfm (1 or 3 channels), .ppm/.pgm (1 or 3 channels, ASCII
+ *    integers), .csv, .txt, .raw (the samples, interleaved), .asc, .npy, or
+ *    the prefixes "TXT:" and "RAW:"; any other name, and a stdout that is not
+ *    a terminal, get NumPy .npy.  A terminal stdout gets the one-line
+ *    "IMAGE wxh,pd float" summary.  FLO and JUV (.uv) files are read too.
  *
  * Errors print a message and return NULL / nonzero; nothing exits.
  */

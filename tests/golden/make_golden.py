@@ -19,6 +19,8 @@ environment the reference ran with, and its planar output ``out``.
 * ``text.json`` CSV / TXT / ASC-looking text images as the reference reads them.
 * ``raw.json``  headerless binary images (RAW[...]:file, IIO_RAW) as the reference
               reads them.
+* ``io_more.json`` the .uv, .flo, .raw, TXT: and RAW: writers, byte for byte,
+              and the reading of .flo and .uv.
 * ``amle_*``  the reference ``amle`` (src/amle.c) on one channel: neighbourhood
               sizes (AMLE_NN), iteration counts (AMLE_NITER), a mask file, an
               AMLE_INIT start image, all-known, all-NaN and 1-pixel images.
@@ -336,6 +338,42 @@ def raw_cases():
     return len(res)
 
 
+def io_more_cases():
+    """Writers the reference command picks by name -- .uv and .flo (two
+    channels), .raw, the TXT: and RAW: prefixes -- byte for byte, and its
+    reading back of .flo and .uv (tests/golden/io_more.json)."""
+    import subprocess
+    import tempfile
+    rng = np.random.default_rng(23)
+    img2 = (rng.standard_normal((5, 6, 2)) * 3).astype(np.float32)
+    img3 = (rng.standard_normal((4, 5, 3)) * 3).astype(np.float32)
+    img1 = (rng.standard_normal((3, 7, 1)) * 3).astype(np.float32)
+    res = {"img2": img2.ravel().tolist(), "img3": img3.ravel().tolist(), "img1": img1.ravel().tolist(),
+           "write": {}, "read": {}}
+    with tempfile.TemporaryDirectory() as td:
+        srcs = {}
+        for tag, a in (("img2", img2), ("img3", img3), ("img1", img1)):
+            srcs[tag] = os.path.join(td, tag + ".npy")
+            np.save(srcs[tag], a)
+        for key, tag, prefix, fname in (("uv", "img2", "", "o.uv"), ("flo", "img2", "", "o.flo"),
+                                        ("raw", "img3", "", "o.raw"), ("txt_prefix", "img1", "TXT:", "o.dat"),
+                                        ("raw_prefix", "img3", "RAW:", "o.bin")):
+            path = os.path.join(td, fname)
+            subprocess.run([O.REF_BIN, "-i", srcs[tag], "-n", "0", "-o", prefix + path], check=True,
+                           capture_output=True)
+            name = prefix + fname
+            res["write"][key] = {"tag": tag, "name": name, "bytes": list(open(path, "rb").read())}
+        for key in ("uv", "flo"):
+            src = os.path.join(td, "o." + key)
+            o = os.path.join(td, "back.npy")
+            subprocess.run([O.REF_BIN, "-i", src, "-n", "0", "-o", o], check=True, capture_output=True)
+            a = np.load(o)
+            res["read"][key] = {"shape": list(a.shape), "out": a.ravel().tolist()}
+    with open(os.path.join(OUT, "io_more.json"), "w") as fh:
+        json.dump(res, fh)
+    return len(res["write"]) + len(res["read"])
+
+
 def mini_cases(rng):
     """The GS-only copy of the ftr viewers (ftr/minisimpois.c) from its own main."""
     k = 0
@@ -423,6 +461,9 @@ def amle_cli_cases():
 def main():
     if not O.have_reference():
         O.build(reference=True)
+    if sys.argv[1:] == ["io_more"]:
+        print(f"wrote {io_more_cases()} writer/reader cases into {OUT}")
+        return
     if sys.argv[1:] == ["raw"]:
         print(f"wrote {raw_cases()} raw-image cases into {OUT}")
         return
@@ -443,7 +484,7 @@ def main():
     n4 = io_cases()
     n5 = mini_cases(np.random.default_rng(4242))
     n6 = amle_cases(np.random.default_rng(5150)) + amle_cli_cases()
-    n7 = trans_cases() + text_cases() + raw_cases()
+    n7 = trans_cases() + text_cases() + raw_cases() + io_more_cases()
     print(f"wrote {n1} pin cases, {n2} converged cases, {n3} CLI cases, {n4} I/O cases, "
           f"{n5} minisimpois cases, {n6} AMLE cases and {n7} transformation cases into {OUT}")
 

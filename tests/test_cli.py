@@ -319,3 +319,31 @@ def test_raw_too_small_fails(harness, tmp_path):
     r = subprocess.run([harness, "read", f"RAW[w4,h4,tfloat,o0]:{src}", str(tmp_path / "o.npy")],
                        capture_output=True, text=True)
     assert r.returncode != 0 and "not large enough" in r.stderr
+
+
+_MORE_SHAPES = {"img2": (5, 6, 2), "img3": (4, 5, 3), "img1": (3, 7, 1)}
+
+
+@pytest.mark.parametrize("key", ["uv", "flo", "raw", "txt_prefix", "raw_prefix"])
+def test_more_writers_match_reference_bytes(harness, tmp_path, key):
+    """.uv and .flo (two channels), .raw, and the TXT: and RAW: name prefixes
+    (iio.c:4110-4148, 4277-4334, 6166-6307), byte for byte."""
+    d = _fixtures("io_more.json")
+    w = d["write"][key]
+    src = str(tmp_path / "src.npy")
+    np.save(src, np.array(d[w["tag"]], np.float32).reshape(_MORE_SHAPES[w["tag"]]))
+    prefix, fname = (w["name"].split(":", 1) + [""])[:2] if ":" in w["name"] else ("", w["name"])
+    path = str(tmp_path / fname)
+    subprocess.run([harness, "write", src, (prefix + ":" if prefix else "") + path], check=True)
+    assert list(open(path, "rb").read()) == w["bytes"]
+
+
+@pytest.mark.parametrize("key", ["uv", "flo"])
+def test_flow_formats_read_like_reference(harness, tmp_path, key):
+    d = _fixtures("io_more.json")
+    src = str(tmp_path / ("in." + key))
+    open(src, "wb").write(bytes(d["write"][key]["bytes"]))
+    got = _read_with(harness, tmp_path, src, "")
+    want = d["read"][key]
+    assert list(got.shape) == want["shape"]
+    assert np.array_equal(got.view(np.uint32), np.array(want["out"], np.float32).reshape(want["shape"]).view(np.uint32))
