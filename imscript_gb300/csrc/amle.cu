@@ -228,6 +228,25 @@ __global__ void __launch_bounds__(SP_THREADS) k_amle_fused(AmleArgs a, const flo
 			// the first nn in-image neighbours in table order, the first
 			// minimum and the first maximum, (a v_min + b v_max) / (a + b)
 			// with a the weight of the maximum and b that of the minimum
+			if (NN == 4 && interior) {
+				// all four neighbours exist: the same first-minimum and
+				// first-maximum scan, in table order (+x, +y, -x, -y),
+				// without the tests
+				const int off[4] = {1, R, -1, -R};
+				float mn0 = zi[q + 1], mx0 = mn0, mn1 = zs[q + 1], mx1 = mn1;
+#pragma unroll
+				for (int p = 1; p < 4; p++) {
+					const int qq = q + off[p];
+					const float v0 = zi[qq], v1 = zs[qq];
+					if (v0 < mn0) mn0 = v0;
+					if (v0 > mx0) mx0 = v0;
+					if (v1 < mn1) mn1 = v1;
+					if (v1 > mx1) mx1 = v1;
+				}
+				zi[q] = __fmul_rn(__fadd_rn(mn0, mx0), 0.5f);
+				zs[q] = __fmul_rn(__fadd_rn(mn1, mx1), 0.5f);
+				continue;
+			}
 			int gi = 0, gj = 0;
 			if (!interior) {
 				const int ry = q / R;
