@@ -228,23 +228,29 @@ __global__ void __launch_bounds__(SP_THREADS) k_amle_fused(AmleArgs a, const flo
 			// the first nn in-image neighbours in table order, the first
 			// minimum and the first maximum, (a v_min + b v_max) / (a + b)
 			// with a the weight of the maximum and b that of the minimum
-			if (NN == 4 && interior) {
-				// all four neighbours exist: the same first-minimum and
-				// first-maximum scan, in table order (+x, +y, -x, -y),
-				// without the tests
-				const int off[4] = {1, R, -1, -R};
+			if ((NN == 4 || NN == 8) && interior) {
+				// every neighbour exists: the same first-minimum and
+				// first-maximum scan, in table order (+x, +y, -x, -y, then
+				// the diagonals of weight 2), without the tests
+				const int off[8] = {1, R, -1, -R, R + 1, -R - 1, R - 1, 1 - R};
 				float mn0 = zi[q + 1], mx0 = mn0, mn1 = zs[q + 1], mx1 = mn1;
+				float wmn0 = 1.f, wmx0 = 1.f, wmn1 = 1.f, wmx1 = 1.f;
 #pragma unroll
-				for (int p = 1; p < 4; p++) {
+				for (int p = 1; p < NN; p++) {
 					const int qq = q + off[p];
-					const float v0 = zi[qq], v1 = zs[qq];
-					if (v0 < mn0) mn0 = v0;
-					if (v0 > mx0) mx0 = v0;
-					if (v1 < mn1) mn1 = v1;
-					if (v1 > mx1) mx1 = v1;
+					const float v0 = zi[qq], v1 = zs[qq], wt = p < 4 ? 1.f : 2.f;
+					if (v0 < mn0) { mn0 = v0; wmn0 = wt; }
+					if (v0 > mx0) { mx0 = v0; wmx0 = wt; }
+					if (v1 < mn1) { mn1 = v1; wmn1 = wt; }
+					if (v1 > mx1) { mx1 = v1; wmx1 = wt; }
 				}
-				zi[q] = __fmul_rn(__fadd_rn(mn0, mx0), 0.5f);
-				zs[q] = __fmul_rn(__fadd_rn(mn1, mx1), 0.5f);
+				if (NN == 4) {
+					zi[q] = __fmul_rn(__fadd_rn(mn0, mx0), 0.5f);
+					zs[q] = __fmul_rn(__fadd_rn(mn1, mx1), 0.5f);
+				} else {
+					zi[q] = amle_mid(mn0, mx0, wmn0, wmx0);
+					zs[q] = amle_mid(mn1, mx1, wmn1, wmx1);
+				}
 				continue;
 			}
 			int gi = 0, gj = 0;
