@@ -170,6 +170,27 @@ __global__ void k_amle_init(AmleArgs a)
 // the same values outside the tiles with unknowns, which no launch touches.
 // NN > 0: the neighbourhood size known at compile time (the loop over the
 // neighbours unrolls); NN == 0: a.nn at run time.
+// The neighbour table again, as compile-time constants for the kernels'
+// unrolled interior path (offsets in table order, and their weights).
+__device__ __forceinline__ int k_di(int p)
+{
+	const int t[AMLE_MAXNN] = {1, 0, -1, 0, 1, -1, -1, 1, 2, 1, 2, 1, -2, -1, -2, -1,
+		3, 1, 3, 1, -3, -1, -3, -1, 3, 2, 3, 2, -3, -2, -3, -2};
+	return t[p];
+}
+__device__ __forceinline__ int k_dj(int p)
+{
+	const int t[AMLE_MAXNN] = {0, 1, 0, -1, 1, -1, 1, -1, 1, 2, -1, -2, -1, -2, 1, 2,
+		1, 3, -1, -3, -1, -3, 1, 3, 2, 3, -2, -3, -2, -3, 2, 3};
+	return t[p];
+}
+__device__ __forceinline__ float k_w(int p)
+{
+	const float t[AMLE_MAXNN] = {1, 1, 1, 1, 2, 2, 2, 2, 5, 5, 5, 5, 5, 5, 5, 5,
+		10, 10, 10, 10, 10, 10, 10, 10, 13, 13, 13, 13, 13, 13, 13, 13};
+	return t[p];
+}
+
 // (wmx v_min + wmn v_max) / (wmx + wmn), the reference's midpoint.  The
 // weights are 1, 2, 5, 10 or 13, so a denominator of 2 or 4 is a power of
 // two: multiplying by its reciprocal gives the same float as dividing.
@@ -228,17 +249,15 @@ __global__ void __launch_bounds__(SP_THREADS) k_amle_fused(AmleArgs a, const flo
 			// the first nn in-image neighbours in table order, the first
 			// minimum and the first maximum, (a v_min + b v_max) / (a + b)
 			// with a the weight of the maximum and b that of the minimum
-			if ((NN == 4 || NN == 8) && interior) {
+			if (NN > 0 && interior) {
 				// every neighbour exists: the same first-minimum and
-				// first-maximum scan, in table order (+x, +y, -x, -y, then
-				// the diagonals of weight 2), without the tests
-				const int off[8] = {1, R, -1, -R, R + 1, -R - 1, R - 1, 1 - R};
+				// first-maximum scan, in table order, without the tests
 				float mn0 = zi[q + 1], mx0 = mn0, mn1 = zs[q + 1], mx1 = mn1;
 				float wmn0 = 1.f, wmx0 = 1.f, wmn1 = 1.f, wmx1 = 1.f;
 #pragma unroll
-				for (int p = 1; p < NN; p++) {
-					const int qq = q + off[p];
-					const float v0 = zi[qq], v1 = zs[qq], wt = p < 4 ? 1.f : 2.f;
+				for (int p = 1; p < (NN > 0 ? NN : 1); p++) {
+					const int qq = q + k_dj(p) * R + k_di(p);
+					const float v0 = zi[qq], v1 = zs[qq], wt = k_w(p);
 					if (v0 < mn0) { mn0 = v0; wmn0 = wt; }
 					if (v0 > mx0) { mx0 = v0; wmx0 = wt; }
 					if (v1 < mn1) { mn1 = v1; wmn1 = wt; }
@@ -408,7 +427,8 @@ int amle_run(simpois_ctx *ctx, float *out, const float *in, int w, int h, int pd
 	if (total > 0) {
 		const int Rmax = SP_TILE + 2 * reach * spl;
 		const int smem_max = amle_smem(Rmax, a.m);
-		auto kern = nn == 4 ? k_amle_fused<4> : nn == 8 ? k_amle_fused<8> : k_amle_fused<0>;
+		auto kern = nn == 4 ? k_amle_fused<4> : nn == 8 ? k_amle_fused<8> : nn == 16 ? k_amle_fused<16>
+				: nn == 32 ? k_amle_fused<32> : k_amle_fused<0>;
 		SP_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max));
 		char buf[256];
 		snprintf(buf, sizeof buf, "%p/%p/%p/%p/%d/%d/%d/%d/%d/%d", (void *)A, (const void *)in,
