@@ -276,6 +276,47 @@ static int read_juv(raw_image *x, const unsigned char *b, size_t n)
 	return 0;
 }
 
+/* ---- farbfeld ("farbfeld", big-endian 32-bit width and height, RGBA
+ * 16-bit big-endian samples) and PCM ("PC", text width, height and scale,
+ * then two float channels) (iio.c:2352-2375, 3164-3183) */
+static int read_ffd(raw_image *x, const unsigned char *b, size_t n)
+{
+	if (n < 16) return 1;
+	const uint32_t w = (uint32_t)b[8] << 24 | (uint32_t)b[9] << 16 | (uint32_t)b[10] << 8 | b[11];
+	const uint32_t h = (uint32_t)b[12] << 24 | (uint32_t)b[13] << 16 | (uint32_t)b[14] << 8 | b[15];
+	const size_t ns = (size_t)w * h * 4;
+	if (n < 16 + 2 * ns) return 1;
+	x->v = xcalloc(ns, sizeof(double));
+	if (!x->v) return 2;
+	for (size_t k = 0; k < ns; k++) x->v[k] = 256 * b[16 + 2 * k] + b[17 + 2 * k];
+	x->w = (int)w; x->h = (int)h; x->pd = 4; x->type = T_U16;
+	return 0;
+}
+
+static int read_pcm(raw_image *x, const unsigned char *b, size_t n)
+{
+	char head[128] = {0};
+	memcpy(head, b, n < 127 ? n : 127);
+	int w, h, used;
+	float scale;
+	if (sscanf(head + 2, " %d %d %g%n", &w, &h, &scale, &used) != 3 || w <= 0 || h <= 0) return 1;
+	size_t p = 2 + (size_t)used;
+	if (p >= n || !isspace(b[p])) return 1;
+	p++;
+	fprintf(stderr, "2 PCM w h scale = %d %d %g\n", w, h, scale);
+	const size_t ns = (size_t)w * h * 2;
+	if (n < p + 4 * ns) return 1;
+	x->v = xcalloc(ns, sizeof(double));
+	if (!x->v) return 2;
+	for (size_t k = 0; k < ns; k++) {
+		float v;
+		memcpy(&v, b + p + 4 * k, 4);
+		x->v[k] = v;
+	}
+	x->w = w; x->h = h; x->pd = 2; x->type = T_F32;
+	return 0;
+}
+
 /* ---- CSV and TXT: one image row per line, samples separated by commas
  * (CSV) or spaces (TXT); height = newlines, width = separators / height + 1,
  * samples parsed in order, any missing ones 0 (iio.c:2992-3071) */
@@ -811,6 +852,8 @@ static int read_core(const char *name, raw_image *x)
 	else if (n >= 2 && b[0] == 'P' && (b[1] == 'f' || b[1] == 'F')) r = read_pfm(x, b, n);
 	else if (n >= 2 && b[0] == 'P' && strchr("2356", b[1])) r = read_pnm(x, b, n);
 	else if (n >= 4 && !memcmp(b, "PIEH", 4)) r = read_flo(x, b, n);
+	else if (n >= 4 && !memcmp(b, "farb", 4)) r = read_ffd(x, b, n);
+	else if (n >= 2 && b[0] == 'P' && b[1] == 'C') r = read_pcm(x, b, n);
 	else if (n >= 3 && !memcmp(b, "#UV", 3)) r = read_juv(x, b, n);
 	else {
 		const int tf = text_format(b, n);

@@ -369,6 +369,17 @@ def io_more_cases():
             subprocess.run([O.REF_BIN, "-i", src, "-n", "0", "-o", o], check=True, capture_output=True)
             a = np.load(o)
             res["read"][key] = {"shape": list(a.shape), "out": a.ravel().tolist()}
+        # farbfeld (RGBA, 16-bit big-endian) and PCM (two float channels)
+        ffd = (b"farbfeld" + np.array([5, 3], ">u4").tobytes()
+               + rng.integers(0, 65536, 5 * 3 * 4, dtype=np.uint16).astype(">u2").tobytes())
+        pcm = b"PC 4 3 1.5\n" + (rng.standard_normal(4 * 3 * 2) * 2).astype("<f4").tobytes()
+        for key, data in (("ffd", ffd), ("pcm", pcm)):
+            src = os.path.join(td, "in." + key)
+            open(src, "wb").write(data)
+            o = os.path.join(td, "back.npy")
+            subprocess.run([O.REF_BIN, "-i", src, "-n", "0", "-o", o], check=True, capture_output=True)
+            a = np.load(o)
+            res["read"][key] = {"shape": list(a.shape), "out": a.ravel().tolist(), "bytes": list(data)}
     with open(os.path.join(OUT, "io_more.json"), "w") as fh:
         json.dump(res, fh)
     return len(res["write"]) + len(res["read"])

@@ -347,3 +347,13 @@ def test_flow_formats_read_like_reference(harness, tmp_path, key):
     want = d["read"][key]
     assert list(got.shape) == want["shape"]
     assert np.array_equal(got.view(np.uint32), np.array(want["out"], np.float32).reshape(want["shape"]).view(np.uint32))
+
+
+@pytest.mark.parametrize("key", ["ffd", "pcm"])
+def test_farbfeld_and_pcm_read_like_reference(harness, tmp_path, key):
+    want = _fixtures("io_more.json")["read"][key]
+    src = str(tmp_path / ("in." + key))
+    open(src, "wb").write(bytes(want["bytes"]))
+    got = _read_with(harness, tmp_path, src, "")
+    assert list(got.shape) == want["shape"]
+    assert np.array_equal(got.view(np.uint32), np.array(want["out"], np.float32).reshape(want["shape"]).view(np.uint32))
