@@ -3064,7 +3064,8 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	std::vector<size_t> off_mask[MAXLEV], off_code[MAXLEV], off_b[MAXLEV], off_z[MAXLEV], off_z2[MAXLEV];
 	std::vector<size_t> off_U(n), off_x(n), off_xlo(n), off_p(n), off_q(n), off_p2(n), off_balt(n);
 	std::vector<size_t> off_r64(n, 0), off_p64(n, 0), off_q64(n, 0);
-	std::vector<std::vector<int4>> lists(MAXLEV);
+	size_t ntl[MAXLEV] = {};   // tiles per level over all problems
+	std::string lkey;          // the problem sizes, which alone decide the tile lists
 	const int cmax = opt.coarse_max > 0 ? clamp_coarse_max(opt.coarse_max) : default_coarse_max();
 	for (int k = 0; k < n; k++) {
 		const MgProblem &q = probs[k];
@@ -3089,9 +3090,9 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 			off_b[l].push_back(Lo.take(px * 4));
 			off_z[l].push_back(Lo.take(px * 4));
 			off_z2[l].push_back(Lo.take(px * 4));
-			for (int ty = 0; ty < ntiles(lh[l]); ty++)
-				for (int tx = 0; tx < ntiles(lw[l]); tx++) lists[l].push_back(make_int4(k, tx, ty, 0));
+			ntl[l] += (size_t)ntiles(lh[l]) * ntiles(lw[l]);
 		}
+		lkey += std::to_string(q.w) + "x" + std::to_string(q.h) + ",";
 		for (int l = nl; l < MAXLEV; l++) {
 			off_mask[l].push_back(0);
 			off_code[l].push_back(0);
@@ -3140,17 +3141,22 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	size_t o_gl = Lo.take(sizeof(Globals) * GMAX);
 	size_t o_pcnt = Lo.take(sizeof(int) * MAXLEV * n), o_trel = Lo.take(sizeof(int) * n);
 	size_t o_all[MAXLEV], o_act[MAXLEV], o_flag[MAXLEV];
+	// every level's tile list in one block (level after level), so that one
+	// copy uploads them all
+	size_t lbeg[MAXLEV + 1] = {};
+	for (int l = 0; l < pl.nlev_max; l++) lbeg[l + 1] = lbeg[l] + ntl[l];
+	const size_t o_lists = Lo.take(sizeof(int4) * std::max<size_t>(1, lbeg[pl.nlev_max]));
 	for (int l = 0; l < pl.nlev_max; l++) {
-		pl.nall[l] = (int)lists[l].size();
-		o_all[l] = Lo.take(sizeof(int4) * lists[l].size());
-		o_act[l] = Lo.take(sizeof(int4) * lists[l].size());
-		o_flag[l] = Lo.take(sizeof(int) * lists[l].size());
+		pl.nall[l] = (int)ntl[l];
+		o_all[l] = o_lists + sizeof(int4) * lbeg[l];
+		o_act[l] = Lo.take(sizeof(int4) * ntl[l]);
+		o_flag[l] = Lo.take(sizeof(int) * ntl[l]);
 	}
 	size_t o_dnall = Lo.take(sizeof(int) * MAXLEV), o_dnact = Lo.take(sizeof(int) * MAXLEV);
 	size_t o_dall = Lo.take(sizeof(int4 *) * MAXLEV), o_dact = Lo.take(sizeof(int4 *) * MAXLEV);
 	size_t o_dflag = Lo.take(sizeof(int *) * MAXLEV);
 	size_t o_tbeg = Lo.take(sizeof(int) * n), o_tcnt = Lo.take(sizeof(int) * n);
-	size_t o_part = Lo.take(sizeof(double) * 2 * std::max<size_t>(1, lists[0].size()));
+	size_t o_part = Lo.take(sizeof(double) * 2 * std::max<size_t>(1, ntl[0]));
 	size_t o_gptr = Lo.take(sizeof(void *) * 3 * n);
 	// TMA maps (b and code) of the tile levels whose rows are 16-byte multiples
 	int nmaps = 0;
@@ -3165,7 +3171,6 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 
 	// host images of the device tables, staged in pinned memory
 	size_t stage_bytes = sizeof(ProbDev) * n + sizeof(ProbState) * n + sizeof(Globals) * GMAX;
-	for (int l = 0; l < pl.nlev_max; l++) stage_bytes += sizeof(int4) * lists[l].size();
 	stage_bytes += 64 * MAXLEV + sizeof(void *) * 3 * n + sizeof(int) * n + 16 * (MAXLEV + 16) + 4096;
 	stage_bytes += sizeof(CUtensorMap) * nmaps + 128;
 	stage_bytes += sizeof(int) * (MAXLEV + 1) * n + 64;   // per-problem tile counts, group offsets
@@ -3274,8 +3279,36 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	SP_CUDA(ctx, put(pl.dst, hst.data(), sizeof(ProbState) * n));
 	SP_CUDA(ctx, put(pl.gls, hg.data(), sizeof(Globals) * GMAX));
 	SP_CUDA(ctx, cudaMemsetAsync(pl.pcnt, 0, sizeof(int) * MAXLEV * n, s));
-	for (int l = 0; l < pl.nlev_max; l++)
-		SP_CUDA(ctx, put(pl.all[l], lists[l].data(), sizeof(int4) * lists[l].size()));
+	// the tile lists, problem after problem in every level: rebuilt only when
+	// the sequence of problem sizes changes (the previous call's copy from
+	// this buffer completed before it returned)
+	const size_t nlist = lbeg[pl.nlev_max];
+	if (ctx->lists_key != lkey || !ctx->lists_host) {
+		ctx->lists_key.clear();
+		if (nlist > ctx->lists_cap) {
+			if (ctx->lists_host) cudaFreeHost(ctx->lists_host);
+			ctx->lists_host = nullptr;
+			ctx->lists_cap = 0;
+			if (cudaMallocHost((void **)&ctx->lists_host, sizeof(int4) * nlist) != cudaSuccess) {
+				cudaGetLastError();
+				return ctx_fail(ctx, SIMPOIS_ENOMEM, "cannot allocate %zu bytes of pinned memory",
+						sizeof(int4) * nlist);
+			}
+			ctx->lists_cap = nlist;
+		}
+		for (int l = 0; l < pl.nlev_max; l++) {
+			int4 *o = ctx->lists_host + lbeg[l];
+			for (int k = 0; k < n; k++) {
+				const int tw = ntiles(hp[k].lv[l].w), th = ntiles(hp[k].lv[l].h);
+				if (l >= hp[k].nlev) continue;
+				for (int ty = 0; ty < th; ty++)
+					for (int tx = 0; tx < tw; tx++) *o++ = make_int4(k, tx, ty, 0);
+			}
+		}
+		ctx->lists_key = lkey;
+	}
+	if (nlist)
+		SP_CUDA(ctx, cudaMemcpyAsync(A + o_lists, ctx->lists_host, sizeof(int4) * nlist, cudaMemcpyHostToDevice, s));
 	SP_CUDA(ctx, put(pl.dnall, pl.nall, sizeof(int) * MAXLEV));
 	SP_CUDA(ctx, put(pl.dall, pl.all, sizeof(int4 *) * MAXLEV));
 	SP_CUDA(ctx, put(pl.dact, pl.act, sizeof(int4 *) * MAXLEV));
