@@ -281,13 +281,22 @@ def text_cases():
     res = {}
     with tempfile.TemporaryDirectory() as td:
         o = os.path.join(td, "o.npy")
+        env0 = {k: v for k, v in os.environ.items() if k not in ("IIO_RAW", "IIO_TRANS", "IIO_TXT")}
         for k, text in files.items():
             assert len(text) >= 256, (k, len(text))
             src = os.path.join(td, k)
             open(src, "w").write(text)
-            subprocess.run([O.REF_BIN, "-i", src, "-n", "0", "-o", o], check=True, capture_output=True)
+            subprocess.run([O.REF_BIN, "-i", src, "-n", "0", "-o", o], check=True, capture_output=True, env=env0)
             out = np.load(o)
             res[k] = {"text": text, "shape": list(out.shape), "out": out.ravel().tolist()}
+        # IIO_TXT: a CSV file read as TXT (one number a line: atof stops at the comma)
+        src = os.path.join(td, "csv_as_txt")
+        open(src, "w").write(files["csv"])
+        subprocess.run([O.REF_BIN, "-i", src, "-n", "0", "-o", o], check=True, capture_output=True,
+                       env=dict(env0, IIO_TXT="1"))
+        out = np.load(o)
+        res["csv_as_txt"] = {"text": files["csv"], "env": {"IIO_TXT": "1"}, "shape": list(out.shape),
+                             "out": out.ravel().tolist()}
     with open(os.path.join(OUT, "text.json"), "w") as fh:
         json.dump(res, fh)
     return len(res)

@@ -276,7 +276,14 @@ def test_text_formats_match_reference(harness, tmp_path, key):
     d = _fixtures("text.json")[key]
     src = str(tmp_path / key)
     open(src, "w").write(d["text"])
-    got = _read_with(harness, tmp_path, src, "")
+    if d.get("env"):   # IIO_TXT: every file read as TXT
+        dst = str(tmp_path / "o.npy")
+        env = {k: v for k, v in os.environ.items() if k not in ("IIO_RAW", "IIO_TRANS", "IIO_TXT")}
+        env.update(d["env"])
+        subprocess.run([harness, "read", src, dst], check=True, env=env)
+        got = np.load(dst)
+    else:
+        got = _read_with(harness, tmp_path, src, "")
     assert list(got.shape) == d["shape"]
     assert np.array_equal(got.view(np.uint32), np.array(d["out"], np.float32).reshape(d["shape"]).view(np.uint32))
 
