@@ -3136,10 +3136,22 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 			return ctx_fail(ctx, SIMPOIS_ECUDA, "coarse kernel shared memory (%d B): %s", pl.coarse_smem,
 					cudaGetErrorString(e));
 	}
-	size_t o_dp = Lo.take(sizeof(ProbDev) * n);
-	size_t o_st = Lo.take(sizeof(ProbState) * n);
-	size_t o_gl = Lo.take(sizeof(Globals) * GMAX);
-	size_t o_pcnt = Lo.take(sizeof(int) * MAXLEV * n), o_trel = Lo.take(sizeof(int) * n);
+	// the small tables -- problem table, states, loop counters, tile counts
+	// and offsets, the lists' pointer tables -- in one block of the arena,
+	// mirrored in the staging buffer and uploaded with one copy
+	Layout Tl;
+	const size_t t_dp = Tl.take(sizeof(ProbDev) * n, 16), t_st = Tl.take(sizeof(ProbState) * n, 16);
+	const size_t t_gl = Tl.take(sizeof(Globals) * GMAX, 16), t_pcnt = Tl.take(sizeof(int) * MAXLEV * n, 16);
+	const size_t t_trel = Tl.take(sizeof(int) * n, 16), t_dnall = Tl.take(sizeof(int) * MAXLEV, 16);
+	const size_t t_dnact = Tl.take(sizeof(int) * MAXLEV, 16), t_dall = Tl.take(sizeof(int4 *) * MAXLEV, 16);
+	const size_t t_dact = Tl.take(sizeof(int4 *) * MAXLEV, 16), t_dflag = Tl.take(sizeof(int *) * MAXLEV, 16);
+	const size_t t_tbeg = Tl.take(sizeof(int) * n, 16), t_tcnt = Tl.take(sizeof(int) * n, 16);
+	const size_t tab_bytes = (Tl.off + 15) / 16 * 16;
+	const size_t o_tab = Lo.take(tab_bytes);
+	const size_t o_dp = o_tab + t_dp, o_st = o_tab + t_st, o_gl = o_tab + t_gl, o_pcnt = o_tab + t_pcnt;
+	const size_t o_trel = o_tab + t_trel, o_dnall = o_tab + t_dnall, o_dnact = o_tab + t_dnact;
+	const size_t o_dall = o_tab + t_dall, o_dact = o_tab + t_dact, o_dflag = o_tab + t_dflag;
+	const size_t o_tbeg = o_tab + t_tbeg, o_tcnt = o_tab + t_tcnt;
 	size_t o_all[MAXLEV], o_act[MAXLEV], o_flag[MAXLEV];
 	// every level's tile list in one block (level after level), so that one
 	// copy uploads them all
@@ -3152,10 +3164,6 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 		o_act[l] = Lo.take(sizeof(int4) * ntl[l]);
 		o_flag[l] = Lo.take(sizeof(int) * ntl[l]);
 	}
-	size_t o_dnall = Lo.take(sizeof(int) * MAXLEV), o_dnact = Lo.take(sizeof(int) * MAXLEV);
-	size_t o_dall = Lo.take(sizeof(int4 *) * MAXLEV), o_dact = Lo.take(sizeof(int4 *) * MAXLEV);
-	size_t o_dflag = Lo.take(sizeof(int *) * MAXLEV);
-	size_t o_tbeg = Lo.take(sizeof(int) * n), o_tcnt = Lo.take(sizeof(int) * n);
 	size_t o_part = Lo.take(sizeof(double) * 2 * std::max<size_t>(1, ntl[0]));
 	size_t o_gptr = Lo.take(sizeof(void *) * 3 * n);
 	// TMA maps (b and code) of the tile levels whose rows are 16-byte multiples
@@ -3174,6 +3182,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	stage_bytes += 64 * MAXLEV + sizeof(void *) * 3 * n + sizeof(int) * n + 16 * (MAXLEV + 16) + 4096;
 	stage_bytes += sizeof(CUtensorMap) * nmaps + 128;
 	stage_bytes += sizeof(int) * (MAXLEV + 1) * n + 64;   // per-problem tile counts, group offsets
+	stage_bytes += tab_bytes;                              // the table block
 	rc = ctx_pinned_reserve(ctx, stage_bytes + 256 * GMAX);
 	if (rc) return rc;
 	char *stage = ctx->pinned + 256 * GMAX;  // the first bytes hold read-back scalars
@@ -3256,8 +3265,8 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 		pl.flag[l] = (int *)(A + o_flag[l]);
 	}
 
-	// stage and upload: problem table, states, tile lists, pointer tables
-	size_t so = 0;
+	// stage and upload: the table block, then (maps, adjoint pointers) after it
+	size_t so = tab_bytes;
 	auto put = [&](void *dst, const void *src, size_t bytes) -> cudaError_t {
 		so = (so + 15) / 16 * 16;
 		memcpy(stage + so, src, bytes);
@@ -3272,13 +3281,22 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 		hst[k].status = SIMPOIS_OK;
 		hst[k].max_iter = opt.max_iter > 0 ? opt.max_iter : 500;
 	}
-	std::vector<Globals> hg(GMAX);
-	memset(hg.data(), 0, sizeof(Globals) * GMAX);
-	SP_CUDA(ctx, put(pl.dp, hp.data(), sizeof(ProbDev) * n));
+	{
+		// loop counters, per-problem tile counts, group offsets, active
+		// counts and tile counts start at 0; tile begins at INT_MAX
+		char *tab = stage;
+		memset(tab, 0, tab_bytes);
+		memcpy(tab + t_dp, hp.data(), sizeof(ProbDev) * n);
+		memcpy(tab + t_st, hst.data(), sizeof(ProbState) * n);
+		memcpy(tab + t_dnall, pl.nall, sizeof(int) * MAXLEV);
+		memcpy(tab + t_dall, pl.all, sizeof(int4 *) * MAXLEV);
+		memcpy(tab + t_dact, pl.act, sizeof(int4 *) * MAXLEV);
+		memcpy(tab + t_dflag, pl.flag, sizeof(int *) * MAXLEV);
+		int *tb = (int *)(tab + t_tbeg);
+		for (int k = 0; k < n; k++) tb[k] = INT_MAX;
+		SP_CUDA(ctx, cudaMemcpyAsync(A + o_tab, tab, tab_bytes, cudaMemcpyHostToDevice, s));
+	}
 	if (nmaps) SP_CUDA(ctx, put(A + o_tmap, maps.data(), sizeof(CUtensorMap) * nmaps));
-	SP_CUDA(ctx, put(pl.dst, hst.data(), sizeof(ProbState) * n));
-	SP_CUDA(ctx, put(pl.gls, hg.data(), sizeof(Globals) * GMAX));
-	SP_CUDA(ctx, cudaMemsetAsync(pl.pcnt, 0, sizeof(int) * MAXLEV * n, s));
 	// the tile lists, problem after problem in every level: rebuilt only when
 	// the sequence of problem sizes changes (the previous call's copy from
 	// this buffer completed before it returned)
@@ -3309,13 +3327,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	}
 	if (nlist)
 		SP_CUDA(ctx, cudaMemcpyAsync(A + o_lists, ctx->lists_host, sizeof(int4) * nlist, cudaMemcpyHostToDevice, s));
-	SP_CUDA(ctx, put(pl.dnall, pl.nall, sizeof(int) * MAXLEV));
-	SP_CUDA(ctx, put(pl.dall, pl.all, sizeof(int4 *) * MAXLEV));
-	SP_CUDA(ctx, put(pl.dact, pl.act, sizeof(int4 *) * MAXLEV));
-	SP_CUDA(ctx, put(pl.dflag, pl.flag, sizeof(int *) * MAXLEV));
-	std::vector<int> init_beg(n, INT_MAX);
-	SP_CUDA(ctx, put(pl.tbeg, init_beg.data(), sizeof(int) * n));
-	SP_CUDA(ctx, cudaMemsetAsync(pl.tcnt, 0, sizeof(int) * n, s));
+
 	if (opt.mode == MG_ADJOINT) {
 		pl.gout = (const float **)(A + o_gptr);
 		pl.gin = (float **)(A + o_gptr) + n;
