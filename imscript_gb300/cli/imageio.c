@@ -185,21 +185,46 @@ static int pnm_int(const unsigned char *b, size_t n, size_t *p, int *v)
 	return 0;
 }
 
+/* an ASCII sample: a float as "%f" reads it, after white space */
+static int pnm_float(const unsigned char *b, size_t n, size_t *p, double *v)
+{
+	while (*p < n && isspace(b[*p])) (*p)++;
+	char t[64];
+	size_t k = 0;
+	while (*p + k < n && k < sizeof t - 1 && !isspace(b[*p + k])) {
+		t[k] = (char)b[*p + k];
+		k++;
+	}
+	t[k] = 0;
+	char *e;
+	const float f = strtof(t, &e);
+	if (e == t) return 1;
+	*p += (size_t)(e - t);
+	*v = f;
+	return 0;
+}
+
 static int read_pnm(raw_image *x, const unsigned char *b, size_t n)
 {
 	char kind = b[1];
 	int pd = (kind == '3' || kind == '6') ? 3 : 1, w, h, mx;
 	size_t p = 2;
-	if (pnm_int(b, n, &p, &w) || pnm_int(b, n, &p, &h) || pnm_int(b, n, &p, &mx)) return 1;
+	if (pnm_int(b, n, &p, &w) || pnm_int(b, n, &p, &h)) return 1;
+	/* iio's n-channel variants: "P7" (ASCII) and "P9" (binary) carry the
+	 * channel count before the maximum value (iio.c:2291-2330) */
+	if ((kind == '7' || kind == '9') && (pnm_int(b, n, &p, &pd) || pd <= 0)) return 1;
+	if (pnm_int(b, n, &p, &mx)) return 1;
+	if (kind == '7') kind = '2';
+	if (kind == '9') kind = '5';
 	size_t ns = (size_t)w * h * pd;
 	x->v = xcalloc(ns, sizeof(double));
 	if (!x->v) return 2;
 	if (kind == '2' || kind == '3') {
-		for (size_t k = 0; k < ns; k++) {
-			int v;
-			if (pnm_int(b, n, &p, &v)) break;
-			x->v[k] = v;
-		}
+		for (size_t k = 0; k < ns; k++)
+			if (pnm_float(b, n, &p, &x->v[k])) {
+				fprintf(stderr, "imageio: fewer samples than the PNM header announces\n");
+				return 1;
+			}
 	} else {
 		p++;   /* the single whitespace after maxval */
 		int bps = mx > 255 ? 2 : 1;
@@ -850,7 +875,7 @@ static int read_core(const char *name, raw_image *x)
 	if (getenv("IIO_TXT")) r = read_text(x, b, n, ' ');   /* IIO_TXT: every file is TXT */
 	else if (n >= 4 && b[0] == 0x93 && b[1] == 'N' && b[2] == 'U' && b[3] == 'M') r = read_npy(x, b, n);
 	else if (n >= 2 && b[0] == 'P' && (b[1] == 'f' || b[1] == 'F')) r = read_pfm(x, b, n);
-	else if (n >= 2 && b[0] == 'P' && strchr("2356", b[1])) r = read_pnm(x, b, n);
+	else if (n >= 2 && b[0] == 'P' && b[1] && strchr("235679", b[1])) r = read_pnm(x, b, n);
 	else if (n >= 4 && !memcmp(b, "PIEH", 4)) r = read_flo(x, b, n);
 	else if (n >= 4 && !memcmp(b, "farb", 4)) r = read_ffd(x, b, n);
 	else if (n >= 2 && b[0] == 'P' && b[1] == 'C') r = read_pcm(x, b, n);

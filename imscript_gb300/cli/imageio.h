@@ -14,7 +14,8 @@
  *    and so does every file while IIO_RAW holds the fields; IIO_TXT reads
  *    every file as TXT (iio.c:3597-3795, 5164-5180);
  *  - the input format is sniffed from the first bytes: NumPy .npy (1.0,
- *    every numeric dtype), PFM ("Pf"/"PF"), PNM ("P2","P3","P5","P6"), and
+ *    every numeric dtype), PFM ("Pf"/"PF"), PNM ("P2","P3","P5","P6", and
+ *    iio's n-channel "P7"/"P9"; ASCII samples read as floats), and
  *    the text formats told apart as iio does -- CSV and TXT (one row per
  *    line, commas or spaces) and ASC ("w h 1 pd" header, planar samples);
  *  - the output format follows the file-name suffix: .uv and .flo (2

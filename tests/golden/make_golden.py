@@ -382,7 +382,12 @@ def io_more_cases():
         ffd = (b"farbfeld" + np.array([5, 3], ">u4").tobytes()
                + rng.integers(0, 65536, 5 * 3 * 4, dtype=np.uint16).astype(">u2").tobytes())
         pcm = b"PC 4 3 1.5\n" + (rng.standard_normal(4 * 3 * 2) * 2).astype("<f4").tobytes()
-        for key, data in (("ffd", ffd), ("pcm", pcm)):
+        # iio's n-channel PNM variants and ASCII samples read as floats
+        p7 = b"P7\n3 2\n2\n255\n" + " ".join(f"{v:.3f}" for v in rng.standard_normal(12) * 9).encode() + b"\n"
+        p9 = b"P9 3 2 2 255\n" + rng.integers(0, 256, 12, dtype=np.uint8).tobytes()
+        p9_16 = b"P9 2 2 3 65535\n" + rng.integers(0, 65536, 12, dtype=np.uint16).astype(">u2").tobytes()
+        p2f = b"P2\n3 2\n255\n0.5 -1 2.25\n3 4e1 5\n"
+        for key, data in (("ffd", ffd), ("pcm", pcm), ("p7", p7), ("p9", p9), ("p9_16", p9_16), ("p2_float", p2f)):
             src = os.path.join(td, "in." + key)
             open(src, "wb").write(data)
             o = os.path.join(td, "back.npy")
