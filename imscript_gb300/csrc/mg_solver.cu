@@ -43,15 +43,23 @@
 // kernels (SIMPOIS_FLAG_UNFUSED), the one-launch-per-sweep cycle and FP32
 // PCG serve both operators (5 colours and 4 sweeps for 13 points).
 //
-// Batching.  All problems of a call share every launch: each level keeps one
-// list of 32 x 32 tiles that contain unknowns, over all problems.  Every
+// Batching.  Each level keeps one list of 32 x 32 tiles that contain
+// unknowns, over all problems of a call, problem after problem.  Every
 // reduction is per problem and deterministic: each tile writes its partial
 // sum, the last tile of a problem to finish (an atomic counter) sums the
 // problem's partials in tile order and updates the problem's scalars.  A
 // problem whose inner solve has converged skips every later launch (early
-// retirement).  The whole solve is one CUDA graph with two nested
-// device-driven WHILE loops (refinement steps, PCG iterations), captured
-// once per plan and replayed.
+// retirement).  The problems are split into groups (contiguous ranges with
+// about equal work); the solve is one CUDA graph in which every group is an
+// independent branch with its own two nested device-driven WHILE loops
+// (refinement steps, PCG iterations) over its slices of the tile lists, so
+// one group's latency-bound coarse levels overlap another's fine ones.  The
+// graph is captured once per plan and replayed; the tile lists are kept per
+// sequence of problem sizes, the small tables go up in one copy.
+//
+// Launches.  The V-cycle kernels use programmatic dependent launch: each
+// waits (griddepcontrol.wait) before its first dependent access and any early
+// return, then releases the next kernel.
 #include <algorithm>
 #include <climits>
 #include <cmath>
