@@ -9,11 +9,20 @@
 // src/amle.c:66-87).  Here a sweep visits the colour classes (i + k j) mod m
 // in turn, (m, k) chosen so that no neighbour offset of the first NN falls in
 // a pixel's own class: a class updates in parallel, in place, and the result
-// does not depend on the order inside the class.  One launch updates one
-// class of both iterates of every channel; the NITER x m launches of a call
-// are one CUDA graph.  Every float operation is the reference's, in its order
-// (round-to-nearest intrinsics, no contraction), so the output is bit for bit
-// the colour-ordered restatement of the reference.
+// does not depend on the order inside the class.  The sweeps are blocked in
+// time: one launch loads a 32 x 32 tile of both iterates with a halo of r S
+// pixels (r the reach of the neighbourhood) into shared memory, sorts its
+// unknowns into per-colour lists, and takes S class updates there, each on
+// the cells still far enough from the region's edge; after them the tile is
+// exact and alone is written back (double-buffered: a tile's halo is other
+// tiles' pixels).  The launches of a call are one CUDA graph.  The kernel is
+// instantiated for NN = 4, 8, 16 and 32 with the neighbour table as
+// compile-time constants (any other NN reads it at run time), and a tile
+// whose region lies wholly in the image skips the bounds tests.  Every float
+// operation is the reference's, in its order (round-to-nearest intrinsics, no
+// contraction; a division by 2 or 4 as the exact multiplication by its
+// reciprocal), so the output is bit for bit the colour-ordered restatement of
+// the reference.
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
