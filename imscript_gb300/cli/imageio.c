@@ -342,6 +342,40 @@ static int read_pcm(raw_image *x, const unsigned char *b, size_t n)
 	return 0;
 }
 
+/* ---- LUM: "FLOA" at byte 8 -- big-endian 16-bit width and height at bytes
+ * 2 and 6, big-endian floats from byte 3988 -- or "12LI" -- little-endian
+ * 32-bit width and height at 0 and 4, 16-bit samples from byte 11968
+ * (iio.c:2656-2697, 5290-5305) */
+static int read_lum(raw_image *x, const unsigned char *b, size_t n)
+{
+	if (b[8] == '1') {
+		uint32_t w, h;
+		memcpy(&w, b, 4);
+		memcpy(&h, b + 4, 4);
+		const size_t ns = (size_t)w * h;
+		if (n < 11968 + 2 * ns) return 1;
+		x->v = xcalloc(ns, sizeof(double));
+		if (!x->v) return 2;
+		for (size_t k = 0; k < ns; k++) x->v[k] = b[11968 + 2 * k] + 256 * b[11969 + 2 * k];
+		x->w = (int)w; x->h = (int)h; x->pd = 1; x->type = T_U16;
+		return 0;
+	}
+	const int w = 256 * b[2] + b[3], h = 256 * b[6] + b[7];
+	const size_t ns = (size_t)w * h;
+	if (n < 0xf94 + 4 * ns) return 1;
+	x->v = xcalloc(ns, sizeof(double));
+	if (!x->v) return 2;
+	for (size_t k = 0; k < ns; k++) {
+		const unsigned char *q = b + 0xf94 + 4 * k;
+		const uint32_t u = (uint32_t)q[0] << 24 | (uint32_t)q[1] << 16 | (uint32_t)q[2] << 8 | q[3];
+		float v;
+		memcpy(&v, &u, 4);
+		x->v[k] = v;
+	}
+	x->w = w; x->h = h; x->pd = 1; x->type = T_F32;
+	return 0;
+}
+
 /* ---- CSV and TXT: one image row per line, samples separated by commas
  * (CSV) or spaces (TXT); height = newlines, width = separators / height + 1,
  * samples parsed in order, any missing ones 0 (iio.c:2992-3071) */
@@ -880,6 +914,8 @@ static int read_core(const char *name, raw_image *x)
 	else if (n >= 4 && !memcmp(b, "farb", 4)) r = read_ffd(x, b, n);
 	else if (n >= 2 && b[0] == 'P' && b[1] == 'C') r = read_pcm(x, b, n);
 	else if (n >= 3 && !memcmp(b, "#UV", 3)) r = read_juv(x, b, n);
+	else if (n >= 12 && !memchr(b, '\n', 8) && (!memcmp(b + 8, "FLOA", 4) || !memcmp(b + 8, "12LI", 4)))
+		r = read_lum(x, b, n);
 	else {
 		const int tf = text_format(b, n);
 		if (tf == TXT_CSV) r = read_text(x, b, n, ',');

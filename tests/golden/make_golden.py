@@ -387,7 +387,19 @@ def io_more_cases():
         p9 = b"P9 3 2 2 255\n" + rng.integers(0, 256, 12, dtype=np.uint8).tobytes()
         p9_16 = b"P9 2 2 3 65535\n" + rng.integers(0, 65536, 12, dtype=np.uint16).astype(">u2").tobytes()
         p2f = b"P2\n3 2\n255\n0.5 -1 2.25\n3 4e1 5\n"
-        for key, data in (("ffd", ffd), ("pcm", pcm), ("p7", p7), ("p9", p9), ("p9_16", p9_16), ("p2_float", p2f)):
+        # LUM: big-endian floats after a 3988-byte header, or 12-bit samples after 11968 bytes
+        hd = bytearray(0xf94)
+        hd[2:4] = (5).to_bytes(2, "big")
+        hd[6:8] = (3).to_bytes(2, "big")
+        hd[8:12] = b"FLOA"
+        lum = bytes(hd) + (rng.standard_normal(15) * 4).astype(">f4").tobytes()
+        hd12 = bytearray(11968)
+        hd12[0:4] = (6).to_bytes(4, "little")   # (4 would read as the RAT magic)
+        hd12[4:8] = (3).to_bytes(4, "little")
+        hd12[8:12] = b"12LI"
+        lum12 = bytes(hd12) + rng.integers(0, 4096, 18, dtype=np.uint16).astype("<u2").tobytes()
+        for key, data in (("ffd", ffd), ("pcm", pcm), ("p7", p7), ("p9", p9), ("p9_16", p9_16), ("p2_float", p2f),
+                          ("lum", lum), ("lum12", lum12)):
             src = os.path.join(td, "in." + key)
             open(src, "wb").write(data)
             o = os.path.join(td, "back.npy")

@@ -356,7 +356,7 @@ def test_flow_formats_read_like_reference(harness, tmp_path, key):
     assert np.array_equal(got.view(np.uint32), np.array(want["out"], np.float32).reshape(want["shape"]).view(np.uint32))
 
 
-@pytest.mark.parametrize("key", ["ffd", "pcm", "p7", "p9", "p9_16", "p2_float"])
+@pytest.mark.parametrize("key", ["ffd", "pcm", "p7", "p9", "p9_16", "p2_float", "lum", "lum12"])
 def test_farbfeld_and_pcm_read_like_reference(harness, tmp_path, key):
     """farbfeld, PCM, iio's n-channel PNM variants P7/P9 and ASCII PNM
     samples read as floats, as the reference reads them."""
