@@ -342,6 +342,83 @@ static int read_pcm(raw_image *x, const unsigned char *b, size_t n)
 	return 0;
 }
 
+/* ---- MegaWave RIM images (iio.c:2400-2560): "IR"/"RI" float and "MI"/"IM"
+ * byte images (comment length, width, height as 16-bit numbers, 56 bytes,
+ * the comment, then the samples), "WE"/"VI" planar ccimage/cfimage (a tag,
+ * then channels, rows, columns, band, form and comment size as 32-bit
+ * numbers, then the planes).  The second spelling of each swaps bytes --
+ * its 16-bit fields are little-endian and its 32-bit ones big-endian, the
+ * first's the other way round -- and float samples are swapped with it,
+ * except in a cfimage. */
+static void swap_bytes(unsigned char *p, size_t words, int size);
+static unsigned rim_short(const unsigned char *p, int swp) { return swp ? p[1] * 256u + p[0] : p[0] * 256u + p[1]; }
+static uint32_t rim_int(const unsigned char *p, int swp)
+{
+	return swp ? (uint32_t)p[0] << 24 | (uint32_t)p[1] << 16 | (uint32_t)p[2] << 8 | p[3]
+	           : (uint32_t)p[3] << 24 | (uint32_t)p[2] << 16 | (uint32_t)p[1] << 8 | p[0];
+}
+
+static int read_rim(raw_image *x, const unsigned char *b, size_t n)
+{
+	const char a = (char)b[0], c = (char)b[1];
+	const int fimage = (a == 'I' && c == 'R') || (a == 'R' && c == 'I');
+	const int cimage = (a == 'M' && c == 'I') || (a == 'I' && c == 'M');
+	const int swp = (a == 'R') || (a == 'I' && c == 'M') || a == 'V';
+	if (fimage || cimage) {
+		if (n < 64) return 1;
+		const unsigned lencomm = rim_short(b + 2, swp), w = rim_short(b + 4, swp), h = rim_short(b + 6, swp);
+		const size_t off = 8 + 56 + lencomm, ns = (size_t)w * h, ss = fimage ? 4 : 1;
+		if (n < off + ns * ss) {
+			fprintf(stderr, "imageio: could not read entire RIM file\n");
+			return 1;
+		}
+		x->v = xcalloc(ns, sizeof(double));
+		if (!x->v) return 2;
+		for (size_t k = 0; k < ns; k++) {
+			if (cimage) { x->v[k] = b[off + k]; continue; }
+			unsigned char q[4];
+			memcpy(q, b + off + 4 * k, 4);
+			if (swp) swap_bytes(q, 1, 4);
+			float v;
+			memcpy(&v, q, 4);
+			x->v[k] = v;
+		}
+		x->w = (int)w; x->h = (int)h; x->pd = 1; x->type = fimage ? T_F32 : T_U8;
+		return 0;
+	}
+	/* ccimage / cfimage */
+	if (n < 28) return 1;
+	const unsigned iv = rim_short(b + 2, swp);
+	if (iv != 0x4956 && iv != 0x5649 && iv != 0x4557 && iv != 0x5745) {
+		fprintf(stderr, "imageio: bad ccimage header %x\n", iv);
+		return 1;
+	}
+	const uint32_t np = rim_int(b + 4, swp), nrow = rim_int(b + 8, swp), ncol = rim_int(b + 12, swp);
+	const uint32_t form = rim_int(b + 20, swp);
+	const size_t ns = (size_t)np * nrow * ncol, ss = form == 0x8001 ? 1 : 4;
+	if (form != 0x8001 && form != 0xc004) {
+		fprintf(stderr, "imageio: unsupported PM_form %x\n", form);
+		return 1;
+	}
+	if (n < 28 + ns * ss) return 1;
+	x->v = xcalloc(ns, sizeof(double));
+	if (!x->v) return 2;
+	for (size_t j = 0; j < nrow; j++)
+		for (size_t i = 0; i < ncol; i++)
+			for (size_t l = 0; l < np; l++) {
+				const size_t src = i + j * ncol + l * ncol * nrow, dst = l + (i + j * ncol) * np;
+				if (ss == 1) {
+					x->v[dst] = b[28 + src];
+				} else {
+					float v;
+					memcpy(&v, b + 28 + 4 * src, 4);
+					x->v[dst] = v;
+				}
+			}
+	x->w = (int)ncol; x->h = (int)nrow; x->pd = (int)np; x->type = ss == 1 ? T_U8 : T_F32;
+	return 0;
+}
+
 /* ---- LUM: "FLOA" at byte 8 -- big-endian 16-bit width and height at bytes
  * 2 and 6, big-endian floats from byte 3988 -- or "12LI" -- little-endian
  * 32-bit width and height at 0 and 4, 16-bit samples from byte 11968
@@ -910,6 +987,10 @@ static int read_core(const char *name, raw_image *x)
 	else if (n >= 4 && b[0] == 0x93 && b[1] == 'N' && b[2] == 'U' && b[3] == 'M') r = read_npy(x, b, n);
 	else if (n >= 2 && b[0] == 'P' && (b[1] == 'f' || b[1] == 'F')) r = read_pfm(x, b, n);
 	else if (n >= 2 && b[0] == 'P' && b[1] && strchr("235679", b[1])) r = read_pnm(x, b, n);
+	else if (n >= 2 && ((b[0] == 'I' && (b[1] == 'R' || b[1] == 'M')) || (b[0] == 'M' && b[1] == 'I') ||
+			(b[0] == 'W' && b[1] == 'E') || (b[0] == 'V' && b[1] == 'I') ||
+			(b[0] == 'R' && b[1] == 'I' && !(n >= 4 && b[2] == 'F' && b[3] == 'F'))))
+		r = read_rim(x, b, n);
 	else if (n >= 4 && !memcmp(b, "PIEH", 4)) r = read_flo(x, b, n);
 	else if (n >= 4 && !memcmp(b, "farb", 4)) r = read_ffd(x, b, n);
 	else if (n >= 2 && b[0] == 'P' && b[1] == 'C') r = read_pcm(x, b, n);
@@ -1062,6 +1143,14 @@ int imgio_write_split(const char *name, const float *x, int w, int h, int pd)
 		write_txt(f, v, w, ns, pd);
 	} else if (suffix(name, ".raw")) {
 		rc = fwrite(v, sizeof(float), ns, f) != ns;   /* the samples, interleaved */
+	} else if (suffix(name, ".mw") && pd == 1) {
+		/* MegaWave fimage: "IR", comment length 2, width, height, 29 zero
+		 * 16-bit fields (big-endian), the floats (iio.c:4376-4406) */
+		unsigned char hd[66] = {'I', 'R', 0, 2};
+		hd[4] = (unsigned char)(w >> 8); hd[5] = (unsigned char)w;
+		hd[6] = (unsigned char)(h >> 8); hd[7] = (unsigned char)h;
+		rc = fwrite(hd, 1, sizeof hd, f) != sizeof hd;
+		rc |= fwrite(v, sizeof(float), ns, f) != ns;
 	} else if (suffix(name, ".asc")) {
 		fprintf(f, "%d %d 1 %d\n", w, h, pd);
 		for (size_t k = 0; k < ns; k++) fprintf(f, "%.9g\n", x[k]);   /* planar */

@@ -23,8 +23,8 @@
  *    integers), .csv, .txt, .raw (the samples, interleaved), .asc, .npy, or
  *    the prefixes "TXT:" and "RAW:"; any other name, and a stdout that is not
  *    a terminal, get NumPy .npy.  A terminal stdout gets the one-line
- *    "IMAGE wxh,pd float" summary.  FLO, JUV (.uv), farbfeld, PCM and LUM
- *    files are read too.
+ *    "IMAGE wxh,pd float" summary.  FLO, JUV (.uv), farbfeld, PCM, LUM and
+ *    MegaWave RIM files are read too, and ".mw" writes a RIM float image.
  *
  * Errors print a message and return NULL / nonzero; nothing exits.
  */

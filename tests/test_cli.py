@@ -331,7 +331,7 @@ def test_raw_too_small_fails(harness, tmp_path):
 _MORE_SHAPES = {"img2": (5, 6, 2), "img3": (4, 5, 3), "img1": (3, 7, 1)}
 
 
-@pytest.mark.parametrize("key", ["uv", "flo", "raw", "txt_prefix", "raw_prefix"])
+@pytest.mark.parametrize("key", ["uv", "flo", "raw", "txt_prefix", "raw_prefix", "mw"])
 def test_more_writers_match_reference_bytes(harness, tmp_path, key):
     """.uv and .flo (two channels), .raw, and the TXT: and RAW: name prefixes
     (iio.c:4110-4148, 4277-4334, 6166-6307), byte for byte."""
@@ -356,7 +356,8 @@ def test_flow_formats_read_like_reference(harness, tmp_path, key):
     assert np.array_equal(got.view(np.uint32), np.array(want["out"], np.float32).reshape(want["shape"]).view(np.uint32))
 
 
-@pytest.mark.parametrize("key", ["ffd", "pcm", "p7", "p9", "p9_16", "p2_float", "lum", "lum12"])
+@pytest.mark.parametrize("key", ["ffd", "pcm", "p7", "p9", "p9_16", "p2_float", "lum", "lum12", "rim_ir",
+                                 "rim_mi", "rim_im", "rim_we", "rim_vi"])
 def test_farbfeld_and_pcm_read_like_reference(harness, tmp_path, key):
     """farbfeld, PCM, iio's n-channel PNM variants P7/P9 and ASCII PNM
     samples read as floats, as the reference reads them."""
@@ -366,3 +367,19 @@ def test_farbfeld_and_pcm_read_like_reference(harness, tmp_path, key):
     got = _read_with(harness, tmp_path, src, "")
     assert list(got.shape) == want["shape"]
     assert np.array_equal(got.view(np.uint32), np.array(want["out"], np.float32).reshape(want["shape"]).view(np.uint32))
+
+
+def test_rim_swapped_float_image_reads_as_its_twin(harness, tmp_path):
+    """An "RI" float image (bytes swapped) reads as the "IR" one with the same
+    samples (the reference aborts on "RI" files, so this case is not pinned)."""
+    d = _fixtures("io_more.json")["read"]["rim_ir"]
+    ir = bytes(d["bytes"])
+    w = int.from_bytes(ir[4:6], "big")
+    h = int.from_bytes(ir[6:8], "big")
+    body = np.frombuffer(ir[8 + 56 + 3:], "<f4")
+    ri = (b"RI" + (3).to_bytes(2, "little") + w.to_bytes(2, "little") + h.to_bytes(2, "little") + bytes(56) + b"abc"
+          + body.astype(">f4").tobytes())
+    src = str(tmp_path / "in.rim")
+    open(src, "wb").write(ri)
+    got = _read_with(harness, tmp_path, src, "")
+    assert np.array_equal(got.view(np.uint32), np.array(d["out"], np.float32).reshape(d["shape"]).view(np.uint32))
