@@ -419,6 +419,35 @@ static int read_rim(raw_image *x, const unsigned char *b, size_t n)
 	return 0;
 }
 
+/* ---- RAT (radar): bytes 04 00 00 00, then 30 32-bit fields of which the
+ * third to sixth are d, width, height and the variant (only 6), then
+ * width x height pixels of 2 d^2 floats (iio.c:3185-3214) */
+static int read_rat(raw_image *x, const unsigned char *b, size_t n)
+{
+	if (n < 124) return 1;
+	int32_t d, w, h, var;
+	memcpy(&d, b + 8, 4);
+	memcpy(&w, b + 12, 4);
+	memcpy(&h, b + 16, 4);
+	memcpy(&var, b + 20, 4);
+	if (var != 6) {
+		fprintf(stderr, "imageio: RAT option var=%d not implemented\n", var);
+		return 1;
+	}
+	if (d <= 0 || w <= 0 || h <= 0) return 1;
+	const size_t pd = 2 * (size_t)d * d, ns = (size_t)w * h * pd;
+	if (n < 124 + 4 * ns) return 1;
+	x->v = xcalloc(ns, sizeof(double));
+	if (!x->v) return 2;
+	for (size_t k = 0; k < ns; k++) {
+		float v;
+		memcpy(&v, b + 124 + 4 * k, 4);
+		x->v[k] = v;
+	}
+	x->w = w; x->h = h; x->pd = (int)pd; x->type = T_F32;
+	return 0;
+}
+
 /* ---- LUM: "FLOA" at byte 8 -- big-endian 16-bit width and height at bytes
  * 2 and 6, big-endian floats from byte 3988 -- or "12LI" -- little-endian
  * 32-bit width and height at 0 and 4, 16-bit samples from byte 11968
@@ -992,6 +1021,7 @@ static int read_core(const char *name, raw_image *x)
 			(b[0] == 'R' && b[1] == 'I' && !(n >= 4 && b[2] == 'F' && b[3] == 'F'))))
 		r = read_rim(x, b, n);
 	else if (n >= 4 && !memcmp(b, "PIEH", 4)) r = read_flo(x, b, n);
+	else if (n >= 4 && b[0] == 4 && b[1] == 0 && b[2] == 0 && b[3] == 0) r = read_rat(x, b, n);
 	else if (n >= 4 && !memcmp(b, "farb", 4)) r = read_ffd(x, b, n);
 	else if (n >= 2 && b[0] == 'P' && b[1] == 'C') r = read_pcm(x, b, n);
 	else if (n >= 3 && !memcmp(b, "#UV", 3)) r = read_juv(x, b, n);

@@ -415,8 +415,13 @@ def io_more_cases():
             return tag + sh(0x4956) + it(np_) + it(nrow) + it(ncol) + it(1) + it(form) + it(0)
         rim_we = cc_head(b"WE", 3, 2, 4, 0x8001, False) + rng.integers(0, 256, 24, dtype=np.uint8).tobytes()
         rim_vi = cc_head(b"VI", 2, 3, 2, 0xc004, True) + (rng.standard_normal(12) * 3).astype("<f4").tobytes()
+        rat_head = bytearray(124)
+        rat_head[0:4] = (4).to_bytes(4, "little")
+        for off, v in ((8, 1), (12, 3), (16, 2), (20, 6)):   # d, width, height, variant
+            rat_head[off:off + 4] = v.to_bytes(4, "little")
+        rat = bytes(rat_head) + (rng.standard_normal(3 * 2 * 2) * 2).astype("<f4").tobytes()
         for key, data in (("ffd", ffd), ("pcm", pcm), ("p7", p7), ("p9", p9), ("p9_16", p9_16), ("p2_float", p2f),
-                          ("lum", lum), ("lum12", lum12), ("rim_ir", rim_ir),
+                          ("lum", lum), ("lum12", lum12), ("rim_ir", rim_ir), ("rat", rat),
                           ("rim_mi", rim_mi), ("rim_im", rim_im), ("rim_we", rim_we), ("rim_vi", rim_vi)):
             # (the reference aborts on "RI" files: it tells them only after 4 header bytes and its
             # reader asserts 2; rim_ri is read here and checked against rim_ir in tests/test_cli.py)
