@@ -419,6 +419,65 @@ static int read_rim(raw_image *x, const unsigned char *b, size_t n)
 	return 0;
 }
 
+/* ---- FITS ("SIMPLE  "): after the first 80-byte line, lines "KEY = value"
+ * up to "END " give BITPIX, NAXIS1 (width), NAXIS2 (height) and NAXIS3
+ * (channels); after padding lines the big-endian samples follow, in file
+ * order (iio.c:3453-3530) */
+static int read_fit(raw_image *x, const unsigned char *b, size_t n)
+{
+	int bitpix = -1, w = -1, h = -1, pd = 1;
+	size_t line = 0;   /* lines read after the first */
+	for (;;) {
+		line++;
+		const size_t o = 80 * line;
+		if (o + 80 > n) {
+			fprintf(stderr, "imageio: FITS reader failed at line %zu\n", line);
+			return 1;
+		}
+		char l[81] = {0}, k[81] = {0}, v[81] = {0};
+		memcpy(l, b + o, 80);
+		if (!memcmp(l, "END ", 4)) break;
+		if (sscanf(l, "%80s = %80s", k, v) != 2) continue;
+		if (!strcmp(k, "BITPIX")) bitpix = atoi(v);
+		if (!strcmp(k, "NAXIS1")) w = atoi(v);
+		if (!strcmp(k, "NAXIS2")) h = atoi(v);
+		if (!strcmp(k, "NAXIS3")) pd = atoi(v);
+	}
+	/* the data starts at line ceil(n / 36) * 36 (n the lines after the first),
+	 * right after "END" when n is a multiple of 36 */
+	const size_t off = 80 * ((line % 36) ? (line / 36 + 1) * 36 : line + 1);
+	int type, ss;
+	switch (bitpix) {
+	case 8: type = T_U8; ss = 1; break;
+	case 16: type = T_I16; ss = 2; break;
+	case 32: type = T_I32; ss = 4; break;
+	case -32: type = T_F32; ss = 4; break;
+	case -64: type = T_F64; ss = 8; break;
+	default:
+		fprintf(stderr, "imageio: unrecognized FITS BITPIX=%d\n", bitpix);
+		return 1;
+	}
+	if (w <= 0 || h <= 0 || pd <= 0) return 1;
+	const size_t ns = (size_t)w * h * pd;
+	if (n < off + ns * ss) return 1;
+	x->v = xcalloc(ns, sizeof(double));
+	if (!x->v) return 2;
+	for (size_t k = 0; k < ns; k++) {
+		unsigned char q[8];
+		memcpy(q, b + off + k * ss, ss);
+		swap_bytes(q, 1, ss);   /* big-endian file, little-endian host */
+		switch (type) {
+		case T_U8: x->v[k] = q[0]; break;
+		case T_I16: { int16_t t; memcpy(&t, q, 2); x->v[k] = t; break; }
+		case T_I32: { int32_t t; memcpy(&t, q, 4); x->v[k] = t; break; }
+		case T_F32: { float t; memcpy(&t, q, 4); x->v[k] = t; break; }
+		default: { double t; memcpy(&t, q, 8); x->v[k] = t; break; }
+		}
+	}
+	x->w = w; x->h = h; x->pd = pd; x->type = type;
+	return 0;
+}
+
 /* ---- RAT (radar): bytes 04 00 00 00, then 30 32-bit fields of which the
  * third to sixth are d, width, height and the variant (only 6), then
  * width x height pixels of 2 d^2 floats (iio.c:3185-3214) */
@@ -1022,6 +1081,7 @@ static int read_core(const char *name, raw_image *x)
 		r = read_rim(x, b, n);
 	else if (n >= 4 && !memcmp(b, "PIEH", 4)) r = read_flo(x, b, n);
 	else if (n >= 4 && b[0] == 4 && b[1] == 0 && b[2] == 0 && b[3] == 0) r = read_rat(x, b, n);
+	else if (n >= 8 && !memcmp(b, "SIMPLE  ", 8)) r = read_fit(x, b, n);
 	else if (n >= 4 && !memcmp(b, "farb", 4)) r = read_ffd(x, b, n);
 	else if (n >= 2 && b[0] == 'P' && b[1] == 'C') r = read_pcm(x, b, n);
 	else if (n >= 3 && !memcmp(b, "#UV", 3)) r = read_juv(x, b, n);

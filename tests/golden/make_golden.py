@@ -420,8 +420,26 @@ def io_more_cases():
         for off, v in ((8, 1), (12, 3), (16, 2), (20, 6)):   # d, width, height, variant
             rat_head[off:off + 4] = v.to_bytes(4, "little")
         rat = bytes(rat_head) + (rng.standard_normal(3 * 2 * 2) * 2).astype("<f4").tobytes()
+
+        # FITS: 80-byte header lines, padded to 36-line blocks, big-endian samples
+        def fits(cards, data):
+            lines = [c.ljust(80).encode() for c in ["SIMPLE  =                    T"] + cards + ["END"]]
+            head = b"".join(lines)
+            head += b" " * 80 * (-len(lines) % 36)   # standard: the header fills 36-line blocks
+            return head + data
+        fit_f32 = fits(["BITPIX  =                  -32 / float", "NAXIS   =                    2",
+                        "NAXIS1  =                    5", "NAXIS2  =                    3"],
+                       (rng.standard_normal(15) * 3).astype(">f4").tobytes())
+        fit_i16 = fits(["BITPIX  =                   16", "NAXIS   =                    3",
+                        "NAXIS1  =                    4", "NAXIS2  =                    2",
+                        "NAXIS3  =                    3"], rng.integers(-900, 900, 24, dtype=np.int16).astype(">i2").tobytes())
+        fit_f64 = fits(["BITPIX  =                  -64", "NAXIS   =                    2",
+                        "NAXIS1  =                    3", "NAXIS2  =                    2"]
+                       + [f"COMMENT card {i}" for i in range(40)],
+                       (rng.standard_normal(6) * 2).astype(">f8").tobytes())
         for key, data in (("ffd", ffd), ("pcm", pcm), ("p7", p7), ("p9", p9), ("p9_16", p9_16), ("p2_float", p2f),
                           ("lum", lum), ("lum12", lum12), ("rim_ir", rim_ir), ("rat", rat),
+                          ("fit_f32", fit_f32), ("fit_i16_3ch", fit_i16), ("fit_f64_long", fit_f64),
                           ("rim_mi", rim_mi), ("rim_im", rim_im), ("rim_we", rim_we), ("rim_vi", rim_vi)):
             # (the reference aborts on "RI" files: it tells them only after 4 header bytes and its
             # reader asserts 2; rim_ri is read here and checked against rim_ir in tests/test_cli.py)
