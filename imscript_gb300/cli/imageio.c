@@ -21,6 +21,11 @@ typedef struct {
 	double *v;      /* w*h*pd interleaved samples, exact in double      */
 } raw_image;
 
+/* transformations of an image as read (defined with IIO_TRANS below) */
+static void flip_leftright(raw_image *x);
+static void flip_topdown(raw_image *x);
+static int trim(raw_image *x, int left, int bottom, int right, int top);
+
 static void *xcalloc(size_t n, size_t s)
 {
 	void *p = calloc(n ? n : 1, s ? s : 1);
@@ -476,6 +481,86 @@ static int read_fit(raw_image *x, const unsigned char *b, size_t n)
 	}
 	x->w = w; x->h = h; x->pd = pd; x->type = type;
 	return 0;
+}
+
+/* ---- PDS ("PDS_"): "KEY = VALUE" label lines from byte 4 (printable
+ * characters only; a last line without newline is dropped; 1000 lines at
+ * most): RECORD_BYTES (RECORD_TYPE UNDEFINED means 1), the record of the
+ * object (^IMAGE, or IIO_PDS_OBJECT), and inside OBJECT = IMAGE: LINES,
+ * LINE_SAMPLES, SAMPLE_BITS, BANDS, SAMPLE_TYPE (REAL is float, else
+ * unsigned), the display directions (RIGHT flips left-right, DOWN top-down)
+ * and LINE_PREFIX_BYTES / LINE_SUFFIX_BYTES (columns around each line, cut
+ * off).  The samples, in this machine's byte order, start at record
+ * ^IMAGE - 1 (iio.c:2863-2990). */
+static int read_pds(raw_image *x, const unsigned char *b, size_t n)
+{
+	const char *oid = getenv("IIO_PDS_OBJECT");
+	if (!oid) oid = "^IMAGE";
+	long rbytes = -1, w = -1, h = -1, spp = 1, bps = 1, obj = -1, cl = 0, cr = 0;
+	int real = 0, in_object = 0, flip_h = 0, flip_v = 0;
+	size_t p = 4;
+	for (int cx = 0; cx < 1000; cx++) {
+		char line[1000], key[1000], value[1000];
+		size_t i = 0;
+		int end = 0;
+		for (;;) {
+			if (p >= n) { end = 1; break; }
+			const unsigned char c = b[p++];
+			if (c == '\n' || c == 0) break;
+			if (isprint(c) && i < sizeof line - 1) line[i++] = (char)c;
+		}
+		if (end) break;
+		line[i] = 0;
+		if (sscanf(line, "%999s = %999s", key, value) != 2) continue;
+		if (!strcmp(key, "RECORD_BYTES")) rbytes = atol(value);
+		if (!strcmp(key, "RECORD_TYPE") && strstr(value, "UNDEFINED")) rbytes = 1;
+		if (!strcmp(key, oid)) obj = atol(value);
+		if (!strcmp(key, "OBJECT") && !strcmp(value, oid + 1)) in_object = 1;
+		if (!in_object) continue;
+		if (!strcmp(key, "LINES")) h = atol(value);
+		if (!strcmp(key, "LINE_SAMPLES")) w = atol(value);
+		if (!strcmp(key, "SAMPLE_BITS")) bps = atol(value);
+		if (!strcmp(key, "BANDS")) spp = atol(value);
+		if (!strcmp(key, "SAMPLE_TYPE")) {
+			if (strstr(value, "REAL")) real = 1;
+			if (strstr(value, "UNSIGNED")) real = 0;
+			if (strstr(value, "INTEGER")) real = 0;
+		}
+		if (!strcmp(key, "SAMPLE_DISPLAY_DIRECTION")) flip_h = !strcmp(value, "RIGHT");
+		if (!strcmp(key, "LINE_DISPLAY_DIRECTION")) flip_v = !strcmp(value, "DOWN");
+		if (!strcmp(key, "LINE_PREFIX_BYTES")) cl = atol(value);
+		if (!strcmp(key, "LINE_SUFFIX_BYTES")) cr = atol(value);
+		if (!strcmp(key, "END_OBJECT") && !strcmp(value, oid + 1)) break;
+	}
+	w += cl + cr;
+	int type = -1;
+	if (real && bps == 32) type = T_F32;
+	if (real && bps == 64) type = T_F64;
+	if (!real && bps == 8) type = T_U8;
+	if (!real && bps == 16) type = T_U16;
+	if (!real && bps == 32) type = T_U32;
+	if (type < 0 || w <= 0 || h <= 0 || spp <= 0 || rbytes < 0 || obj < 1) {
+		fprintf(stderr, "imageio: unsupported or incomplete PDS label\n");
+		return 1;
+	}
+	const size_t ss = (size_t)bps / 8, ns = (size_t)w * h * spp, off = (size_t)rbytes * (obj - 1);
+	if (off + ns * ss > n) return 1;
+	x->v = xcalloc(ns, sizeof(double));
+	if (!x->v) return 2;
+	for (size_t k = 0; k < ns; k++) {
+		const unsigned char *q = b + off + k * ss;
+		switch (type) {
+		case T_U8: x->v[k] = q[0]; break;
+		case T_U16: { uint16_t t; memcpy(&t, q, 2); x->v[k] = t; break; }
+		case T_U32: { uint32_t t; memcpy(&t, q, 4); x->v[k] = t; break; }
+		case T_F32: { float t; memcpy(&t, q, 4); x->v[k] = t; break; }
+		default: { double t; memcpy(&t, q, 8); x->v[k] = t; break; }
+		}
+	}
+	x->w = (int)w; x->h = (int)h; x->pd = (int)spp; x->type = type;
+	if (flip_v) flip_topdown(x);
+	if (flip_h) flip_leftright(x);
+	return trim(x, (int)cl, 0, (int)cr, 0);
 }
 
 /* ---- RAT (radar): bytes 04 00 00 00, then 30 32-bit fields of which the
@@ -1082,6 +1167,7 @@ static int read_core(const char *name, raw_image *x)
 	else if (n >= 4 && !memcmp(b, "PIEH", 4)) r = read_flo(x, b, n);
 	else if (n >= 4 && b[0] == 4 && b[1] == 0 && b[2] == 0 && b[3] == 0) r = read_rat(x, b, n);
 	else if (n >= 8 && !memcmp(b, "SIMPLE  ", 8)) r = read_fit(x, b, n);
+	else if (n >= 4 && !memcmp(b, "PDS_", 4)) r = read_pds(x, b, n);
 	else if (n >= 4 && !memcmp(b, "farb", 4)) r = read_ffd(x, b, n);
 	else if (n >= 2 && b[0] == 'P' && b[1] == 'C') r = read_pcm(x, b, n);
 	else if (n >= 3 && !memcmp(b, "#UV", 3)) r = read_juv(x, b, n);

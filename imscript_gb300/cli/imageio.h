@@ -24,10 +24,10 @@
  *    the prefixes "TXT:" and "RAW:"; any other name, and a stdout that is not
  *    a terminal, get NumPy .npy.  A terminal stdout gets the one-line
  *    "IMAGE wxh,pd float" summary.  FLO, JUV (.uv), farbfeld, PCM, LUM, RAT,
- *    FITS and MegaWave RIM files are read too, and ".mw" writes a RIM float
- *    image.  Not read: iio's label formats PDS, VICAR, CCSD and GDAL VRT,
- *    and those that need libraries (PNG, TIFF, JPEG, EXR, WebP, HEIF, HDF5);
- *    BMP and DLM are not read by iio either.
+ *    FITS, PDS and MegaWave RIM files are read too, and ".mw" writes a RIM
+ *    float image.  Not read: iio's VICAR, CCSD and GDAL VRT, and the formats
+ *    that need libraries (PNG, TIFF, JPEG, EXR, WebP, HEIF, HDF5); BMP and
+ *    DLM are not read by iio either.
  *
  * Errors print a message and return NULL / nonzero; nothing exits.
  */

@@ -437,9 +437,28 @@ def io_more_cases():
                         "NAXIS1  =                    3", "NAXIS2  =                    2"]
                        + [f"COMMENT card {i}" for i in range(40)],
                        (rng.standard_normal(6) * 2).astype(">f8").tobytes())
+
+        # PDS: a label of KEY = VALUE lines, the samples at record ^IMAGE - 1
+        def pds(lines, record, nrec, data):
+            label = ("PDS_VERSION_ID = PDS3\n" + "".join(l + "\n" for l in lines) + "END\n").encode()
+            assert len(label) <= record * nrec
+            return label.ljust(record * nrec, b" ") + data
+        pds_f32 = pds(["RECORD_TYPE = FIXED_LENGTH", "RECORD_BYTES = 256", "^IMAGE = 3", "OBJECT = IMAGE",
+                       "LINES = 3", "LINE_SAMPLES = 4", "SAMPLE_BITS = 32", "SAMPLE_TYPE = PC_REAL",
+                       "BANDS = 1", "END_OBJECT = IMAGE"], 256, 2,
+                      (rng.standard_normal(12) * 5).astype("<f4").tobytes())
+        pds_u16 = pds(["RECORD_TYPE = FIXED_LENGTH", "RECORD_BYTES = 512", "^IMAGE = 2", "OBJECT = IMAGE",
+                       "LINES = 3", "LINE_SAMPLES = 4", "SAMPLE_BITS = 16", "SAMPLE_TYPE = LSB_UNSIGNED_INTEGER",
+                       "SAMPLE_DISPLAY_DIRECTION = RIGHT", "LINE_DISPLAY_DIRECTION = DOWN",
+                       "LINE_PREFIX_BYTES = 1", "BANDS = 1", "END_OBJECT = IMAGE"], 512, 1,
+                      rng.integers(0, 65536, 15, dtype=np.uint16).astype("<u2").tobytes())
+        pds_und = pds(["RECORD_TYPE = UNDEFINED", "^IMAGE = 301", "OBJECT = IMAGE", "LINES = 2",
+                       "LINE_SAMPLES = 5", "SAMPLE_BITS = 8", "SAMPLE_TYPE = UNSIGNED_INTEGER", "BANDS = 1",
+                       "END_OBJECT = IMAGE"], 300, 1, rng.integers(0, 256, 10, dtype=np.uint8).tobytes())
         for key, data in (("ffd", ffd), ("pcm", pcm), ("p7", p7), ("p9", p9), ("p9_16", p9_16), ("p2_float", p2f),
                           ("lum", lum), ("lum12", lum12), ("rim_ir", rim_ir), ("rat", rat),
                           ("fit_f32", fit_f32), ("fit_i16_3ch", fit_i16), ("fit_f64_long", fit_f64),
+                          ("pds_f32", pds_f32), ("pds_u16_flips_prefix", pds_u16), ("pds_undefined", pds_und),
                           ("rim_mi", rim_mi), ("rim_im", rim_im), ("rim_we", rim_we), ("rim_vi", rim_vi)):
             # (the reference aborts on "RI" files: it tells them only after 4 header bytes and its
             # reader asserts 2; rim_ri is read here and checked against rim_ir in tests/test_cli.py)
