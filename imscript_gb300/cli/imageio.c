@@ -563,6 +563,80 @@ static int read_pds(raw_image *x, const unsigned char *b, size_t n)
 	return trim(x, (int)cl, 0, (int)cr, 0);
 }
 
+/* ---- VICAR ("LBLSIZE="): the 9 characters after the tag give the label
+ * size n; the label up to byte n - 1 holds space-separated KEY=VALUE
+ * tokens: TYPE 'IMAGE' and ORG 'BSQ' required, FORMAT (BYTE, HALF 16-bit
+ * signed, FULL, REAL, DOUBL), NL lines, NS samples, NB bands, RECSIZE =
+ * NBB + NS x sample size, NBB bytes before each line, NLB records skipped,
+ * INTFMT 'HIGH' swapping 2- and 4-byte samples.  The NL x NB records
+ * follow the label, band after band, read as they come (iio.c:3298-3418). */
+static int read_vic(raw_image *x, const unsigned char *b, size_t n)
+{
+	if (n < 17) return 1;
+	char sz[10] = {0};
+	memcpy(sz, b + 8, 9);
+	const long lbl = atol(sz);
+	if (lbl < 18 || (size_t)lbl > n) return 1;
+	char *l = malloc((size_t)lbl);
+	if (!l) return 2;
+	memcpy(l, b + 17, (size_t)lbl - 18);   /* the label's last byte is dropped */
+	l[lbl - 18] = 0;
+	long recsize = -1, nl = -1, ns = -1, nb = -1, nbb = 0, nlb = 0;
+	char format[99] = "", type[99] = "", org[99] = "", ifmt[99] = "";
+	char *save = NULL;
+	for (char *tok = strtok_r(l, " ", &save); tok; tok = strtok_r(NULL, " ", &save)) {
+		char *eq = strchr(tok, '=');
+		if (!eq || eq == tok || !eq[1]) continue;
+		*eq = 0;
+		const char *k = tok, *v = eq + 1;
+		char vv[99];
+		sscanf(v, "%98s", vv);
+		if (!strcmp(k, "RECSIZE")) recsize = atol(vv);
+		if (!strcmp(k, "FORMAT")) snprintf(format, sizeof format, "%s", vv);
+		if (!strcmp(k, "TYPE")) snprintf(type, sizeof type, "%s", vv);
+		if (!strcmp(k, "ORG")) snprintf(org, sizeof org, "%s", vv);
+		if (!strcmp(k, "INTFMT")) snprintf(ifmt, sizeof ifmt, "%s", vv);
+		if (!strcmp(k, "NL")) nl = atol(vv);
+		if (!strcmp(k, "NS")) ns = atol(vv);
+		if (!strcmp(k, "NB")) nb = atol(vv);
+		if (!strcmp(k, "NBB")) nbb = atol(vv);
+		if (!strcmp(k, "NLB")) nlb = atol(vv);
+	}
+	free(l);
+	int t = -1, ss = 0;
+	if (!strcmp(format, "'BYTE'")) { t = T_U8; ss = 1; }
+	if (!strcmp(format, "'HALF'")) { t = T_I16; ss = 2; }
+	if (!strcmp(format, "'FULL'")) { t = T_I32; ss = 4; }
+	if (!strcmp(format, "'REAL'")) { t = T_F32; ss = 4; }
+	if (!strcmp(format, "'DOUBL'")) { t = T_F64; ss = 8; }
+	if (strcmp(type, "'IMAGE'") || strcmp(org, "'BSQ'") || recsize <= 0 || t < 0 || nl <= 0 || ns <= 0 ||
+			nb <= 0 || recsize != nbb + ns * ss) {
+		fprintf(stderr, "imageio: unsupported VICAR label\n");
+		return 1;
+	}
+	const size_t nrec = (size_t)nl * nb, off = (size_t)lbl + (size_t)nlb * recsize;
+	if (off + nrec * recsize > n) return 1;
+	const int swap = !strcmp(ifmt, "'HIGH'") && (ss == 2 || ss == 4);
+	x->v = xcalloc(nrec * ns, sizeof(double));
+	if (!x->v) return 2;
+	size_t k = 0;
+	for (size_t r = 0; r < nrec; r++)
+		for (long i = 0; i < ns; i++, k++) {
+			unsigned char q[8];
+			memcpy(q, b + off + r * recsize + nbb + i * ss, ss);
+			if (swap) swap_bytes(q, 1, ss);
+			switch (t) {
+			case T_U8: x->v[k] = q[0]; break;
+			case T_I16: { int16_t v; memcpy(&v, q, 2); x->v[k] = v; break; }
+			case T_I32: { int32_t v; memcpy(&v, q, 4); x->v[k] = v; break; }
+			case T_F32: { float v; memcpy(&v, q, 4); x->v[k] = v; break; }
+			default: { double v; memcpy(&v, q, 8); x->v[k] = v; break; }
+			}
+		}
+	x->w = (int)ns; x->h = (int)nl; x->pd = (int)nb; x->type = t;
+	return 0;
+}
+
 /* ---- RAT (radar): bytes 04 00 00 00, then 30 32-bit fields of which the
  * third to sixth are d, width, height and the variant (only 6), then
  * width x height pixels of 2 d^2 floats (iio.c:3185-3214) */
@@ -1168,6 +1242,7 @@ static int read_core(const char *name, raw_image *x)
 	else if (n >= 4 && b[0] == 4 && b[1] == 0 && b[2] == 0 && b[3] == 0) r = read_rat(x, b, n);
 	else if (n >= 8 && !memcmp(b, "SIMPLE  ", 8)) r = read_fit(x, b, n);
 	else if (n >= 4 && !memcmp(b, "PDS_", 4)) r = read_pds(x, b, n);
+	else if (n >= 8 && !memcmp(b, "LBLSIZE=", 8)) r = read_vic(x, b, n);
 	else if (n >= 4 && !memcmp(b, "farb", 4)) r = read_ffd(x, b, n);
 	else if (n >= 2 && b[0] == 'P' && b[1] == 'C') r = read_pcm(x, b, n);
 	else if (n >= 3 && !memcmp(b, "#UV", 3)) r = read_juv(x, b, n);

@@ -452,6 +452,20 @@ def io_more_cases():
                        "SAMPLE_DISPLAY_DIRECTION = RIGHT", "LINE_DISPLAY_DIRECTION = DOWN",
                        "LINE_PREFIX_BYTES = 1", "BANDS = 1", "END_OBJECT = IMAGE"], 512, 1,
                       rng.integers(0, 65536, 15, dtype=np.uint16).astype("<u2").tobytes())
+        # VICAR: "LBLSIZE=" and a 9-character size, KEY=VALUE tokens, then the records
+        def vic(n, tokens, records):
+            label = ("LBLSIZE=" + f"{n:<9d}" + " " + " ".join(tokens)).ljust(n)
+            assert len(label) == n
+            return label.encode() + records
+        vic_real = vic(256, ["FORMAT='REAL'", "TYPE='IMAGE'", "ORG='BSQ'", "NL=3", "NS=4", "NB=1", "NBB=0",
+                             "NLB=0", "RECSIZE=16", "INTFMT='LOW'"],
+                       (rng.standard_normal(12) * 4).astype("<f4").tobytes())
+        half = rng.integers(-3000, 3000, (3, 5), dtype=np.int16)
+        vic_half = vic(300, ["FORMAT='HALF'", "TYPE='IMAGE'", "ORG='BSQ'", "NL=3", "NS=5", "NB=1", "NBB=2",
+                             "NLB=1", "RECSIZE=12", "INTFMT='HIGH'"],
+                       bytes(12) + b"".join(b"\xaa\xbb" + row.astype(">i2").tobytes() for row in half))
+        vic_byte = vic(200, ["FORMAT='BYTE'", "TYPE='IMAGE'", "ORG='BSQ'", "NL=2", "NS=3", "NB=2", "NBB=0",
+                             "NLB=0", "RECSIZE=3"], rng.integers(0, 256, 12, dtype=np.uint8).tobytes())
         pds_und = pds(["RECORD_TYPE = UNDEFINED", "^IMAGE = 301", "OBJECT = IMAGE", "LINES = 2",
                        "LINE_SAMPLES = 5", "SAMPLE_BITS = 8", "SAMPLE_TYPE = UNSIGNED_INTEGER", "BANDS = 1",
                        "END_OBJECT = IMAGE"], 300, 1, rng.integers(0, 256, 10, dtype=np.uint8).tobytes())
@@ -459,6 +473,7 @@ def io_more_cases():
                           ("lum", lum), ("lum12", lum12), ("rim_ir", rim_ir), ("rat", rat),
                           ("fit_f32", fit_f32), ("fit_i16_3ch", fit_i16), ("fit_f64_long", fit_f64),
                           ("pds_f32", pds_f32), ("pds_u16_flips_prefix", pds_u16), ("pds_undefined", pds_und),
+                          ("vic_real", vic_real), ("vic_half_high_nbb_nlb", vic_half), ("vic_byte_2bands", vic_byte),
                           ("rim_mi", rim_mi), ("rim_im", rim_im), ("rim_we", rim_we), ("rim_vi", rim_vi)):
             # (the reference aborts on "RI" files: it tells them only after 4 header bytes and its
             # reader asserts 2; rim_ri is read here and checked against rim_ir in tests/test_cli.py)
