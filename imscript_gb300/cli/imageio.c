@@ -483,7 +483,8 @@ static int read_fit(raw_image *x, const unsigned char *b, size_t n)
 	return 0;
 }
 
-/* ---- PDS ("PDS_"): "KEY = VALUE" label lines from byte 4 (printable
+/* ---- PDS ("PDS_"), and CCSD ("CCSD3Z" at byte 0, 1 or 2, the same label
+ * language): "KEY = VALUE" label lines from byte 4 (8) (printable
  * characters only; a last line without newline is dropped; 1000 lines at
  * most): RECORD_BYTES (RECORD_TYPE UNDEFINED means 1), the record of the
  * object (^IMAGE, or IIO_PDS_OBJECT), and inside OBJECT = IMAGE: LINES,
@@ -492,13 +493,13 @@ static int read_fit(raw_image *x, const unsigned char *b, size_t n)
  * and LINE_PREFIX_BYTES / LINE_SUFFIX_BYTES (columns around each line, cut
  * off).  The samples, in this machine's byte order, start at record
  * ^IMAGE - 1 (iio.c:2863-2990). */
-static int read_pds(raw_image *x, const unsigned char *b, size_t n)
+static int read_pds(raw_image *x, const unsigned char *b, size_t n, size_t start)
 {
 	const char *oid = getenv("IIO_PDS_OBJECT");
 	if (!oid) oid = "^IMAGE";
 	long rbytes = -1, w = -1, h = -1, spp = 1, bps = 1, obj = -1, cl = 0, cr = 0;
 	int real = 0, in_object = 0, flip_h = 0, flip_v = 0;
-	size_t p = 4;
+	size_t p = start;
 	for (int cx = 0; cx < 1000; cx++) {
 		char line[1000], key[1000], value[1000];
 		size_t i = 0;
@@ -1241,7 +1242,9 @@ static int read_core(const char *name, raw_image *x)
 	else if (n >= 4 && !memcmp(b, "PIEH", 4)) r = read_flo(x, b, n);
 	else if (n >= 4 && b[0] == 4 && b[1] == 0 && b[2] == 0 && b[3] == 0) r = read_rat(x, b, n);
 	else if (n >= 8 && !memcmp(b, "SIMPLE  ", 8)) r = read_fit(x, b, n);
-	else if (n >= 4 && !memcmp(b, "PDS_", 4)) r = read_pds(x, b, n);
+	else if (n >= 4 && !memcmp(b, "PDS_", 4)) r = read_pds(x, b, n, 4);
+	else if (n >= 8 && (!memcmp(b, "CCSD3Z", 6) || !memcmp(b + 1, "CCSD3Z", 6) || !memcmp(b + 2, "CCSD3Z", 6)))
+		r = read_pds(x, b, n, 8);
 	else if (n >= 8 && !memcmp(b, "LBLSIZE=", 8)) r = read_vic(x, b, n);
 	else if (n >= 4 && !memcmp(b, "farb", 4)) r = read_ffd(x, b, n);
 	else if (n >= 2 && b[0] == 'P' && b[1] == 'C') r = read_pcm(x, b, n);

@@ -24,8 +24,8 @@
  *    the prefixes "TXT:" and "RAW:"; any other name, and a stdout that is not
  *    a terminal, get NumPy .npy.  A terminal stdout gets the one-line
  *    "IMAGE wxh,pd float" summary.  FLO, JUV (.uv), farbfeld, PCM, LUM, RAT,
- *    FITS, PDS, VICAR and MegaWave RIM files are read too, and ".mw" writes
- *    a RIM float image.  Not read: iio's CCSD and GDAL VRT, and the formats
+ *    FITS, PDS, CCSD, VICAR and MegaWave RIM files are read too, and ".mw"
+ *    writes a RIM float image.  Not read: iio's GDAL VRT, and the formats
  *    that need libraries (PNG, TIFF, JPEG, EXR, WebP, HEIF, HDF5); BMP and
  *    DLM are not read by iio either.
  *

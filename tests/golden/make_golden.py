@@ -466,6 +466,11 @@ def io_more_cases():
                        bytes(12) + b"".join(b"\xaa\xbb" + row.astype(">i2").tobytes() for row in half))
         vic_byte = vic(200, ["FORMAT='BYTE'", "TYPE='IMAGE'", "ORG='BSQ'", "NL=2", "NS=3", "NB=2", "NBB=0",
                              "NLB=0", "RECSIZE=3"], rng.integers(0, 256, 12, dtype=np.uint8).tobytes())
+        ccsd_label = ("CCSD3ZF0000100000001NJPL3IF0PDS200000001 = SFDU_LABEL\nRECORD_TYPE = FIXED_LENGTH\n"
+                      "RECORD_BYTES = 256\n^IMAGE = 2\nOBJECT = IMAGE\nLINES = 2\nLINE_SAMPLES = 3\n"
+                      "SAMPLE_BITS = 32\nSAMPLE_TYPE = PC_REAL\nEND_OBJECT = IMAGE\nEND\n").encode()
+        assert len(ccsd_label) <= 256
+        ccsd = ccsd_label.ljust(256, b" ") + (rng.standard_normal(6) * 2).astype("<f4").tobytes()
         pds_und = pds(["RECORD_TYPE = UNDEFINED", "^IMAGE = 301", "OBJECT = IMAGE", "LINES = 2",
                        "LINE_SAMPLES = 5", "SAMPLE_BITS = 8", "SAMPLE_TYPE = UNSIGNED_INTEGER", "BANDS = 1",
                        "END_OBJECT = IMAGE"], 300, 1, rng.integers(0, 256, 10, dtype=np.uint8).tobytes())
@@ -474,6 +479,7 @@ def io_more_cases():
                           ("fit_f32", fit_f32), ("fit_i16_3ch", fit_i16), ("fit_f64_long", fit_f64),
                           ("pds_f32", pds_f32), ("pds_u16_flips_prefix", pds_u16), ("pds_undefined", pds_und),
                           ("vic_real", vic_real), ("vic_half_high_nbb_nlb", vic_half), ("vic_byte_2bands", vic_byte),
+                          ("ccsd", ccsd),
                           ("rim_mi", rim_mi), ("rim_im", rim_im), ("rim_we", rim_we), ("rim_vi", rim_vi)):
             # (the reference aborts on "RI" files: it tells them only after 4 header bytes and its
             # reader asserts 2; rim_ri is read here and checked against rim_ir in tests/test_cli.py)

@@ -359,7 +359,7 @@ def test_flow_formats_read_like_reference(harness, tmp_path, key):
 @pytest.mark.parametrize("key", ["ffd", "pcm", "p7", "p9", "p9_16", "p2_float", "lum", "lum12", "rim_ir",
                                  "rim_mi", "rim_im", "rim_we", "rim_vi", "rat", "fit_f32", "fit_i16_3ch",
                                  "fit_f64_long", "pds_f32", "pds_u16_flips_prefix", "pds_undefined", "vic_real",
-                                 "vic_half_high_nbb_nlb", "vic_byte_2bands"])
+                                 "vic_half_high_nbb_nlb", "vic_byte_2bands", "ccsd"])
 def test_farbfeld_and_pcm_read_like_reference(harness, tmp_path, key):
     """farbfeld, PCM, iio's n-channel PNM variants P7/P9 and ASCII PNM
     samples read as floats, as the reference reads them."""
