@@ -940,6 +940,78 @@ static int flip(raw_image *x, const char *s)
 }
 
 static int read_core(const char *name, raw_image *x);
+static int read_raw(const char *name, raw_image *x);
+static float gray_of(const double *p, int type);
+
+/* ---- GDAL VRT ("<VRT"): the first line's rasterXSize and rasterYSize give
+ * the size of one float channel; then every DstRect (xOff, yOff, xSize,
+ * ySize) with a "<SourceFilename attributes>name<" tag pastes that image,
+ * read as one gray channel from the VRT's directory, at the offset
+ * (iio.c:3085-3160).  Pixels no tile covers read 0. */
+static int xml_attr(int *out, const char *line, const char *tag, const char *attr)
+{
+	if (!strstr(line, tag)) return 0;
+	const char *a = strstr(line, attr);
+	if (!a) return 0;
+	*out = atoi(a + 2 + strlen(attr));
+	return 1;
+}
+
+static int read_vrt(raw_image *x, const unsigned char *b, size_t n, const char *name)
+{
+	char *text = malloc(n + 1);
+	if (!text) return 2;
+	memcpy(text, b, n);
+	text[n] = 0;
+	char *save = NULL, *line = strtok_r(text + 4, "\n", &save);   /* lines (empty ones skipped) */
+	int w = 0, h = 0, cx = 0;
+	if (line) {
+		cx += xml_attr(&w, line, "Dataset", "rasterXSize");
+		cx += xml_attr(&h, line, "Dataset", "rasterYSize");
+	}
+	if (!line || w <= 0 || h <= 0 || cx != 2) { free(text); return 1; }
+	x->v = xcalloc((size_t)w * h, sizeof(double));
+	if (!x->v) { free(text); return 2; }
+	x->w = w; x->h = h; x->pd = 1; x->type = T_F32;
+	char dir[4096];
+	snprintf(dir, sizeof dir, "%s", strcmp(name, "-") ? name : ".");
+	char *slash = strrchr(dir, '/');
+	if (slash) *slash = 0; else snprintf(dir, sizeof dir, ".");
+	int pos[4] = {0, 0, 0, 0}, pos_cx = 0, has_fname = 0, r = 0;
+	char fname[4096] = "";
+	while (!r && (line = strtok_r(NULL, "\n", &save))) {
+		pos_cx += xml_attr(pos + 0, line, "DstRect", "xOff");
+		pos_cx += xml_attr(pos + 1, line, "DstRect", "yOff");
+		pos_cx += xml_attr(pos + 2, line, "DstRect", "xSize");
+		pos_cx += xml_attr(pos + 3, line, "DstRect", "ySize");
+		char tmp[4096];
+		if (sscanf(line, " <SourceFilename %*[^>]>%4095[^<]s</SourceFilename>", tmp) == 1) {
+			snprintf(fname, sizeof fname, "%s", tmp);
+			has_fname++;
+		}
+		if (pos_cx == 4 && has_fname == 1) {
+			pos_cx = has_fname = 0;
+			char full[8200];
+			snprintf(full, sizeof full, "%s/%s", dir, fname);
+			raw_image t = {0};
+			r = read_raw(full, &t);
+			if (!r && t.pd != 1 && t.pd != 3 && t.pd != 4) {
+				fprintf(stderr, "imageio: non-scalarizable image \"%s\"\n", full);
+				r = 1;
+			}
+			for (int j = 0; !r && j < pos[3]; j++)
+				for (int i = 0; i < pos[2]; i++) {
+					const int ii = i + pos[0], jj = j + pos[1];
+					if (ii < 0 || jj < 0 || ii >= w || jj >= h || i >= t.w || j >= t.h) continue;
+					const double *q = t.v + ((size_t)j * t.w + i) * t.pd;
+					x->v[(size_t)jj * w + ii] = t.pd == 1 ? (float)q[0] : gray_of(q, t.type);
+				}
+			free(t.v);
+		}
+	}
+	free(text);
+	return r;
+}
 
 /* ---- RAW: headerless binary samples described by a list of one-letter
  * fields, "RAW[w640,h480,p3,tuint16,e1]:file" or the IIO_RAW variable
@@ -1246,6 +1318,7 @@ static int read_core(const char *name, raw_image *x)
 	else if (n >= 8 && (!memcmp(b, "CCSD3Z", 6) || !memcmp(b + 1, "CCSD3Z", 6) || !memcmp(b + 2, "CCSD3Z", 6)))
 		r = read_pds(x, b, n, 8);
 	else if (n >= 8 && !memcmp(b, "LBLSIZE=", 8)) r = read_vic(x, b, n);
+	else if (n >= 4 && !memcmp(b, "<VRT", 4)) r = read_vrt(x, b, n, name);
 	else if (n >= 4 && !memcmp(b, "farb", 4)) r = read_ffd(x, b, n);
 	else if (n >= 2 && b[0] == 'P' && b[1] == 'C') r = read_pcm(x, b, n);
 	else if (n >= 3 && !memcmp(b, "#UV", 3)) r = read_juv(x, b, n);

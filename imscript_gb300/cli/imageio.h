@@ -24,9 +24,9 @@
  *    the prefixes "TXT:" and "RAW:"; any other name, and a stdout that is not
  *    a terminal, get NumPy .npy.  A terminal stdout gets the one-line
  *    "IMAGE wxh,pd float" summary.  FLO, JUV (.uv), farbfeld, PCM, LUM, RAT,
- *    FITS, PDS, CCSD, VICAR and MegaWave RIM files are read too, and ".mw"
- *    writes a RIM float image.  Not read: iio's GDAL VRT, and the formats
- *    that need libraries (PNG, TIFF, JPEG, EXR, WebP, HEIF, HDF5); BMP and
+ *    FITS, PDS, CCSD, VICAR, GDAL VRT and MegaWave RIM files are read too,
+ *    and ".mw" writes a RIM float image.  Not read: the formats for which
+ *    iio needs libraries (PNG, TIFF, JPEG, EXR, WebP, HEIF, HDF5); BMP and
  *    DLM are not read by iio either.
  *
  * Errors print a message and return NULL / nonzero; nothing exits.

@@ -489,9 +489,34 @@ def io_more_cases():
             subprocess.run([O.REF_BIN, "-i", src, "-n", "0", "-o", o], check=True, capture_output=True)
             a = np.load(o)
             res["read"][key] = {"shape": list(a.shape), "out": a.ravel().tolist(), "bytes": list(data)}
+        # GDAL VRT: three tiles pasted into an 8x5 raster, read from the VRT's directory
+        tiles = {"a.npy": (rng.standard_normal((3, 4)) * 3).astype(np.float32),
+                 "b.npy": (rng.random((3, 4, 3)) * 100).astype(np.float32),
+                 "c.npy": rng.integers(0, 256, (2, 8), dtype=np.uint8)}
+        vrt_text = ('<VRTDataset rasterXSize="8" rasterYSize="5">\n'
+                    '  <VRTRasterBand dataType="Float32" band="1">\n')
+        for fname, (x0, y0, w, h) in (("a.npy", (0, 0, 4, 3)), ("b.npy", (4, 0, 4, 3)), ("c.npy", (0, 3, 8, 2))):
+            vrt_text += ('    <SimpleSource>\n'
+                         f'      <SourceFilename relativeToVRT="1">{fname}</SourceFilename>\n'
+                         f'      <SrcRect xOff="0" yOff="0" xSize="{w}" ySize="{h}"/>\n'
+                         f'      <DstRect xOff="{x0}" yOff="{y0}" xSize="{w}" ySize="{h}"/>\n'
+                         '    </SimpleSource>\n')
+        vrt_text += "  </VRTRasterBand>\n</VRTDataset>\n"
+        vd = os.path.join(td, "vrt")
+        os.makedirs(vd)
+        tile_bytes = {}
+        for fname, a in tiles.items():
+            np.save(os.path.join(vd, fname), a)
+            tile_bytes[fname] = list(open(os.path.join(vd, fname), "rb").read())
+        open(os.path.join(vd, "m.vrt"), "w").write(vrt_text)
+        o = os.path.join(td, "back.npy")
+        subprocess.run([O.REF_BIN, "-i", os.path.join(vd, "m.vrt"), "-n", "0", "-o", o], check=True,
+                       capture_output=True)
+        a = np.load(o)
+        res["vrt"] = {"text": vrt_text, "tiles": tile_bytes, "shape": list(a.shape), "out": a.ravel().tolist()}
     with open(os.path.join(OUT, "io_more.json"), "w") as fh:
         json.dump(res, fh)
-    return len(res["write"]) + len(res["read"])
+    return len(res["write"]) + len(res["read"]) + 1
 
 
 def mini_cases(rng):

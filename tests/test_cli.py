@@ -385,3 +385,17 @@ def test_rim_swapped_float_image_reads_as_its_twin(harness, tmp_path):
     open(src, "wb").write(ri)
     got = _read_with(harness, tmp_path, src, "")
     assert np.array_equal(got.view(np.uint32), np.array(d["out"], np.float32).reshape(d["shape"]).view(np.uint32))
+
+
+def test_vrt_mosaic_reads_like_reference(harness, tmp_path):
+    """A GDAL VRT pasting three tiles (gray float, colour float, bytes) read
+    from its directory (iio.c:3085-3160), as the reference reads it."""
+    d = _fixtures("io_more.json")["vrt"]
+    vd = tmp_path / "vrt"
+    vd.mkdir()
+    for fname, data in d["tiles"].items():
+        open(vd / fname, "wb").write(bytes(data))
+    open(vd / "m.vrt", "w").write(d["text"])
+    got = _read_with(harness, tmp_path, str(vd / "m.vrt"), "")
+    assert list(got.shape) == d["shape"]
+    assert np.array_equal(got.view(np.uint32), np.array(d["out"], np.float32).reshape(d["shape"]).view(np.uint32))
