@@ -16,7 +16,7 @@
 // the cells still far enough from the region's edge; after them the tile is
 // exact and alone is written back (double-buffered: a tile's halo is other
 // tiles' pixels).  The launches of a call are one CUDA graph.  The kernel is
-// instantiated for NN = 4, 8, 16 and 32 with the neighbour table as
+// instantiated for NN = 4, 6, 8, 16, 26 and 32 with the neighbour table as
 // compile-time constants (any other NN reads it at run time), and a tile
 // whose region lies wholly in the image skips the bounds tests.  Every float
 // operation is the reference's, in its order (round-to-nearest intrinsics, no
@@ -436,8 +436,9 @@ int amle_run(simpois_ctx *ctx, float *out, const float *in, int w, int h, int pd
 	if (total > 0) {
 		const int Rmax = SP_TILE + 2 * reach * spl;
 		const int smem_max = amle_smem(Rmax, a.m);
-		auto kern = nn == 4 ? k_amle_fused<4> : nn == 8 ? k_amle_fused<8> : nn == 16 ? k_amle_fused<16>
-				: nn == 32 ? k_amle_fused<32> : k_amle_fused<0>;
+		auto kern = nn == 4 ? k_amle_fused<4> : nn == 6 ? k_amle_fused<6> : nn == 8 ? k_amle_fused<8>
+				: nn == 16 ? k_amle_fused<16> : nn == 26 ? k_amle_fused<26> : nn == 32 ? k_amle_fused<32>
+				: k_amle_fused<0>;
 		SP_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max));
 		char buf[256];
 		snprintf(buf, sizeof buf, "%p/%p/%p/%p/%d/%d/%d/%d/%d/%d", (void *)A, (const void *)in,
