@@ -107,6 +107,10 @@ static int read_npy(raw_image *x, const unsigned char *b, size_t n)
 	}
 	if (r < 5) pd = 1;
 	if (r < 4) w = h, h = 1;   /* a 1-D array is one row */
+	if (h <= 0 || w <= 0 || pd <= 0) {
+		fprintf(stderr, "imageio: badly formed npy header (shape not positive)\n");
+		return 2;
+	}
 	if (h == 1 && w > 1 && pd > 1) { h = w; w = pd; pd = 1; }
 	const char *d = descr;
 	if (*d == '<' || *d == '>' || *d == '=' || *d == '|') {

@@ -117,7 +117,10 @@ __global__ void k_resid_noalloc(const float *__restrict__ u, const float *__rest
 std::mutex g_na_mu;
 double *g_na_addr[NA_MAX_DEVICES];   // device address of the scratch, per device
 
-// Device address of the scratch on the current device (looked up once).
+// Device address of the scratch on the current device, looked up once per
+// device and kept for the process's life.  A cudaDeviceReset unloads the
+// library's module and with it this address: the entry point is not for use
+// on a device after a reset (documented in the header).
 int scratch_address(simpois_ctx *ctx, double **out)
 {
 	std::lock_guard<std::mutex> lock(g_na_mu);

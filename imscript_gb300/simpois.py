@@ -120,6 +120,43 @@ def solve_batch(images, *, rtol=1e-6, tstep=0.25, max_iter=0, flags=0, allow=(_l
     return outs, reps
 
 
+def solve_batch_host(images, *, rtol=1e-6, tstep=0.25, max_iter=0, flags=0, allow=(_lib.OK,), outs=None,
+                     device=0):
+    """Batched converged solve of numpy images in host memory (page-locked
+    ones move fastest) through simpois_solve_batch_host: the copies to and
+    from the device are part of the call.  ``images`` as in ``solve_batch``;
+    returns (outputs, reports)."""
+    items = []
+    for k, it in enumerate(images):
+        if isinstance(it, (tuple, list)):
+            g, f = it[0], (it[1] if len(it) > 1 else None)
+            t = it[2] if len(it) > 2 else tstep
+        else:
+            g, f, t = it, None, tstep
+        if not (isinstance(g, np.ndarray) and g.dtype == np.float32 and g.flags.c_contiguous):
+            raise ValueError(f"image {k}: contiguous float32 numpy array expected")
+        if f is not None and (f.shape != g.shape or f.dtype != np.float32 or not f.flags.c_contiguous):
+            raise ValueError(f"image {k}: data term must match the image")
+        items.append((g, f, t))
+    if outs is None:
+        outs = [np.empty_like(g) for g, _, _ in items]
+    arr = (_lib.Image * len(items))()
+    total = 0
+    for k, (g, f, t) in enumerate(items):
+        pd, h, w = _shape3(g)
+        if outs[k].shape != g.shape or outs[k].dtype != np.float32 or not outs[k].flags.c_contiguous:
+            raise ValueError(f"output {k} must match image {k}")
+        arr[k] = _lib.Image(g.ctypes.data, f.ctypes.data if f is not None else None, outs[k].ctypes.data,
+                            w, h, pd, float(t), float(rtol))
+        total += pd
+    reps = (_lib.Report * max(1, total))()
+    prm = _lib.default_params(rtol=float(rtol), max_iter=int(max_iter), flags=int(flags), tstep=float(tstep))
+    ctx = context(device)
+    rc = _lib.load().simpois_solve_batch_host(ctx.handle, arr, len(items), ctypes.byref(prm), reps)
+    ctx.check(rc, allow)
+    return outs, [reps[k].as_dict() for k in range(total)]
+
+
 def autotune(images, *, rtol=1e-6, tstep=0.25, max_iter=0, flags=0, allow=(_lib.OK,), outs=None):
     """``solve_batch`` that also times the fused V-cycle's hand-over sizes and
     keeps the fastest for later batches of the same shapes on this context.
@@ -171,7 +208,19 @@ def _batch(images, rtol, tstep, max_iter, flags, allow, outs, tune):
 
 def residual(u, g, f=None, kind=0):
     """FP64 relative residual of a float output per channel (CUDA tensors)."""
+    import torch
     pd, h, w = _shape3(g)
+    for name, t in (("u", u), ("g", g), ("f", f)):
+        if t is None:
+            continue
+        if not t.is_cuda or t.device != g.device:
+            raise ValueError(f"residual: {name} must be a CUDA tensor on {g.device}")
+        if t.dtype != torch.float32:
+            raise TypeError(f"residual: {name} must be float32, got {t.dtype}")
+        if tuple(t.shape[-2:]) != (h, w) or t.numel() != pd * h * w:
+            raise ValueError(f"residual: {name} has shape {tuple(t.shape)}, expected {(pd, h, w)}")
+    u, g = u.contiguous(), g.contiguous()
+    f = f.contiguous() if f is not None else None
     rel = (ctypes.c_double * pd)()
     bn = (ctypes.c_double * pd)()
     ctx = context(g.device.index or 0, _torch_stream(g))

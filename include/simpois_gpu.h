@@ -29,6 +29,8 @@
 #ifndef SIMPOIS_GPU_H
 #define SIMPOIS_GPU_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -154,6 +156,14 @@ int simpois_solve_device(simpois_ctx *ctx, float *out, const float *in,
 int simpois_solve_batch(simpois_ctx *ctx, const simpois_image *images, int n,
 		const simpois_params *params, simpois_report *reports);
 
+/* simpois_solve_batch with every image's in, dat and out in HOST memory (the
+ * batched form of poisson_solver_separable, simpois.c:288-302, over many
+ * images): the inputs go to the device, the batch is solved, the outputs come
+ * back; the call returns when they are written.  Page-locked buffers move at
+ * the link's full rate. */
+int simpois_solve_batch_host(simpois_ctx *ctx, const simpois_image *images,
+		int n, const simpois_params *params, simpois_report *reports);
+
 /* FP64 relative residual of a float output `u` (device pointers) for every
  * channel: kind 0 = 5-point -Laplacian, 1 = 13-point bilaplacian; unknowns
  * are the NaN pixels of `in`.  rel and bnorm receive pd values (host). */
@@ -167,8 +177,11 @@ int simpois_residual_device(simpois_ctx *ctx, const float *u, const float *in,
  * must not enter an allocator.  Its scratch is a fixed 1 MiB + 4 KiB array
  * inside the library (held on each GPU that loads the library until exit);
  * at most 16,777,216 pixels per channel and 64 channels, else SIMPOIS_EINVAL.
- * The first call on a device looks up the array's device address: make it
- * before any stream capture on that device.  All calls share the array, so
+ * The first call on a device looks up the array's device address and keeps
+ * it for the life of the process; a cudaDeviceReset invalidates it, so do not
+ * call this entry point on a device after resetting it.  Every call ends by
+ * synchronising ctx's stream (the sums come back to the host), so it cannot be
+ * called while that stream is being captured.  All calls share the array, so
  * calls that overlap on the GPU race: serialise them. */
 int simpois_residual_device_noalloc(simpois_ctx *ctx, const float *u,
 		const float *in, const float *dat, int w, int h, int pd, int kind,
@@ -189,7 +202,7 @@ int simpois_adjoint_device(simpois_ctx *ctx, const float *grad_out,
 /* AMLE fill (absolutely minimizing Lipschitz extension), the work of
  * imscript's amle (src/amle.c:196-246, replaces that function) on every
  * channel of a planar w x h x pd image whose NaN pixels are unknown: nn
- * neighbours of the reference's table (AMLE_NN: 4, 6, 8, 16, 24 or 32; 0..32),
+ * neighbours of the reference's table (AMLE_NN: 4, 6, 8, 16, 26 or 32; 0..32),
  * niter iterations (AMLE_NITER, the reference's default 100), init (may be
  * NULL, planar like in) the start of the upper iterate at the unknowns (the
  * AMLE_INIT image).  out receives the upper iterate, as the reference's.  The
@@ -222,6 +235,14 @@ int simpois_autotune(simpois_ctx *ctx, const simpois_image *images, int n,
 		const simpois_params *params, simpois_report *reports,
 		int *coarse_max);
 int simpois_set_coarse_max(simpois_ctx *ctx, int coarse_max);
+
+/* Device-memory budget of a context (no counterpart in the reference, whose
+ * xmalloc exits on an allocation failure, simpois.c:10-19).  A solve whose
+ * working set would take the context's device arena above `bytes` returns
+ * SIMPOIS_ENOMEM before it allocates, frees or launches anything, leaves the
+ * output untouched and the context usable; 0 removes the limit (the default).
+ * For services that share one GPU between several contexts. */
+int simpois_set_memory_limit(simpois_ctx *ctx, size_t bytes);
 
 /* Instrumentation (no counterpart in the reference): the number of kernel
  * launches this context has issued (a graph replay counts its kernel nodes),

@@ -50,12 +50,14 @@ class _Opts(ctypes.Structure):
 _lib = None
 
 
-def build(reference: bool | None = None) -> None:
-    """Compile the restatement (and the reference binary when its sources exist)."""
+def build(reference: bool | None = None, tree: str | None = None) -> None:
+    """Compile the restatement, and the reference binaries from the reference
+    tree ``tree`` (default: the SIMPOIS_REFERENCE_TREE environment variable)
+    when its sources are there."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    ref_src = os.environ.get("SIMPOIS_REFERENCE_TREE", "/root/reference")
+    ref_src = tree or os.environ.get("SIMPOIS_REFERENCE_TREE", "")
     if reference is None:
-        reference = os.path.isfile(os.path.join(ref_src, "src", "simpois.c"))
+        reference = bool(ref_src) and os.path.isfile(os.path.join(ref_src, "src", "simpois.c"))
     if reference:
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFERENCE={ref_src}"], check=True)
 
