@@ -28,6 +28,10 @@ int ctx_fail(simpois_ctx *ctx, int status, const char *fmt, ...)
 int ctx_arena_reserve(simpois_ctx *ctx, size_t bytes)
 {
 	if (bytes <= ctx->arena_cap) return SIMPOIS_OK;
+	// the caller's budget is checked before anything is freed or allocated
+	if (ctx->arena_limit && bytes > ctx->arena_limit)
+		return ctx_fail(ctx, SIMPOIS_ENOMEM, "%zu bytes of device memory needed, above the context's limit of %zu",
+				bytes, ctx->arena_limit);
 	if (ctx->arena) {
 		cudaStreamSynchronize(ctx->stream);
 		cudaFree(ctx->arena);
@@ -35,6 +39,7 @@ int ctx_arena_reserve(simpois_ctx *ctx, size_t bytes)
 		ctx->arena_cap = 0;
 	}
 	size_t cap = bytes + bytes / 8 + (1 << 20);
+	if (ctx->arena_limit && cap > ctx->arena_limit) cap = ctx->arena_limit;
 	if (cudaMalloc((void **)&ctx->arena, cap) != cudaSuccess) {
 		cudaGetLastError();
 		return ctx_fail(ctx, SIMPOIS_ENOMEM, "cannot allocate %zu bytes of device memory", cap);
@@ -594,6 +599,53 @@ int simpois_solve_batch(simpois_ctx *ctx, const simpois_image *images, int n, co
 	return solve_batch(ctx, images, n, params, reports, 0, nullptr);
 }
 
+int simpois_solve_batch_host(simpois_ctx *ctx, const simpois_image *images, int n, const simpois_params *params,
+		simpois_report *reports)
+{
+	if (!ctx || (!images && n > 0) || n < 0) return ctx_fail(ctx, SIMPOIS_EINVAL, "bad batch");
+	if (cudaSetDevice(ctx->device) != cudaSuccess) return ctx_fail(ctx, SIMPOIS_ECUDA, "cudaSetDevice");
+	// device slots of every image's in, dat and out, one after the other
+	std::vector<size_t> off(3 * (size_t)n);
+	size_t total = 0;
+	for (int k = 0; k < n; k++) {
+		const simpois_image &im = images[k];
+		if (!im.in || !im.out) return ctx_fail(ctx, SIMPOIS_EINVAL, "image %d: null buffer", k);
+		int rc = check_dims(ctx, im.w, im.h, im.pd);
+		if (rc) return rc;
+		const size_t slot = ((size_t)im.w * im.h * im.pd * sizeof(float) + 255) / 256 * 256;
+		off[3 * k] = total;
+		total += slot;
+		off[3 * k + 1] = total;
+		total += im.dat ? slot : 0;
+		off[3 * k + 2] = total;
+		total += slot;
+	}
+	int rc = ctx_io_reserve(ctx, total > 0 ? total : 256);
+	if (rc) return rc;
+	cudaStream_t s = ctx->stream;
+	std::vector<simpois_image> dev(images, images + n);
+	for (int k = 0; k < n; k++) {
+		const size_t bytes = (size_t)images[k].w * images[k].h * images[k].pd * sizeof(float);
+		dev[k].in = (const float *)(ctx->io + off[3 * k]);
+		dev[k].dat = images[k].dat ? (const float *)(ctx->io + off[3 * k + 1]) : nullptr;
+		dev[k].out = (float *)(ctx->io + off[3 * k + 2]);
+		SP_CUDA(ctx, cudaMemcpyAsync((void *)dev[k].in, images[k].in, bytes, cudaMemcpyHostToDevice, s));
+		if (images[k].dat)
+			SP_CUDA(ctx, cudaMemcpyAsync((void *)dev[k].dat, images[k].dat, bytes, cudaMemcpyHostToDevice, s));
+	}
+	const int st = solve_batch(ctx, dev.data(), n, params, reports, 0, nullptr);
+	if (st != SIMPOIS_OK && st != SIMPOIS_NOT_CONVERGED && st != SIMPOIS_BREAKDOWN) {
+		cudaStreamSynchronize(s);
+		return st;
+	}
+	for (int k = 0; k < n; k++) {
+		const size_t bytes = (size_t)images[k].w * images[k].h * images[k].pd * sizeof(float);
+		SP_CUDA(ctx, cudaMemcpyAsync(images[k].out, dev[k].out, bytes, cudaMemcpyDeviceToHost, s));
+	}
+	SP_CUDA(ctx, cudaStreamSynchronize(s));
+	return st;
+}
+
 int simpois_autotune(simpois_ctx *ctx, const simpois_image *images, int n, const simpois_params *params,
 		simpois_report *reports, int *coarse_max)
 {
@@ -609,6 +661,13 @@ int simpois_set_coarse_max(simpois_ctx *ctx, int coarse_max)
 	if (coarse_max != 0 && (coarse_max < 8 || coarse_max > 128))
 		return ctx_fail(ctx, SIMPOIS_EINVAL, "hand-over size %d outside 8..128", coarse_max);
 	ctx->coarse_max_fixed = coarse_max;
+	return SIMPOIS_OK;
+}
+
+int simpois_set_memory_limit(simpois_ctx *ctx, size_t bytes)
+{
+	if (!ctx) return SIMPOIS_EINVAL;
+	ctx->arena_limit = bytes;
 	return SIMPOIS_OK;
 }
 

@@ -27,6 +27,8 @@ struct simpois_ctx {
 	// device arena: one allocation reused by every solve on this context
 	char *arena = nullptr;
 	size_t arena_cap = 0;
+	// largest arena the context may hold (simpois_set_memory_limit; 0: none)
+	size_t arena_limit = 0;
 
 	// pinned host staging for small read-backs (counts, flags, reports)
 	char *pinned = nullptr;

@@ -67,8 +67,8 @@ class Image(ctypes.Structure):
 EXPORTS = [
     "simpois_default_params", "simpois_params_from_env", "simpois_create", "simpois_destroy",
     "simpois_strerror", "simpois_last_error", "simpois_solve", "simpois_solve_device",
-    "simpois_solve_batch", "simpois_residual_device", "simpois_residual_device_noalloc",
-    "simpois_adjoint_device", "simpois_autotune", "simpois_set_coarse_max",
+    "simpois_solve_batch", "simpois_solve_batch_host", "simpois_residual_device", "simpois_residual_device_noalloc",
+    "simpois_adjoint_device", "simpois_autotune", "simpois_set_coarse_max", "simpois_set_memory_limit",
     "simpois_amle_device", "simpois_amle", "amle",
     "simpois_launch_count", "simpois_reset_launch_count", "simpois_kernel_stats",
     "simpois_reset_kernel_stats",
@@ -112,6 +112,7 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
         L.simpois_solve.argtypes = [vp, vp, vp, vp, ip, ip, ip, P, R]
         L.simpois_solve_device.argtypes = [vp, vp, vp, vp, ip, ip, ip, P, R]
         L.simpois_solve_batch.argtypes = [vp, ctypes.POINTER(Image), ip, P, R]
+        L.simpois_solve_batch_host.argtypes = [vp, ctypes.POINTER(Image), ip, P, R]
         L.simpois_residual_device.argtypes = [vp, vp, vp, vp, ip, ip, ip, ip,
                                               ctypes.POINTER(ctypes.c_double),
                                               ctypes.POINTER(ctypes.c_double)]
@@ -119,6 +120,7 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
         L.simpois_adjoint_device.argtypes = [vp, vp, vp, ip, ip, ip, vp, vp, P, R]
         L.simpois_autotune.argtypes = [vp, ctypes.POINTER(Image), ip, P, R, ctypes.POINTER(ip)]
         L.simpois_set_coarse_max.argtypes = [vp, ip]
+        L.simpois_set_memory_limit.argtypes = [vp, ctypes.c_size_t]
         dp = ctypes.POINTER(ctypes.c_double)
         L.simpois_amle_device.argtypes = [vp, vp, vp, ip, ip, ip, ip, ip, vp, dp]
         L.simpois_amle.argtypes = [vp, vp, vp, ip, ip, ip, ip, ip, vp, dp]
@@ -188,6 +190,11 @@ class Context:
     def set_coarse_max(self, coarse_max: int):
         """Fix the fused V-cycle's hand-over size (8..128; 0: tuned or default)."""
         self.check(self._lib.simpois_set_coarse_max(self.handle, int(coarse_max)))
+
+    def set_memory_limit(self, nbytes: int):
+        """Largest device arena this context may hold (0: no limit); a solve
+        that needs more returns ENOMEM before it touches anything."""
+        self.check(self._lib.simpois_set_memory_limit(self.handle, int(nbytes)))
 
     def last_error(self) -> str:
         return self._lib.simpois_last_error(self.handle).decode()
