@@ -8,8 +8,13 @@ the reference's CG solves (cleant_cgpois.c:197-264):
 * kind 1: A = the 13-point bilaplacian with a single clamp
   (cleant_cgpois.c:91-121); b = -f_U - A_UK g_K.
 
-and solves it with ``scipy.sparse.linalg.spsolve`` in float64.  The result is
-the "FP64 converged solve" every GPU result is compared against.
+and solves it with a sparse LU factorisation (SuperLU through scipy) in
+float64.  The result is the "FP64 converged solve" every GPU result is
+compared against.  Large systems are ordered by geometric nested dissection
+first (the unknowns are split by separator lines as wide as the stencil's
+reach, recursively, separators last): for the 13-point operator on a
+1024 x 1024 hole this cuts the factor from 1.2e9 to 4e8 nonzeros and the time
+from 23 minutes to under one.
 """
 from __future__ import annotations
 
@@ -56,13 +61,59 @@ def build_system(g, f=None, kind=0):
     return A, b, idx
 
 
+def nested_dissection(ii, jj, reach, leaf=32):
+    """Elimination order of the points (ii, jj): the box of a set is cut
+    across its longer side by a separator band `reach` pixels wide (no
+    stencil couples the two halves through it); halves first, recursively,
+    then the band; sets of at most `leaf` points are kept in raster order."""
+    out = []
+    stack = [(np.arange(ii.size), 0)]
+    # explicit stack: (set, state); state 1 = its halves are done, emit the band
+    while stack:
+        idx, state = stack.pop()
+        if state == 1:
+            out.append(idx)
+            continue
+        if idx.size <= leaf:
+            out.append(idx)
+            continue
+        xi, yj = ii[idx], jj[idx]
+        x0, x1, y0, y1 = xi.min(), xi.max(), yj.min(), yj.max()
+        key, lo, hi = (xi, x0, x1) if x1 - x0 >= y1 - y0 else (yj, y0, y1)
+        c = (lo + hi) // 2
+        a, b = idx[key < c], idx[key >= c + reach]
+        if a.size == 0 or b.size == 0:
+            out.append(idx)
+            continue
+        sep = idx[(key >= c) & (key < c + reach)]
+        # popped in the order a, b, then the band
+        stack.append((sep, 1))
+        stack.append((b, 0))
+        stack.append((a, 0))
+    return np.concatenate(out) if out else np.zeros(0, np.int64)
+
+
+def lu_solve(A, b, idx, w, kind):
+    """x with A x = b (A symmetric positive definite, unknowns at flat
+    indices idx of a width-w grid)."""
+    n = idx.size
+    if n < 20000:
+        return spla.spsolve(A.tocsc(), b)
+    p = nested_dissection(idx % w, idx // w, 2 if kind == 1 else 1)
+    Ap = A[p][:, p].tocsc()
+    lu = spla.splu(Ap, permc_spec="NATURAL", diag_pivot_thresh=0.0, options=dict(SymmetricMode=True))
+    x = np.empty(n)
+    x[p] = lu.solve(b[p])
+    return x
+
+
 def solve(g, f=None, kind=0):
     """FP64 solution image (h, w): g at the knowns, the exact solve at the unknowns."""
     g = np.asarray(g, dtype=np.float32)
     out = g.astype(np.float64).ravel().copy()
     A, b, idx = build_system(g, f, kind)
     if idx.size:
-        out[idx] = spla.spsolve(A.tocsc(), b)
+        out[idx] = lu_solve(A, b, idx, g.shape[1], kind)
     return out.reshape(g.shape)
 
 

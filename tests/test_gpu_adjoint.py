@@ -2,9 +2,12 @@
 
 The loss is L = 0.5 * sum((u - T)^2) of the converged Poisson fill u of known
 pixels g and guidance G (f = div G).  References: the FP64 adjoint formula
-through scipy's direct solve, FP64 central finite differences on random
-coordinates, and torch autograd through a dense FP64 solve (64 x 64 crops).
-Tolerance: 1e-5 relative.
+through a sparse FP64 factorisation, FP64 central finite differences on 64
+coordinates (on a whole 1024 x 1024 image of the differentiation workload,
+and on a 64 x 64 one), and torch autograd through a dense FP64 solve (64 x 64
+crops).  Forward and adjoint solves run at rtol 1e-6, the setting the
+benchmark and autograd.fill use.  Tolerance: 1e-5 of the gradient's largest
+magnitude.
 """
 import numpy as np
 import pytest
@@ -50,7 +53,7 @@ def _fp64_loss(base, m, gx, gy, T):
     return 0.5 * np.sum((u - T.ravel()) ** 2), u, A, idx
 
 
-def _gpu_grads(ag, base, m, gx, gy, T):
+def _gpu_grads(ag, base, m, gx, gy, T, rtol=1e-6):
     dev = "cuda"
     img = torch.tensor(base, device=dev, requires_grad=True)
     Gx = torch.tensor(gx, device=dev, requires_grad=True)
@@ -58,7 +61,7 @@ def _gpu_grads(ag, base, m, gx, gy, T):
     mask = torch.tensor(m, device=dev)
     g = torch.where(mask, torch.full_like(img, float("nan")), img)[None]
     f = ag.divergence(Gx, Gy)[None]
-    u = ag.fill(g, f, rtol=1e-9)
+    u = ag.fill(g, f, rtol=rtol)
     loss = 0.5 * ((u[0] - torch.tensor(T, device=dev)) ** 2).sum()
     loss.backward()
     return (loss.item(), u.detach().cpu().numpy()[0], img.grad.cpu().numpy().astype(np.float64),
@@ -153,3 +156,75 @@ def test_autograd_against_dense_fp64_solve(ag):
     loss.backward()
     for got, want in ((g_img, img.grad.numpy()), (g_gx, Gx.grad.numpy()), (g_gy, Gy.grad.numpy())):
         assert np.abs(got - want).max() <= REL * np.abs(want).max()
+
+
+def _div64(gx, gy):
+    F = gx.astype(np.float64).copy()
+    F[:, 1:] -= gx[:, :-1]
+    F += gy
+    F[1:, :] -= gy[:-1, :]
+    return F
+
+
+def test_adjoint_1024_against_central_differences(ag):
+    """A whole 1024 x 1024 image of the differentiation workload (15 % holes
+    as blobs, 157k unknowns): 64 central differences of the FP64 loss, each
+    two solves with one FP64 factorisation.  The loss is quadratic in the
+    inputs, so the central difference is exact up to rounding for any step."""
+    import scipy.sparse.linalg as spla
+    from imscript_gb300 import synth
+    from oracle import fp64
+    insts, targets, guid = synth.config4(seed=5, n=1)
+    g32 = insts[0].g[0]
+    m = np.isnan(g32)
+    base = np.nan_to_num(g32, nan=0.0)
+    gx, gy = guid[0]
+    T = targets[0]
+    _, _, g_img, g_gx, g_gy = _gpu_grads(ag, base, m, gx, gy, T, rtol=1e-6)
+    A, _, idx = fp64.build_system(g32, None, 0)
+    p = fp64.nested_dissection(idx % g32.shape[1], idx // g32.shape[1], 1)
+    lu = spla.splu(A[p][:, p].tocsc(), permc_spec="NATURAL", diag_pivot_thresh=0.0,
+                   options=dict(SymmetricMode=True))
+
+    def loss(img, Gx, Gy):
+        gg = img.astype(np.float32).copy()
+        gg[m] = np.nan
+        _, b, _ = fp64.build_system(gg, None, 0)
+        b = b - _div64(Gx, Gy).ravel()[idx]
+        x = np.empty(idx.size)
+        x[p] = lu.solve(b[p])
+        u = img.astype(np.float64).ravel().copy()
+        u[idx] = x
+        return 0.5 * np.sum((u - T.ravel()) ** 2)
+
+    # coordinates where the gradient goes through the solve: known pixels with
+    # an unknown 4-neighbour, guidance samples whose divergence reaches an
+    # unknown pixel; every third one anywhere
+    h, w = m.shape
+    near = np.zeros_like(m)
+    near[:, :-1] |= m[:, 1:]
+    near[:, 1:] |= m[:, :-1]
+    near[:-1, :] |= m[1:, :]
+    near[1:, :] |= m[:-1, :]
+    rng = np.random.default_rng(11)
+    scale = max(np.abs(g_img).max(), np.abs(g_gx).max(), np.abs(g_gy).max())
+    eps = 0.25
+    worst = 0.0
+    for n in range(64):
+        k = n % 3
+        if k == 0:
+            cand = np.argwhere(near & ~m) if n % 2 == 0 else np.argwhere(~m)
+        else:
+            cand = np.argwhere(m) if n % 2 == 0 else np.argwhere(np.ones_like(m))
+        j, i = cand[rng.integers(len(cand))]
+        arrs = [base.astype(np.float64), gx.astype(np.float64), gy.astype(np.float64)]
+        plus = [a.copy() for a in arrs]
+        minus = [a.copy() for a in arrs]
+        plus[k][j, i] += eps
+        minus[k][j, i] -= eps
+        fd = (loss(*plus) - loss(*minus)) / (2 * eps)
+        got = [g_img, g_gx, g_gy][k][j, i]
+        worst = max(worst, abs(fd - got) / scale)
+    print(f"\n1024x1024 adjoint at rtol 1e-6: worst |FD - adjoint| / max|grad| over 64 coordinates "
+          f"{worst:.3e}")
+    assert worst <= REL
