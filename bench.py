@@ -1,21 +1,27 @@
 #!/usr/bin/env python
 """Benchmark of the GB300 simpois fill: filled Mpx/s at a 1e-6 FP64 relative residual.
 
-Workload (default): Poisson with guidance, one 2048 x 2048 x 3 float32 image
-(128 Gaussians per channel), guidance f = div of the forward-difference
-gradient of an independent field, 6 irregular blobs covering 15 % of the
-pixels, seeded synthetic data; every channel solved to an FP64 relative
-residual <= 1e-6 (the workload's own target is 1e-5; 1e-6 is stricter).
+Workload (default, ``--workload c3``): 256 uneven instances -- sides drawn
+log-uniform in [64, 1024] (non-square), 1 or 3 float32 channels, 5-60 % holes
+as random disks, half Laplace, half guided Poisson -- every channel solved to
+an FP64 relative residual <= 1e-6.  Seeded synthetic data stands in for
+images; three input sets (different seeds: sizes, masks and fields) are
+solved in rotation, one per step, so that no step reuses the previous step's
+plan or solve graph.
 
-A step is one converged solve of the whole image (all channels batched in one
-call).  ``value`` times it with the inputs resident in HBM; ``e2e`` times the
-same solve through the C-ABI host entry point (simpois_solve) from pinned host
-buffers, host-to-device and device-to-host copies included; ``plain`` times
-the same channels solved one per call.  L2 is flushed (a 512 MiB write)
-between timed steps.
+A step is one converged solve of a whole input set (all instances batched in
+one call).  ``value`` times it with the inputs resident in HBM; ``plain``
+times the same images solved one image per call; ``same_input`` times the
+batched solve of one input set repeated (plan and graph reused); ``e2e``
+times the batched solve through the C-ABI host entry point
+(simpois_solve_batch_host) from page-locked host buffers, every copy to and
+from the device included; ``bwd_fwd`` is the backward / forward time of the
+differentiation workload (32 x 1024^2 guided Poisson, MSE loss) through the
+torch.autograd.Function.  L2 is flushed (a 512 MiB write) between timed steps.
 
 ``--impl reference`` times the CPU restatement of the reference's CG recipe
-(``CG_EPS = rtol * ||b|| simpois -s 1 -c -1``) on the host cores instead.
+(``CG_EPS = rtol * ||b|| simpois -s 1 -c -1``, bit-exact with the reference
+binary) on the host cores, on whole images of the same input sets.
 """
 from __future__ import annotations
 
@@ -34,6 +40,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 HBM_FALLBACK = 6800.0
+METRIC = "filled Mpx/s at 1e-6 rel. residual (FP64), batched vs plain on 1 GB300"
 
 
 def measured_peaks():
@@ -101,71 +108,115 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def make_workload(name, rank):
+WORKLOADS = {
+    "c3": "batched-256-uneven (64..1024 px, 1 or 3 ch, 5-60% holes as disks, half Laplace, half guided Poisson)",
+    "c1": "poisson-guided-2048x2048x3 (6 blobs, 15% holes)",
+    "c1s": "poisson-guided-512x512x3 (6 blobs, 15% holes)",
+    "c0": "laplace-512x512x1 (disks, 20% holes)",
+    "c2": "biharmonic-4096x4096x1 (1024^2 square + 200 scratches)",
+    "c2s": "biharmonic-1024x1024x1 (256^2 square + 50 scratches)",
+}
+
+
+def make_workload(name, seed):
+    """The instances of workload `name` for one seed."""
     from imscript_gb300 import synth
-    seed = 1000 * rank
     if name == "c1":
-        inst = synth.config1(seed=seed, rtol=1e-6)
-        return [inst], "poisson-guided-2048x2048x3 (6 blobs, 15% holes)"
+        return [synth.config1(seed=seed, rtol=1e-6)]
     if name == "c1s":  # reduced size, for quick checks
-        inst = synth.config1(seed=seed, size=512, rtol=1e-6)
-        return [inst], "poisson-guided-512x512x3 (6 blobs, 15% holes)"
+        return [synth.config1(seed=seed, size=512, rtol=1e-6)]
     if name == "c0":
-        return [synth.config0(seed=seed)], "laplace-512x512x1 (disks, 20% holes)"
+        return [synth.config0(seed=seed)]
     if name == "c3":
-        return synth.config3(seed=seed), "batched-256-uneven (64..1024 px, 5-60% holes)"
+        return synth.config3(seed=seed)
     if name == "c2":
-        return [synth.config2(seed=seed)], "biharmonic-4096x4096x1 (1024^2 square + 200 scratches)"
+        return [synth.config2(seed=seed)]
     if name == "c2s":  # reduced size, for quick checks
-        return [synth.config2(seed=seed, size=1024, hole=256, n_scratch=50)], \
-            "biharmonic-1024x1024x1 (256^2 square + 50 scratches)"
+        return [synth.config2(seed=seed, size=1024, hole=256, n_scratch=50)]
     raise SystemExit(f"unknown workload {name}")
 
 
-# ------------------------------------------------------------------ CPU baseline
-
-def cpu_sample(insts, crop, max_crops, seed=0):
-    """Crops of the workload's channels with their unknowns, for the CPU."""
-    rng = np.random.default_rng(seed)
-    out = []
-    chans = [(inst, l) for inst in insts for l in range(inst.g.shape[0])]
-    tries = 0
-    while len(out) < max_crops and tries < 64 * max_crops:
-        inst, l = chans[tries % len(chans)]
-        tries += 1
-        _, h, w = inst.g.shape
-        y0 = int(rng.integers(0, max(1, h - crop + 1)))
-        x0 = int(rng.integers(0, max(1, w - crop + 1)))
-        g = inst.g[l, y0:y0 + crop, x0:x0 + crop]
-        n = int(np.isnan(g).sum())
-        if 0 < n < g.size:
-            f = None if inst.f is None else inst.f[l, y0:y0 + crop, x0:x0 + crop]
-            out.append((np.ascontiguousarray(g), None if f is None else np.ascontiguousarray(f),
-                        0 if inst.tstep > 0 else 1, inst.rtol))
-    return out
+def input_seeds(rank, rotate):
+    """Seeds of the input sets a rank solves in rotation."""
+    return [1000 * rank + k for k in range(max(1, rotate))]
 
 
-def cpu_time(sample, threads):
-    """Run the oracle's restatement of the reference CG recipe on every crop
-    (CG_EPS = rtol * ||b||, -s 1 -c -1), in parallel threads."""
+def bench_config(args, sets):
+    """The `config` of the line: the same dict on both arms."""
+    unk = [sum(i.unknowns for i in insts) for insts in sets]
+    return {"workload": WORKLOADS[args.workload], "instances_per_step": len(sets[0]),
+            "unknown_samples_per_step": int(round(sum(unk) / len(unk))), "rtol": 1e-6,
+            "inputs": f"{len(sets)} seeded input sets (sizes, masks and fields differ), one per step in rotation",
+            "l2": "flushed between timed steps (512 MiB write)", "parallelism": "single GPU"}
+
+
+# ------------------------------------------------------------------ CPU side
+
+def _cg_channel(item):
+    """The reference CG recipe (CG_EPS = rtol*||b||, -s 1 -c -1) on one whole
+    channel, in the oracle's bit-exact C restatement."""
+    from oracle import oracle
+    g, f, kind, rtol = item
+    bn = float(oracle.rhs_norm(g[None], None if f is None else f[None], kind)[0])
+    out, it, _ = oracle.cg_extension(g, f, init=np.zeros_like(g), maxit=-1, kind=kind, cg_eps=rtol * bn)
+    return int(np.isnan(g).sum()), it
+
+
+def channels_of(insts):
+    return [(np.ascontiguousarray(i.g[l]), None if i.f is None else np.ascontiguousarray(i.f[l]),
+             0 if i.tstep > 0 else 1, i.rtol) for i in insts for l in range(i.g.shape[0])]
+
+
+def cpu_time(chans, threads):
+    """Solve every channel with the reference CG recipe, one channel per host
+    thread at a time (the C code releases the GIL), largest first."""
     from concurrent.futures import ThreadPoolExecutor
     from oracle import oracle
-
     oracle.lib()
-
-    def one(item):
-        g, f, kind, rtol = item
-        bn = float(oracle.rhs_norm(g[None], None if f is None else f[None], kind)[0])
-        out, it, _ = oracle.cg_extension(g, f, init=np.zeros_like(g), maxit=-1, kind=kind,
-                                         cg_eps=rtol * bn)
-        return int(np.isnan(g).sum()), it
-
+    order = sorted(chans, key=lambda c: -int(np.isnan(c[0]).sum()))
     t0 = time.perf_counter()
     with ThreadPoolExecutor(max_workers=threads) as ex:
-        res = list(ex.map(one, sample))
+        res = list(ex.map(_cg_channel, order))
     dt = time.perf_counter() - t0
-    unk = sum(r[0] for r in res)
-    return unk, dt, res
+    return sum(r[0] for r in res), dt
+
+
+def cpu_sample(insts, part, nparts):
+    """Whole instances of the workload, every nparts-th one from `part`."""
+    return [inst for k, inst in enumerate(insts) if k % nparts == part]
+
+
+def cpu_baseline(insts, nparts):
+    threads = os.cpu_count() or 1
+    sub = cpu_sample(insts, 0, nparts)
+    unk, dt = cpu_time(channels_of(sub), threads)
+    return {"value": unk / dt / 1e6, "unit": "filled Mpx/s", "cores": threads, "kind": "port",
+            "sample": f"{len(sub)} whole instances of the first input set (every {nparts}th, {unk} unknowns), "
+                      f"each channel solved by the CPU restatement of the reference CG recipe to FP64 "
+                      f"relative residual 1e-6, channels on {threads} host threads; {dt:.1f} s"}
+
+
+def _fp64_err(item):
+    """max |u - x| / max |x| over the filled pixels, x the FP64 direct solve"""
+    from oracle import fp64
+    g, f, kind, u = item
+    x = fp64.solve(g, f, kind)
+    m = np.isnan(g)
+    if not m.any():
+        return 0.0
+    return float(np.abs(u[m].astype(np.float64) - x[m]).max() / max(np.abs(x[m]).max(), 1e-30))
+
+
+def fp64_errors(insts, outs):
+    """Error of every channel's output against the FP64 direct solve, in a
+    process pool started with spawn (after CUDA is up a fork would hang)."""
+    import multiprocessing as mp
+    items = [(np.ascontiguousarray(i.g[l]), None if i.f is None else np.ascontiguousarray(i.f[l]),
+              0 if i.tstep > 0 else 1, np.ascontiguousarray(o[l]))
+             for i, o in zip(insts, outs) for l in range(i.g.shape[0])]
+    items.sort(key=lambda it: -int(np.isnan(it[0]).sum()))
+    with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
+        return pool.map(_fp64_err, items, chunksize=1)
 
 
 def ncu_traffic(kernel, workload):
@@ -191,15 +242,7 @@ def ncu_traffic(kernel, workload):
                               "one launch, cold-cache ncu capture)"}
 
 
-def cpu_baseline(insts, budget_s=20.0):
-    threads = os.cpu_count() or 1
-    crop = 384
-    sample = cpu_sample(insts, crop, max_crops=threads)
-    unk, dt, res = cpu_time(sample, threads)
-    return {"value": unk / dt / 1e6, "unit": "filled Mpx/s", "cores": threads, "kind": "port",
-            "sample": f"{len(sample)} crops of {crop}x{crop} px cut from the workload's channels "
-                      f"({unk} unknowns), each solved by the CPU restatement of the reference CG "
-                      f"to FP64 relative residual 1e-6, one crop per thread; {dt:.1f} s"}
+PROFILE_NAMES = {"c3": "batched_256_uneven", "c1": "poisson_guided_2048x2048x3"}
 
 
 # ------------------------------------------------------------------ AMLE
@@ -293,15 +336,15 @@ def run_amle(args):
 
 # ------------------------------------------------------------------ differentiation
 
-def run_diff(args):
-    """32 x 1024^2 guided Poisson fills: forward (converged fill) and backward
-    (adjoint solve + scatter) through the torch.autograd.Function, timed with
-    CUDA events; reports forward filled Mpx/s and the bwd/fwd time ratio."""
+def diff_times(steps, warmup, n=32):
+    """n x 1024^2 guided Poisson fills (the differentiation workload): forward
+    (converged fill) and backward (adjoint solve + scatter) through the
+    torch.autograd.Function, timed with CUDA events; forward filled Mpx/s and
+    the bwd/fwd time ratio."""
     import torch
     from imscript_gb300 import autograd as ag, synth
-    n = 32 if args.size == 0 else max(1, args.size)
     insts, targets, guid = synth.config4(seed=0, n=n)
-    dev = torch.device("cuda", 0)
+    dev = torch.device("cuda", torch.cuda.current_device())
     base = torch.stack([torch.from_numpy(np.nan_to_num(i.g[0], nan=0.0)) for i in insts]).to(dev)
     mask = torch.stack([torch.from_numpy(np.isnan(i.g[0])) for i in insts]).to(dev)
     gx = torch.stack([torch.from_numpy(x) for x, _ in guid]).to(dev)
@@ -310,7 +353,7 @@ def run_diff(args):
     unknowns = int(mask.sum().item())
     stream = torch.cuda.current_stream(dev)
     fwd_ms, bwd_ms = [], []
-    for it in range(args.warmup + args.steps):
+    for it in range(warmup + steps):
         img = base.clone().requires_grad_(True)
         Gx = gx.clone().requires_grad_(True)
         Gy = gy.clone().requires_grad_(True)
@@ -325,14 +368,19 @@ def run_diff(args):
         loss.backward()
         e2.record(stream)
         torch.cuda.synchronize()
-        if it >= args.warmup:
+        if it >= warmup:
             fwd_ms.append(e0.elapsed_time(e1))
             bwd_ms.append(e1.elapsed_time(e2))
     f_ms, b_ms = sum(fwd_ms) / len(fwd_ms), sum(bwd_ms) / len(bwd_ms)
-    print(json.dumps({"workload": f"differentiation {n}x1024x1024 guided Poisson (MSE loss)",
-                      "forward_ms": f_ms, "backward_ms": b_ms, "bwd_fwd_ratio": b_ms / f_ms,
-                      "forward_filled_mpx_s": unknowns / (f_ms / 1e3) / 1e6,
-                      "unknown_samples": unknowns, "steps": args.steps, "warmup": args.warmup}))
+    return {"workload": f"differentiation {n}x1024x1024x1 guided Poisson, MSE loss, rtol 1e-6",
+            "ratio": round(b_ms / f_ms, 3), "forward_ms": round(f_ms, 3), "backward_ms": round(b_ms, 3),
+            "forward_filled_mpx_s": round(unknowns / (f_ms / 1e3) / 1e6, 1),
+            "unknown_samples": unknowns, "steps": steps}
+
+
+def run_diff(args):
+    n = 32 if args.size == 0 else max(1, args.size)
+    print(json.dumps(diff_times(args.steps, args.warmup, n)))
 
 
 # ------------------------------------------------------------------ GPU arm
@@ -352,101 +400,109 @@ def run_ours(args):
     dev = torch.device("cuda", local)
 
     from imscript_gb300 import dist as sdist
+    seeds = input_seeds(0 if args.shard else rank, args.rotate)
+    sets = [make_workload(args.workload, sd) for sd in seeds]
     if args.shard and world > 1:
         # one batch partitioned across the ranks (strong scaling), no collective
         # on the data path
-        insts, wname = make_workload(args.workload, 0)
-        insts = sdist.shard(insts, [i.unknowns for i in insts], rank, world)
-        wname += f" sharded over {world} ranks"
-    else:
-        # every rank solves its own seeded copy of the workload (weak scaling)
-        insts, wname = make_workload(args.workload, rank)
-    unknowns = sum(i.unknowns for i in insts)
-    gs = [torch.from_numpy(i.g).to(dev) for i in insts]
-    fs = [None if i.f is None else torch.from_numpy(i.f).to(dev) for i in insts]
-    outs = [torch.empty_like(g) for g in gs]
-    rtol = insts[0].rtol
+        sets = [sdist.shard(insts, [i.unknowns for i in insts], rank, world) for insts in sets]
+    unk = [sum(i.unknowns for i in insts) for insts in sets]
+    dsets = []
+    for insts in sets:
+        gs = [torch.from_numpy(i.g).to(dev) for i in insts]
+        fs = [None if i.f is None else torch.from_numpy(i.f).to(dev) for i in insts]
+        dsets.append((insts, gs, fs, [torch.empty_like(g) for g in gs]))
+    rtol = 1e-6
     flush = torch.empty(512 * 2 ** 20 // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
     ctx = simpois.context(local, stream.cuda_stream)
 
-    def step_batched():
+    def batched(k):
+        insts, gs, fs, outs = dsets[k % len(dsets)]
         if len(insts) == 1:
             _, reps = simpois.solve(gs[0], fs[0], tstep=insts[0].tstep, rtol=rtol, out=outs[0])
         else:
-            _, reps = simpois.solve_batch(list(zip(gs, fs, [i.tstep for i in insts])), rtol=rtol,
-                                          outs=outs)
+            _, reps = simpois.solve_batch(list(zip(gs, fs, [i.tstep for i in insts])), rtol=rtol, outs=outs)
         return reps
 
-    def step_plain():
+    def plain(k):
+        insts, gs, fs, outs = dsets[k % len(dsets)]
         reps = []
         for g, f, i, o in zip(gs, fs, insts, outs):
-            for l in range(g.shape[0]):
-                _, r = simpois.solve(g[l:l + 1], None if f is None else f[l:l + 1], tstep=i.tstep,
-                                     rtol=rtol, out=o[l:l + 1])
-                reps += r
+            _, r = simpois.solve(g, f, tstep=i.tstep, rtol=rtol, out=o)
+            reps += r
         return reps
 
     def barrier():
         if world > 1:
             dist.barrier()
 
-    def timed(fn, steps):
+    def timed(fn, steps, same=False):
+        """device time of `steps` steps (step k solves input set k, or set 0
+        when `same`), CUDA events on the solve's stream, L2 flushed between"""
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
                for _ in range(steps)]
-        reps = None
+        reps = []
         barrier()
         torch.cuda.synchronize()
         for k in range(steps):
             flush.fill_(float(k))
             evs[k][0].record(stream)
-            reps = fn()
+            reps.append(fn(0 if same else k))
             evs[k][1].record(stream)
         torch.cuda.synchronize()
         barrier()
         ms = sum(a.elapsed_time(b) for a, b in evs)
-        return ms, reps
+        units = sum(unk[0 if same else k % len(unk)] for k in range(steps))
+        return ms, units, reps
 
-    # untimed: the autotuner times the fused V-cycle's hand-over sizes on this
-    # workload and the timed solves reuse its choice (the same output bits
+    # untimed: the autotuner times the fused V-cycle's hand-over sizes on every
+    # input set and the timed solves reuse its choice (the same output bits
     # whichever size it picks)
-    coarse_max = None
+    tuned = None
     if not args.no_autotune:
-        _, _, coarse_max = simpois.autotune(list(zip(gs, fs, [i.tstep for i in insts])), rtol=rtol,
-                                            outs=outs)
-    for _ in range(args.warmup):
-        step_batched()
+        tuned = []
+        for insts, gs, fs, outs in dsets:
+            _, _, cm = simpois.autotune(list(zip(gs, fs, [i.tstep for i in insts])), rtol=rtol, outs=outs)
+            tuned.append(cm)
+    for k in range(args.warmup):
+        batched(k)
     ctx.reset_launches()
     with ClockSampler(local) as clocks:
-        ms, reps = timed(step_batched, args.steps)
+        ms, units, reps_all = timed(batched, args.steps)
     launches = ctx.launches()
-    bad = [r for r in reps if r["status"] not in (splib.OK,)]
+    reps = [r for rs in reps_all for r in rs]
+    bad = [r for r in reps if r["status"] != splib.OK]
     worst = max(r["rel_residual"] for r in reps)
     ms = sdist.max_over_ranks(ms, device=dev)
-    total_unknowns = sdist.sum_over_ranks(unknowns, device=dev)
-    value = total_unknowns * args.steps / (ms / 1e3) / 1e6
+    units = sdist.sum_over_ranks(units, device=dev)
+    value = units / (ms / 1e3) / 1e6
     if args.quick:
         line = {"value": value, "ms_per_step": ms / args.steps, "gpu_launches": launches,
-                "iterations": [r["iterations"] for r in reps], "max_rel": worst,
-                "coarse_max": coarse_max}
+                "iterations_max": max(r["iterations"] for r in reps), "max_rel": worst, "coarse_max": tuned}
         if args.with_plain:
-            step_plain()
-            ms_p, _ = timed(step_plain, args.steps)
-            line["plain_value"] = unknowns * args.steps / (ms_p / 1e3) / 1e6
-            line["batched_over_plain"] = value / line["plain_value"]
+            plain(0)
+            ms_p, u_p, _ = timed(plain, args.steps)
+            line["plain_value"] = u_p / (ms_p / 1e3) / 1e6
+            line["batched_over_plain"] = value / world / line["plain_value"]
         if rank == 0:
             print(json.dumps(line))
         return
 
-    # kernel roofline: one more step of the same workload on the same stream,
+    # the same input set every step: the plan and the solve graph are reused
+    ms_same, u_same, _ = timed(batched, args.steps, same=True)
+    value_same = u_same / (ms_same / 1e3) / 1e6
+
+    # kernel roofline: one more step of input set 0 on the same stream, the
     # launches issued eagerly with a CUDA-event pair around each main-loop
     # kernel; achieved = algorithmic bytes / event-timed duration
     ctx.reset_kernel_stats()
     flush.fill_(0.0)
-    if len(insts) == 1:
-        simpois.solve(gs[0], fs[0], tstep=insts[0].tstep, rtol=rtol, out=outs[0], flags=splib.FLAG_KTIMER)
+    insts0, gs0, fs0, outs0 = dsets[0]
+    if len(insts0) == 1:
+        simpois.solve(gs0[0], fs0[0], tstep=insts0[0].tstep, rtol=rtol, out=outs0[0], flags=splib.FLAG_KTIMER)
     else:
-        simpois.solve_batch(list(zip(gs, fs, [i.tstep for i in insts])), rtol=rtol, outs=outs,
+        simpois.solve_batch(list(zip(gs0, fs0, [i.tstep for i in insts0])), rtol=rtol, outs=outs0,
                             flags=splib.FLAG_KTIMER)
     torch.cuda.synchronize()
     kstats = ctx.kernel_stats()
@@ -467,57 +523,65 @@ def run_ours(args):
                     "frac": round(d["achieved_gbs"] / hbm, 4), "traffic": None,
                     "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
                     else "fallback 6.8 TB/s"}
-        if args.workload == "c1":
-            tr = ncu_traffic(dom, "poisson_guided_2048x2048x3")
+        if args.workload in PROFILE_NAMES:
+            tr = ncu_traffic(dom, PROFILE_NAMES[args.workload])
             if tr:
                 roofline.update(tr)
 
-    # plain: one channel per call
-    for _ in range(max(1, args.warmup // 2)):
-        step_plain()
-    ms_plain, reps_plain = timed(step_plain, args.steps)
-    value_plain = unknowns * args.steps / (ms_plain / 1e3) / 1e6
+    # plain: one image per call
+    for k in range(max(1, args.warmup // 2)):
+        plain(k)
+    ms_plain, u_plain, _ = timed(plain, args.steps)
+    value_plain = u_plain / (ms_plain / 1e3) / 1e6
 
-    # e2e: the C-ABI host entry point, pinned host buffers
-    e2e = None
-    if len(insts) == 1:
-        hg = torch.from_numpy(insts[0].g).pin_memory()
-        hf = None if insts[0].f is None else torch.from_numpy(insts[0].f).pin_memory()
-        ho = torch.empty_like(hg).pin_memory()
-        hin = (hg.numpy(), None if hf is None else hf.numpy(), ho.numpy())
+    # e2e: the C-ABI host entry point from page-locked host buffers, every
+    # copy to and from the device inside the timed region
+    hsets = []
+    for insts, _, _, _ in dsets:
+        hg = [torch.from_numpy(i.g).pin_memory() for i in insts]
+        hf = [None if i.f is None else torch.from_numpy(i.f).pin_memory() for i in insts]
+        ho = [torch.empty_like(g).pin_memory() for g in hg]
+        hsets.append(([(g.numpy(), None if f is None else f.numpy(), i.tstep) for g, f, i in zip(hg, hf, insts)],
+                      [o.numpy() for o in ho], (hg, hf, ho)))
 
-        def step_e2e():
-            _, r = simpois.poisson_solver_separable(hin[0], hin[1], insts[0].tstep, rtol=rtol, out=hin[2])
-            return r
+    def e2e_step(k):
+        items, houts, _ = hsets[k % len(hsets)]
+        _, r = simpois.solve_batch_host(items, rtol=rtol, outs=houts, device=local)
+        return r
 
-        step_e2e()
-        ms_e2e, _ = timed(step_e2e, args.steps)
-        # page-locked, aligned buffers whose size is a multiple of 4 take the
-        # direct path: g in; f only in the 4-pixel groups that hold an unknown;
-        # out back whole during the solve, then its groups with an unknown
-        g0 = insts[0].g
-        direct = g0.size % 4 == 0 and os.environ.get("SIMPOIS_NO_DIRECT_IO", "0") in ("", "0")
-        if direct:
-            grp = int(np.isnan(g0.reshape(-1, 4)).any(axis=1).sum())
-            bi = g0.nbytes + (0 if hf is None else 16 * grp)
-            bo = g0.nbytes + 16 * grp
-        else:
-            bi = hg.numel() * 4 + (0 if hf is None else hf.numel() * 4)
-            bo = ho.numel() * 4
-        e2e = {"value": unknowns * args.steps / (ms_e2e / 1e3) / 1e6, "unit": "filled Mpx/s",
-               "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo,
-               "io": "direct" if direct else "copies", "ms_per_step": ms_e2e / args.steps}
+    e2e_step(0)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        e2e_step(k)
+    e2e_ms = (time.perf_counter() - t0) * 1e3
+    e2e_units = sum(unk[k % len(unk)] for k in range(args.steps))
+    h2d = sum(sum(it[0].nbytes + (0 if it[1] is None else it[1].nbytes) for it in hs[0]) for hs in hsets) / len(hsets)
+    d2h = sum(sum(o.nbytes for o in hs[1]) for hs in hsets) / len(hsets)
+    e2e = {"value": e2e_units / (e2e_ms / 1e3) / 1e6, "unit": "filled Mpx/s",
+           "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms / args.steps,
+           "api": "simpois_solve_batch_host (page-locked buffers), wall clock"}
+
+    # differentiation workload: bwd/fwd
+    bwd_fwd = None
+    if not args.no_diff and world == 1:
+        bwd_fwd = diff_times(max(3, args.steps // 4), 2)
 
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
         return
-    src = peak_src
+    # after every timed region: the CPU baseline and the error against the
+    # FP64 direct solve (host processes would disturb the timing)
     cpu = None
     if not args.no_cpu_baseline and world == 1:
-        cpu = cpu_baseline(insts)
+        cpu = cpu_baseline(sets[0], args.cpu_parts)
+    errs = None
+    if not args.no_fp64_check:
+        batched(0)
+        torch.cuda.synchronize()
+        errs = fp64_errors(sets[0], [o.cpu().numpy() for o in dsets[0][3]])
     line = {
-        "metric": "filled Mpx/s at 1e-6 rel. residual (FP64), batched vs plain on 1 GB300",
+        "metric": METRIC,
         "value": round(value, 3),
         "unit": "filled Mpx/s",
         "n_gpus": world,
@@ -529,22 +593,24 @@ def run_ours(args):
         "vs_baseline": None,
         "dtype": "f32 (FP64 refinement and reductions)",
         "data": "synthetic (seeded; shapes and distributions of the benchmark workload)",
-        "config": {"workload": wname, "unknown_samples_per_step": unknowns, "rtol": rtol,
-                   "l2": "flushed between timed steps (512 MiB write)",
-                   "autotuned": {"coarse_max": coarse_max},
-                   "parallelism": ("shards" if args.shard else "replicas") if world > 1 else "single GPU"},
-        "plain": {"value": round(value_plain, 3), "unit": "filled Mpx/s",
-                  "ms_per_step": ms_plain / args.steps,
-                  "batched_over_plain": round(value / world / value_plain, 3)},
+        "config": bench_config(args, sets),
+        "plain": {"value": round(value_plain, 3), "unit": "filled Mpx/s", "ms_per_step": ms_plain / args.steps,
+                  "batched_over_plain": round(value / world / value_plain, 3), "calls": "one image per call"},
+        "same_input": {"value": round(value_same, 3), "ms_per_step": ms_same / args.steps,
+                       "note": "input set 0 every step: plan and solve graph reused"},
         "e2e": e2e,
+        "bwd_fwd": bwd_fwd,
         "gpu_launches": launches,
         "clocks": clocks.summary(),
-        "solver": {"max_rel_residual": worst, "iterations": [r["iterations"] for r in reps],
-                   "refinements": [r["refinements"] for r in reps], "not_ok": len(bad)},
+        "autotuned": {"coarse_max": tuned},
+        "solver": {"max_rel_residual": worst, "iterations_max": max(r["iterations"] for r in reps),
+                   "refinements_max": max(r["refinements"] for r in reps), "not_ok": len(bad),
+                   "max_err_vs_fp64": None if errs is None else max(errs),
+                   "median_err_vs_fp64": None if errs is None else float(np.median(errs)),
+                   "err_channels": None if errs is None else len(errs)},
         "roofline": roofline,
         "kernels": kernels,
         "cpu_baseline": cpu,
-        "peaks_source": src,
     }
     print(json.dumps(line))
     if world > 1:
@@ -552,32 +618,37 @@ def run_ours(args):
 
 
 def run_reference(args):
+    """The reference CG recipe on the host cores: every step solves whole
+    images -- every cpu_parts-th instance of one input set of the workload, the
+    parts and the sets taken in rotation -- channels on all host threads."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    insts, wname = make_workload(args.workload, 0)
+    sets = [make_workload(args.workload, sd) for sd in input_seeds(0, args.rotate)]
     threads = os.cpu_count() or 1
-    sample = cpu_sample(insts, 384, max_crops=threads)
-    for _ in range(min(args.warmup, 1)):
-        cpu_time(sample[: max(1, len(sample) // 4)], threads)
+    nparts = args.cpu_parts
+    plan = [(k % len(sets), (k // len(sets)) % nparts) for k in range(args.steps)]
+    if args.warmup:
+        cpu_time(channels_of(cpu_sample(sets[0], nparts - 1, 4 * nparts)), threads)
     tot_unk, tot_t = 0, 0.0
-    for _ in range(args.steps):
-        unk, dt, _ = cpu_time(sample, threads)
+    for si, part in plan:
+        unk, dt = cpu_time(channels_of(cpu_sample(sets[si], part, nparts)), threads)
         tot_unk += unk
         tot_t += dt
     v = tot_unk / tot_t / 1e6
     line = {
-        "metric": "filled Mpx/s at 1e-6 rel. residual (FP64), batched vs plain on 1 GB300",
+        "metric": METRIC,
         "impl": "reference",
         "value": round(v, 3), "unit": "filled Mpx/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64 CG vectors, f32 stencil (as the reference)",
-        "data": "synthetic (seeded)",
-        "config": {"workload": wname, "rtol": insts[0].rtol},
+        "data": "synthetic (seeded; shapes and distributions of the benchmark workload)",
+        "config": bench_config(args, sets),
         "cpu_baseline": {"value": round(v, 3), "unit": "filled Mpx/s", "cores": threads, "kind": "port",
-                         "sample": f"per step {len(sample)} crops of 384x384 px of the workload, the "
-                                   "reference CG recipe (CG_EPS = rtol*||b||, -s 1 -c -1) in the "
-                                   "oracle's bit-exact C restatement, one crop per host thread"},
+                         "sample": f"per step the whole images of every {nparts}th instance of one input set "
+                                   f"(sets and parts in rotation), each channel solved by the reference CG "
+                                   f"recipe (CG_EPS = rtol*||b||, -s 1 -c -1) in the oracle's bit-exact C "
+                                   f"restatement, channels on {threads} host threads"},
         "e2e": {"value": round(v, 3), "unit": "filled Mpx/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -586,14 +657,20 @@ def run_reference(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--gpus", type=int, default=1,
+                    help="GPUs of the run (one process per GPU under torchrun; each solves its own input sets)")
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="c1")
+    ap.add_argument("--workload", default="c3")
+    ap.add_argument("--rotate", type=int, default=3, help="input sets solved in rotation, one per step")
+    ap.add_argument("--cpu-parts", type=int, default=2,
+                    help="CPU legs: a step solves every n-th instance of an input set")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-check", action="store_true", help="skip the error against the FP64 direct solve")
+    ap.add_argument("--no-diff", action="store_true", help="skip the differentiation workload (bwd/fwd)")
     ap.add_argument("--no-autotune", action="store_true",
-                    help="skip the untimed autotuning solve (default hand-over size)")
+                    help="skip the untimed autotuning solves (default hand-over size)")
     ap.add_argument("--size", type=int, default=0, help="c4: number of images (default 32)")
     ap.add_argument("--shard", action="store_true",
                     help="N>1: partition one batch across the ranks instead of one copy per rank")
@@ -601,6 +678,11 @@ def main():
     ap.add_argument("--quick", action="store_true",
                     help="batched solves only, short JSON (for profiling runs)")
     args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.gpus != world and not (args.gpus == 1 and world == 1):
+        if int(os.environ.get("RANK", "0")) == 0:
+            print(f"bench: --gpus {args.gpus} but WORLD_SIZE {world}; launch N > 1 under torchrun",
+                  file=sys.stderr)
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "c4":

@@ -76,3 +76,25 @@ def test_direct_io_all_known_and_all_unknown():
         got, _ = simpois.poisson_solver_separable(hg, hf, 0.25, rtol=1e-6, out=ho,
                                                   allow=(0, simpois._lib.NOT_CONVERGED))
         assert np.array_equal(_bits(got), _bits(want))
+
+
+def test_batch_host_entry_point_gives_the_device_batch_bits():
+    """simpois_solve_batch_host (host buffers, page-locked or pageable) gives
+    the bits of simpois_solve_batch on the same images in device memory."""
+    import torch
+    from imscript_gb300 import simpois, synth
+    insts = synth.config3(seed=3, n=6, smax=256)
+    dev = [(torch.from_numpy(i.g).cuda(), None if i.f is None else torch.from_numpy(i.f).cuda(), i.tstep)
+           for i in insts]
+    douts, dreps = simpois.solve_batch(dev, rtol=1e-6)
+    for pinned in (True, False):
+        if pinned:
+            hg = [torch.from_numpy(i.g).pin_memory().numpy() for i in insts]
+            hf = [None if i.f is None else torch.from_numpy(i.f).pin_memory().numpy() for i in insts]
+        else:
+            hg = [i.g.copy() for i in insts]
+            hf = [None if i.f is None else i.f.copy() for i in insts]
+        houts, hreps = simpois.solve_batch_host(list(zip(hg, hf, [i.tstep for i in insts])), rtol=1e-6)
+        for d, h in zip(douts, houts):
+            assert np.array_equal(d.cpu().numpy().view(np.uint32), h.view(np.uint32))
+        assert [r["iterations"] for r in hreps] == [r["iterations"] for r in dreps]
