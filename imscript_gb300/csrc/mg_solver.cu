@@ -1393,27 +1393,100 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 	__shared__ __align__(16) uint8_t sc[FN];
 	__shared__ double sh[32];
 	__shared__ uint64_t bar;
+	// Before the dependency wait, what no kernel of the solve's loop writes:
+	// the tile, the level tables of levels l and l + 1 (the last level-0 tile
+	// of this kernel swaps lv[0].b with b_alt, and the kernel before a level-0
+	// launch is k_spmv5 or k_resid64, which write no table), the cell codes
+	// and the coarse mask.  The kernel before this one writes b of this level
+	// (the restriction) and the problem's state: those come after the wait.
 	const int4 t = tl[blockIdx.x];
-	grid_wait();
-	grid_release();
 	const int prob = t.x;
 	const ProbDev &pr = P[prob];
-	// the problem's state and level table in one round trip (l + 1 < MAXLEV)
-	const int active = st[prob].inner_active, nf = pr.nfine, pending = st[prob].pending;
-	const double alpha = st[prob].alpha;
+	const int nf = pr.nfine;
 	const LevelDev L = pr.lv[l], C = pr.lv[l + 1];
-	together(active, nf, pending, alpha, L.w, L.h, L.b, L.code, L.z, L.tmb, L.tmc, L.mask, C.w, C.h, C.mask, C.b, pr.q,
-			pr.x, pr.xlo, pr.p, pr.p2, pr.b_alt);
-	if (!active || l >= nf) return;
+	const bool fine = l < nf;
+	const int x0 = t.y * SP_TILE - FH, y0 = t.z * SP_TILE - FH;
+	// the coarse cell this thread restricts to (16 x 16 per tile)
+	const int ci = t.y * (SP_TILE / 2) + (threadIdx.x & 15), cj = t.z * (SP_TILE / 2) + (threadIdx.x >> 4);
+	const bool cun = fine && ci < C.w && cj < C.h && C.mask[(size_t)cj * C.w + ci];
+	constexpr int NV = (FN / 4 + SP_THREADS - 1) / SP_THREADS;   // 4-cell groups per thread
+	const bool vec = (L.w & 3) == 0;
+	uint32_t cdv[NV];   // vector path: the region codes of the thread's groups
+	if (fine && !L.tmb) {
+		if (vec) {
+#pragma unroll
+			for (int it = 0; it < NV; it++) {
+				const int f = threadIdx.x + it * SP_THREADS;
+				cdv[it] = 0;
+				if (f < FN / 4) {
+					const int ry = f / (FR / 4), rx = 4 * (f - ry * (FR / 4)), gi = x0 + rx, gj = y0 + ry;
+					const bool in = gi >= 0 && gi < L.w && gj >= 0 && gj < L.h;
+					uint32_t cd = in ? *(const uint32_t *)(L.code + (size_t)gj * L.w + gi) : 0u;
+					cd = region_codes4(cd, rx, ry);
+					cdv[it] = cd;
+					const int c = ry * FR + rx;
+					*(uint32_t *)(sc + c) = cd;
+					*(float4 *)(sz + c) = make_float4(0.f, 0.f, 0.f, 0.f);
+				}
+			}
+		} else {
+			for (int c = threadIdx.x; c < FN; c += SP_THREADS) {
+				const int ry = c / FR, rx = c - ry * FR, gi = x0 + rx, gj = y0 + ry;
+				const bool in = gi >= 0 && gi < L.w && gj >= 0 && gj < L.h;
+				sc[c] = region_code1(in ? L.code[(size_t)gj * L.w + gi] : 0, rx, ry);
+				sz[c] = 0.f;
+			}
+		}
+	}
+	grid_wait();
+	grid_release();
+	const int active = st[prob].inner_active, pending = st[prob].pending;
+	const double alpha = st[prob].alpha;
 	const bool upd = l == 0 && pending;
 	const float a = upd ? (float)alpha : 0.f;
 	const float *qv = pr.q;
-	const int x0 = t.y * SP_TILE - FH, y0 = t.z * SP_TILE - FH;
-	// the coarse cell this thread restricts to (16 x 16 per tile); its mask is
-	// loaded now, with the region, not after the sweeps
-	const int ci = t.y * (SP_TILE / 2) + (threadIdx.x & 15), cj = t.z * (SP_TILE / 2) + (threadIdx.x >> 4);
-	const bool cun = ci < C.w && cj < C.h && C.mask[(size_t)cj * C.w + ci];
-	// every load depends only on the coordinates, so all are in flight at once
+	// b (and at level 0 q) of the region: issued with the state's loads, before
+	// the early-return test, so that one round trip follows the wait
+	if (fine && !L.tmb && vec) {
+		// groups of 4 cells of a row (aligned, wholly inside or outside)
+#pragma unroll
+		for (int it = 0; it < NV; it++) {
+			const int f = threadIdx.x + it * SP_THREADS;
+			if (f < FN / 4) {
+				const int ry = f / (FR / 4), rx = 4 * (f - ry * (FR / 4)), gi = x0 + rx, gj = y0 + ry;
+				const uint32_t cd = cdv[it];
+				float4 bv = make_float4(0.f, 0.f, 0.f, 0.f);
+				if (cd) {   // a group holding an unknown lies in the image
+					const size_t k = (size_t)gj * L.w + gi;
+					bv = *(const float4 *)(L.b + k);
+					if (l == 0) {
+						const float4 qq = *(const float4 *)(qv + k);
+						if (upd) {
+							bv.x = __fmaf_rn(-a, qq.x, bv.x);
+							bv.y = __fmaf_rn(-a, qq.y, bv.y);
+							bv.z = __fmaf_rn(-a, qq.z, bv.z);
+							bv.w = __fmaf_rn(-a, qq.w, bv.w);
+						}
+					}
+				}
+				*(float4 *)(sb + ry * FR + rx) = make_float4((cd & 1u) ? bv.x : 0.f, (cd & 0x100u) ? bv.y : 0.f,
+						(cd & 0x10000u) ? bv.z : 0.f, (cd & 0x1000000u) ? bv.w : 0.f);
+			}
+		}
+	} else if (fine && !L.tmb) {
+		for (int c = threadIdx.x; c < FN; c += SP_THREADS) {
+			const int ry = c / FR, rx = c - ry * FR, gi = x0 + rx, gj = y0 + ry;
+			const uint8_t cd = sc[c];   // written by this thread before the wait
+			float bv = 0.f;
+			if (cd & 1) {
+				const size_t k = (size_t)gj * L.w + gi;
+				bv = L.b[k];
+				if (upd) bv = __fmaf_rn(-a, qv[k], bv);
+			}
+			sb[c] = bv;
+		}
+	}
+	if (!active || !fine) return;
 	if (L.tmb) {
 		// TMA: b as a 40 x 40 box at (x0, y0) straight into sb, the codes as a
 		// 64 x 40 box from x0 - 12 (a 16-byte boundary); out of the image both
@@ -1429,7 +1502,7 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 		__syncthreads();   // the barrier is initialised
 		mbar_wait0(&bar, &gl->tma_timeout);
 #pragma unroll
-		for (int it = 0; it < (FN / 4 + SP_THREADS - 1) / SP_THREADS; it++) {
+		for (int it = 0; it < NV; it++) {
 			const int f = threadIdx.x + it * SP_THREADS;
 			if (f < FN / 4) {
 				const int ry = f / (FR / 4), rx = 4 * (f - ry * (FR / 4));
@@ -1445,51 +1518,6 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 					b4[3] = __fmaf_rn(-a, qq.w, b4[3]);
 				}
 			}
-		}
-	} else if ((L.w & 3) == 0) {
-		// groups of 4 cells of a row (aligned, wholly inside or outside)
-#pragma unroll
-		for (int it = 0; it < (FN / 4 + SP_THREADS - 1) / SP_THREADS; it++) {
-			const int f = threadIdx.x + it * SP_THREADS;
-			if (f < FN / 4) {
-				const int ry = f / (FR / 4), rx = 4 * (f - ry * (FR / 4)), gi = x0 + rx, gj = y0 + ry;
-				const bool in = gi >= 0 && gi < L.w && gj >= 0 && gj < L.h;
-				const size_t k = in ? (size_t)gj * L.w + gi : 0;
-				uint32_t cd = 0;
-				float4 bv = make_float4(0.f, 0.f, 0.f, 0.f);
-				if (in) {
-					cd = *(const uint32_t *)(L.code + k);
-					bv = *(const float4 *)(L.b + k);
-					if (upd) {
-						const float4 qq = *(const float4 *)(qv + k);
-						bv.x = __fmaf_rn(-a, qq.x, bv.x);
-						bv.y = __fmaf_rn(-a, qq.y, bv.y);
-						bv.z = __fmaf_rn(-a, qq.z, bv.z);
-						bv.w = __fmaf_rn(-a, qq.w, bv.w);
-					}
-				}
-				cd = region_codes4(cd, rx, ry);
-				const int c = ry * FR + rx;
-				*(uint32_t *)(sc + c) = cd;
-				*(float4 *)(sb + c) = make_float4((cd & 1u) ? bv.x : 0.f, (cd & 0x100u) ? bv.y : 0.f,
-						(cd & 0x10000u) ? bv.z : 0.f, (cd & 0x1000000u) ? bv.w : 0.f);
-				*(float4 *)(sz + c) = make_float4(0.f, 0.f, 0.f, 0.f);
-			}
-		}
-	} else
-#pragma unroll
-	for (int it = 0; it < (FN + SP_THREADS - 1) / SP_THREADS; it++) {
-		const int c = threadIdx.x + it * SP_THREADS;
-		if (c < FN) {
-			const int ry = c / FR, rx = c - ry * FR, gi = x0 + rx, gj = y0 + ry;
-			const bool in = gi >= 0 && gi < L.w && gj >= 0 && gj < L.h;
-			const size_t k = in ? (size_t)gj * L.w + gi : 0;
-			const uint8_t cd = region_code1(in ? L.code[k] : 0, rx, ry);
-			float bv = in ? L.b[k] : 0.f;
-			if (upd && in) bv = __fmaf_rn(-a, qv[k], bv);
-			sc[c] = cd;
-			sb[c] = (cd & 1) ? bv : 0.f;
-			sz[c] = 0.f;
 		}
 	}
 	// the PCG step on the tile: the pixel -> thread map and the order of the
@@ -1592,21 +1620,27 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_post5(const ProbDev *__restri
 	__shared__ __align__(16) float sb[FN], sz[FN];
 	__shared__ __align__(16) uint8_t sc[FN];
 	__shared__ double sh[32];
+	// Before the dependency wait: the kernel before this one (k_post5 of level
+	// l + 1 or k_coarse5) writes only z2 of level l + 1, so the tile, the level
+	// tables, the problem's inner_active (k_coarse5 changes it only for
+	// problems without tile levels, which return here), the cell codes, b and z
+	// of this level and the coarse mask are loaded first; the coarse
+	// correction after the wait.
 	const int4 t = tl[blockIdx.x];
-	grid_wait();
-	grid_release();
 	const int prob = t.x;
 	const ProbDev &pr = P[prob];
 	const int active = st[prob].inner_active, nf = pr.nfine;
 	const LevelDev L = pr.lv[l], C = pr.lv[l + 1];
-	together(active, nf, L.w, L.h, L.code, L.b, L.z, L.z2, C.w, C.mask, C.z2);
-	if (!active || l >= nf) return;
+	const bool fine = active && l < nf;
 	const int x0 = t.y * SP_TILE - FH, y0 = t.z * SP_TILE - FH;
-	if ((L.w & 3) == 0) {
+	constexpr int NV = (FN / 4 + SP_THREADS - 1) / SP_THREADS;
+	const bool vec = (L.w & 3) == 0;
+	uint32_t addm = 0;   // vector path: per group (4 bits each) the cells that take the correction
+	if (fine && vec) {
 		// groups of 4 cells of a row: with w % 4 == 0 (and x0 % 4 == 0) a group
 		// is wholly inside or outside the image and every access is aligned
 #pragma unroll
-		for (int it = 0; it < (FN / 4 + SP_THREADS - 1) / SP_THREADS; it++) {
+		for (int it = 0; it < NV; it++) {
 			const int f = threadIdx.x + it * SP_THREADS;
 			if (f < FN / 4) {
 				const int ry = f / (FR / 4), rx = 4 * (f - ry * (FR / 4)), gi = x0 + rx, gj = y0 + ry;
@@ -1615,13 +1649,11 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_post5(const ProbDev *__restri
 				const size_t kc = in ? (size_t)(gj >> 1) * C.w + (gi >> 1) : 0;
 				uint32_t cd = 0;
 				float4 bv = make_float4(0.f, 0.f, 0.f, 0.f), zv = bv;
-				float2 cz = make_float2(0.f, 0.f);
 				uint8_t cm0 = 0, cm1 = 0;
 				if (in) {
 					cd = *(const uint32_t *)(L.code + k);
 					bv = *(const float4 *)(L.b + k);
 					zv = *(const float4 *)(L.z + k);
-					cz = *(const float2 *)(C.z2 + kc);
 					cm0 = C.mask[kc];
 					cm1 = C.mask[kc + 1];
 				}
@@ -1631,29 +1663,51 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_post5(const ProbDev *__restri
 				const bool m0 = cd & 1u, m1 = cd & 0x100u, m2 = cd & 0x10000u, m3 = cd & 0x1000000u;
 				*(float4 *)(sb + c) = make_float4(m0 ? bv.x : 0.f, m1 ? bv.y : 0.f, m2 ? bv.z : 0.f,
 						m3 ? bv.w : 0.f);
-				*(float4 *)(sz + c) = make_float4(m0 ? (cm0 ? zv.x + cz.x : zv.x) : 0.f,
-						m1 ? (cm0 ? zv.y + cz.x : zv.y) : 0.f, m2 ? (cm1 ? zv.z + cz.y : zv.z) : 0.f,
-						m3 ? (cm1 ? zv.w + cz.y : zv.w) : 0.f);
+				*(float4 *)(sz + c) = make_float4(m0 ? zv.x : 0.f, m1 ? zv.y : 0.f, m2 ? zv.z : 0.f,
+						m3 ? zv.w : 0.f);
+				const uint32_t am = (m0 && cm0 ? 1u : 0u) | (m1 && cm0 ? 2u : 0u) | (m2 && cm1 ? 4u : 0u) |
+						(m3 && cm1 ? 8u : 0u);
+				addm |= am << (4 * it);
 			}
 		}
-	} else
-#pragma unroll
-	for (int it = 0; it < (FN + SP_THREADS - 1) / SP_THREADS; it++) {
-		const int c = threadIdx.x + it * SP_THREADS;
-		if (c < FN) {
+	} else if (fine) {
+		for (int c = threadIdx.x; c < FN; c += SP_THREADS) {
 			const int ry = c / FR, rx = c - ry * FR, gi = x0 + rx, gj = y0 + ry;
 			const bool in = gi >= 0 && gi < L.w && gj >= 0 && gj < L.h;
 			const size_t k = in ? (size_t)gj * L.w + gi : 0;
-			const size_t kc = in ? (size_t)(gj >> 1) * C.w + (gi >> 1) : 0;
 			const uint8_t cd = region_code1(in ? L.code[k] : 0, rx, ry);
-			const float bv = in ? L.b[k] : 0.f;
-			const float zv = in ? L.z[k] : 0.f;
-			const uint8_t cm = in ? C.mask[kc] : 0;
-			const float cz = in ? C.z2[kc] : 0.f;
 			const bool m = cd & 1;
 			sc[c] = cd;
-			sb[c] = m ? bv : 0.f;
-			sz[c] = m ? (cm ? zv + cz : zv) : 0.f;
+			sb[c] = m ? L.b[k] : 0.f;
+			sz[c] = m ? L.z[k] : 0.f;
+		}
+	}
+	grid_wait();
+	grid_release();
+	if (!fine) return;
+	// the coarse correction: z + z2 of the coarse cell at the unknown cells
+	// whose coarse cell is unknown (the same sum as before, z + cz)
+	if (vec) {
+#pragma unroll
+		for (int it = 0; it < NV; it++) {
+			const uint32_t am = (addm >> (4 * it)) & 15u;
+			const int f = threadIdx.x + it * SP_THREADS;
+			if (am) {
+				const int ry = f / (FR / 4), rx = 4 * (f - ry * (FR / 4)), gi = x0 + rx, gj = y0 + ry;
+				const float2 cz = *(const float2 *)(C.z2 + (size_t)(gj >> 1) * C.w + (gi >> 1));
+				float *z4 = sz + ry * FR + rx;
+				if (am & 1u) z4[0] = z4[0] + cz.x;
+				if (am & 2u) z4[1] = z4[1] + cz.x;
+				if (am & 4u) z4[2] = z4[2] + cz.y;
+				if (am & 8u) z4[3] = z4[3] + cz.y;
+			}
+		}
+	} else {
+		for (int c = threadIdx.x; c < FN; c += SP_THREADS) {
+			if (!(sc[c] & 1)) continue;   // written by this thread before the wait
+			const int ry = c / FR, rx = c - ry * FR, gi = x0 + rx, gj = y0 + ry;
+			const size_t kc = (size_t)(gj >> 1) * C.w + (gi >> 1);
+			if (C.mask[kc]) sz[c] = sz[c] + C.z2[kc];
 		}
 	}
 	int cells[2][4];
@@ -2007,38 +2061,65 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_spmv5(const ProbDev *__restri
 	__shared__ __align__(16) float sp[RW * RH];
 	__shared__ __align__(16) uint8_t sc[RW * RH];
 	__shared__ double sh[32];
+	// Before the dependency wait: the tile, the level table, the cell codes and
+	// p_old (the previous SpMV's p_new); the kernel before this one (k_post5
+	// at level 0) writes z2 and the PCG scalars, loaded after it.
 	const int4 t = tl[blockIdx.x];
-	grid_wait();
-	grid_release();
 	const int prob = t.x;
 	const ProbDev &pr = P[prob];
-	const int active = st[prob].inner_active;
-	const double beta64 = st[prob].beta;
 	const LevelDev L = pr.lv[0];
-	together(active, beta64, L.w, L.h, L.code, L.z2, pr.p, pr.p2, pr.q);
-	if (!active) return;
-	const float beta = (float)beta64;
 	const float *pold = new_is_p2 ? pr.p : pr.p2;
 	float *pnew = new_is_p2 ? pr.p2 : pr.p;
 	FF pq = {0.f, 0.f};
 	if ((L.w & 3) == 0) {
 		const int x0 = t.y * SP_TILE - 4, y0 = t.z * SP_TILE - 1;
+		constexpr int NV = (RW * RH / 4 + SP_THREADS - 1) / SP_THREADS;
+		// p_old of the region in sp, the codes in sc (p_old is read whatever
+		// beta is: it is only used when beta != 0)
 #pragma unroll
-		for (int it = 0; it < (RW * RH / 4 + SP_THREADS - 1) / SP_THREADS; it++) {
+		for (int it = 0; it < NV; it++) {
 			const int f = threadIdx.x + it * SP_THREADS;
 			if (f < RW * RH / 4) {
 				const int ry = f / (RW / 4), rx = 4 * (f - ry * (RW / 4)), gi = x0 + rx, gj = y0 + ry;
 				const bool in = gi >= 0 && gi < L.w && gj >= 0 && gj < L.h;
 				const size_t k = in ? (size_t)gj * L.w + gi : 0;
 				uint32_t cd = 0;
-				float4 zv = make_float4(0.f, 0.f, 0.f, 0.f), po = zv;
+				float4 po = make_float4(0.f, 0.f, 0.f, 0.f);
 				if (in) {
 					cd = *(const uint32_t *)(L.code + k);
-					zv = *(const float4 *)(L.z2 + k);
-					if (beta != 0.f) po = *(const float4 *)(pold + k);
+					if (cd) po = *(const float4 *)(pold + k);
 				}
 				const int c = ry * RW + rx;
 				*(uint32_t *)(sc + c) = cd;
+				*(float4 *)(sp + c) = po;
+			}
+		}
+		grid_wait();
+		grid_release();
+		const int active = st[prob].inner_active;
+		const double beta64 = st[prob].beta;
+		// z2 of the region, issued with the state's loads
+		float4 zr[NV];
+#pragma unroll
+		for (int it = 0; it < NV; it++) {
+			const int f = threadIdx.x + it * SP_THREADS;
+			zr[it] = make_float4(0.f, 0.f, 0.f, 0.f);
+			if (f < RW * RH / 4) {
+				const int ry = f / (RW / 4), rx = 4 * (f - ry * (RW / 4)), gi = x0 + rx, gj = y0 + ry;
+				const uint32_t cd = *(const uint32_t *)(sc + ry * RW + rx);
+				if (cd) zr[it] = *(const float4 *)(L.z2 + (size_t)gj * L.w + gi);   // in the image
+			}
+		}
+		if (!active) return;
+		const float beta = (float)beta64;
+#pragma unroll
+		for (int it = 0; it < NV; it++) {
+			const int f = threadIdx.x + it * SP_THREADS;
+			if (f < RW * RH / 4) {
+				const int ry = f / (RW / 4), rx = 4 * (f - ry * (RW / 4));
+				const int c = ry * RW + rx;
+				const uint32_t cd = *(const uint32_t *)(sc + c);
+				const float4 zv = zr[it], po = *(const float4 *)(sp + c);
 				*(float4 *)(sp + c) = make_float4((cd & 1u) ? (beta != 0.f ? zv.x + beta * po.x : zv.x) : 0.f,
 						(cd & 0x100u) ? (beta != 0.f ? zv.y + beta * po.y : zv.y) : 0.f,
 						(cd & 0x10000u) ? (beta != 0.f ? zv.z + beta * po.z : zv.z) : 0.f,
@@ -2069,6 +2150,12 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_spmv5(const ProbDev *__restri
 			*(float4 *)(pr.q + k) = make_float4(qk[0], qk[1], qk[2], qk[3]);
 		}
 	} else {
+		grid_wait();
+		grid_release();
+		const int active = st[prob].inner_active;
+		const double beta64 = st[prob].beta;
+		if (!active) return;
+		const float beta = (float)beta64;
 		uint8_t *sm = sc;
 		const int x0 = t.y * SP_TILE - 1, y0 = t.z * SP_TILE - 1;
 #pragma unroll

@@ -119,20 +119,31 @@ def test_batch_of_256_uneven_instances_against_fp64(pool):
 
 def test_biharmonic_4096x4096_against_fp64(pool):
     """The 13-point system of 1.23M unknowns (a 1024^2 square and 200
-    scratches): the FP64 factorisation takes about a minute and 14 GB."""
+    scratches): the FP64 factorisation takes about a minute and 14 GB.
+
+    The workload's own target, a relative residual of 1e-6, leaves an error
+    of about 6e-4 against the FP64 solve: the operator's condition number is
+    about 1e11 (its smallest eigenvalue ~ (pi/1024)^4), so a residual does not
+    bound the error as it does for the 5-point systems.  That error is
+    measured and bounded here; the 1e-4 agreement of two converged solvers is
+    asserted on the solve to rtol 1e-8."""
     from imscript_gb300 import simpois, synth
     inst = synth.config2(seed=0)
     job = pool.apply_async(_fp64_job, ((inst.g[0], None, 1),))
-    out, reps = simpois.solve(_dev(inst.g), None, tstep=inst.tstep, rtol=1e-6)
-    out = out.cpu().numpy()
-    _check_known(out, inst.g)
-    assert reps[0]["status"] == 0 and reps[0]["rel_residual"] <= 1e-6, reps
-    x = job.get()
     m = np.isnan(inst.g[0])
-    e = _err(out[0], x, m)
-    print(f"\n4096x4096 biharmonic, rtol 1e-6 ({reps[0]['iterations']} PCG iterations): max rel. error "
-          f"vs FP64 {e:.3e}")
-    assert e <= REL
+    errs = {}
+    for rtol in (1e-6, 1e-8):
+        out, reps = simpois.solve(_dev(inst.g), None, tstep=inst.tstep, rtol=rtol)
+        out = out.cpu().numpy()
+        _check_known(out, inst.g)
+        assert reps[0]["status"] == 0 and reps[0]["rel_residual"] <= rtol, reps
+        errs[rtol] = (out[0], reps[0]["iterations"])
+    x = job.get()
+    e6, e8 = (_err(errs[r][0], x, m) for r in (1e-6, 1e-8))
+    print(f"\n4096x4096 biharmonic: max rel. error vs FP64 {e6:.3e} at rtol 1e-6 ({errs[1e-6][1]} PCG "
+          f"iterations), {e8:.3e} at rtol 1e-8 ({errs[1e-8][1]} iterations)")
+    assert e6 <= 2e-3
+    assert e8 <= REL
 
 
 def test_laplace_512x512_against_fp64(pool):
