@@ -285,6 +285,53 @@ __device__ __forceinline__ void st4(float *p, const Grp &g, const float v[4])
 	}
 }
 
+// A 4-cell row group of a shared-memory region (first column gi a multiple of
+// 4): the number of its cells inside the w x h level (0..4) and the loads of
+// its cells -- one 16-byte (4-byte) access when the level's rows keep that
+// alignment (vec: w a multiple of 4, where a group is wholly in or out), else
+// one access per cell in the image.  Cells outside read 0.
+__device__ __forceinline__ int group_cells(int gi, int gj, int w, int h)
+{
+	return (gi >= 0 && gi < w && gj >= 0 && gj < h) ? min(4, w - gi) : 0;
+}
+
+__device__ __forceinline__ float4 gload4(const float *p, size_t k, int n, bool vec)
+{
+	float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+	if (vec) {
+		if (n) v = *(const float4 *)(p + k);
+	} else {
+		if (n > 0) v.x = p[k];
+		if (n > 1) v.y = p[k + 1];
+		if (n > 2) v.z = p[k + 2];
+		if (n > 3) v.w = p[k + 3];
+	}
+	return v;
+}
+
+__device__ __forceinline__ uint32_t gload4u8(const uint8_t *p, size_t k, int n, bool vec)
+{
+	if (vec) return n ? *(const uint32_t *)(p + k) : 0u;
+	uint32_t v = 0;
+	if (n > 0) v |= p[k];
+	if (n > 1) v |= (uint32_t)p[k + 1] << 8;
+	if (n > 2) v |= (uint32_t)p[k + 2] << 16;
+	if (n > 3) v |= (uint32_t)p[k + 3] << 24;
+	return v;
+}
+
+__device__ __forceinline__ void gstore4(float *p, size_t k, int n, bool vec, float4 v)
+{
+	if (vec) {
+		if (n) *(float4 *)(p + k) = v;
+	} else {
+		if (n > 0) p[k] = v.x;
+		if (n > 1) p[k + 1] = v.y;
+		if (n > 2) p[k + 2] = v.z;
+		if (n > 3) p[k + 3] = v.w;
+	}
+}
+
 // Per-problem deterministic reduction of up to two values over the level-0
 // tiles of the problem.  Returns true in the last tile's block (all threads);
 // the sums are then in tot[0..1] (thread 0).
@@ -813,7 +860,7 @@ __global__ void k_spmv(const ProbDev *__restrict__ P, ProbState *st, const int4 
 	const ProbDev &pr = P[prob];
 	const LevelDev &L = pr.lv[0];
 	FF pq = {0.f, 0.f};
-	if (K == 0 && (pr.w & 3) == 0) {
+	if (K == 0) {
 		// k_spmv5's order: the 4 cells of a row group per thread, in row order
 		const Grp g = grp_of(t, pr.w, pr.h);
 		for (int e = 0; e < g.n; e++) {
@@ -1251,23 +1298,13 @@ __device__ __forceinline__ bool mbar_wait0(uint64_t *bar, int *timeout_flag)
 
 // Region code of a shared region cell: the level's cell code (cell_code) with
 // the neighbour bits that point out of the region cleared (those cells are
-// not in shared memory).  For a group of 4 cells of a row (x the lowest byte)
-// and for one cell.
+// not in shared memory), for a group of 4 cells of a row (x the lowest byte).
 __device__ __forceinline__ uint32_t region_codes4(uint32_t cd, int rx, int ry)
 {
 	if (rx == 0) cd &= ~0x00000004u;        // W of the first column
 	if (rx == FR - 4) cd &= ~0x02000000u;   // E of the last column
 	if (ry == 0) cd &= ~0x10101010u;        // N of the first row
 	if (ry == FR - 1) cd &= ~0x08080808u;   // S of the last row
-	return cd;
-}
-
-__device__ __forceinline__ uint8_t region_code1(uint8_t cd, int rx, int ry)
-{
-	if (rx == 0) cd &= ~4;
-	if (rx == FR - 1) cd &= ~2;
-	if (ry == 0) cd &= ~16;
-	if (ry == FR - 1) cd &= ~8;
 	return cd;
 }
 
@@ -1314,19 +1351,6 @@ constexpr CellTable make_cell_table()
 }
 
 __device__ const CellTable g_cells = make_cell_table();
-
-// Make the values a kernel's early-return test and its first region loads
-// need be loaded together, before the test, rather than each after the one
-// before it (one global round trip instead of several): an empty volatile asm
-// that takes them all as inputs stands before the test.
-__device__ __forceinline__ void touch(int v) { asm volatile("" ::"r"(v)); }
-__device__ __forceinline__ void touch(double v) { asm volatile("" ::"d"(v)); }
-__device__ __forceinline__ void touch(const void *v) { asm volatile("" ::"l"(v)); }
-template <typename... T>
-__device__ __forceinline__ void together(const T &...v)
-{
-	(touch(v), ...);
-}
 
 // Programmatic dependent launch.  A kernel launched with programmatic stream
 // serialisation may be scheduled while the kernel before it drains; it calls
@@ -1411,30 +1435,21 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 	const bool cun = fine && ci < C.w && cj < C.h && C.mask[(size_t)cj * C.w + ci];
 	constexpr int NV = (FN / 4 + SP_THREADS - 1) / SP_THREADS;   // 4-cell groups per thread
 	const bool vec = (L.w & 3) == 0;
-	uint32_t cdv[NV];   // vector path: the region codes of the thread's groups
+	uint32_t cdv[NV];   // the region codes of the thread's groups
 	if (fine && !L.tmb) {
-		if (vec) {
 #pragma unroll
-			for (int it = 0; it < NV; it++) {
-				const int f = threadIdx.x + it * SP_THREADS;
-				cdv[it] = 0;
-				if (f < FN / 4) {
-					const int ry = f / (FR / 4), rx = 4 * (f - ry * (FR / 4)), gi = x0 + rx, gj = y0 + ry;
-					const bool in = gi >= 0 && gi < L.w && gj >= 0 && gj < L.h;
-					uint32_t cd = in ? *(const uint32_t *)(L.code + (size_t)gj * L.w + gi) : 0u;
-					cd = region_codes4(cd, rx, ry);
-					cdv[it] = cd;
-					const int c = ry * FR + rx;
-					*(uint32_t *)(sc + c) = cd;
-					*(float4 *)(sz + c) = make_float4(0.f, 0.f, 0.f, 0.f);
-				}
-			}
-		} else {
-			for (int c = threadIdx.x; c < FN; c += SP_THREADS) {
-				const int ry = c / FR, rx = c - ry * FR, gi = x0 + rx, gj = y0 + ry;
-				const bool in = gi >= 0 && gi < L.w && gj >= 0 && gj < L.h;
-				sc[c] = region_code1(in ? L.code[(size_t)gj * L.w + gi] : 0, rx, ry);
-				sz[c] = 0.f;
+		for (int it = 0; it < NV; it++) {
+			const int f = threadIdx.x + it * SP_THREADS;
+			cdv[it] = 0;
+			if (f < FN / 4) {
+				const int ry = f / (FR / 4), rx = 4 * (f - ry * (FR / 4)), gi = x0 + rx, gj = y0 + ry;
+				const int n = group_cells(gi, gj, L.w, L.h);
+				const size_t k = n ? (size_t)gj * L.w + gi : 0;
+				const uint32_t cd = region_codes4(gload4u8(L.code, k, n, vec), rx, ry);
+				cdv[it] = cd;
+				const int c = ry * FR + rx;
+				*(uint32_t *)(sc + c) = cd;
+				*(float4 *)(sz + c) = make_float4(0.f, 0.f, 0.f, 0.f);
 			}
 		}
 	}
@@ -1447,8 +1462,7 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 	const float *qv = pr.q;
 	// b (and at level 0 q) of the region: issued with the state's loads, before
 	// the early-return test, so that one round trip follows the wait
-	if (fine && !L.tmb && vec) {
-		// groups of 4 cells of a row (aligned, wholly inside or outside)
+	if (fine && !L.tmb) {
 #pragma unroll
 		for (int it = 0; it < NV; it++) {
 			const int f = threadIdx.x + it * SP_THREADS;
@@ -1456,11 +1470,12 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 				const int ry = f / (FR / 4), rx = 4 * (f - ry * (FR / 4)), gi = x0 + rx, gj = y0 + ry;
 				const uint32_t cd = cdv[it];
 				float4 bv = make_float4(0.f, 0.f, 0.f, 0.f);
-				if (cd) {   // a group holding an unknown lies in the image
+				if (cd) {   // a group holding an unknown lies (partly) in the image
+					const int n = min(4, L.w - gi);
 					const size_t k = (size_t)gj * L.w + gi;
-					bv = *(const float4 *)(L.b + k);
+					bv = gload4(L.b, k, n, vec);
 					if (l == 0) {
-						const float4 qq = *(const float4 *)(qv + k);
+						const float4 qq = gload4(qv, k, n, vec);
 						if (upd) {
 							bv.x = __fmaf_rn(-a, qq.x, bv.x);
 							bv.y = __fmaf_rn(-a, qq.y, bv.y);
@@ -1472,18 +1487,6 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 				*(float4 *)(sb + ry * FR + rx) = make_float4((cd & 1u) ? bv.x : 0.f, (cd & 0x100u) ? bv.y : 0.f,
 						(cd & 0x10000u) ? bv.z : 0.f, (cd & 0x1000000u) ? bv.w : 0.f);
 			}
-		}
-	} else if (fine && !L.tmb) {
-		for (int c = threadIdx.x; c < FN; c += SP_THREADS) {
-			const int ry = c / FR, rx = c - ry * FR, gi = x0 + rx, gj = y0 + ry;
-			const uint8_t cd = sc[c];   // written by this thread before the wait
-			float bv = 0.f;
-			if (cd & 1) {
-				const size_t k = (size_t)gj * L.w + gi;
-				bv = L.b[k];
-				if (upd) bv = __fmaf_rn(-a, qv[k], bv);
-			}
-			sb[c] = bv;
 		}
 	}
 	if (!active || !fine) return;
@@ -1635,29 +1638,27 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_post5(const ProbDev *__restri
 	const int x0 = t.y * SP_TILE - FH, y0 = t.z * SP_TILE - FH;
 	constexpr int NV = (FN / 4 + SP_THREADS - 1) / SP_THREADS;
 	const bool vec = (L.w & 3) == 0;
-	uint32_t addm = 0;   // vector path: per group (4 bits each) the cells that take the correction
-	if (fine && vec) {
-		// groups of 4 cells of a row: with w % 4 == 0 (and x0 % 4 == 0) a group
-		// is wholly inside or outside the image and every access is aligned
+	uint32_t addm = 0;   // per group (4 bits each) the cells that take the correction
+	if (fine) {
+		// groups of 4 cells of a row (with w % 4 == 0 wholly inside or outside
+		// the image, every access aligned)
 #pragma unroll
 		for (int it = 0; it < NV; it++) {
 			const int f = threadIdx.x + it * SP_THREADS;
 			if (f < FN / 4) {
 				const int ry = f / (FR / 4), rx = 4 * (f - ry * (FR / 4)), gi = x0 + rx, gj = y0 + ry;
-				const bool in = gi >= 0 && gi < L.w && gj >= 0 && gj < L.h;
-				const size_t k = in ? (size_t)gj * L.w + gi : 0;
-				const size_t kc = in ? (size_t)(gj >> 1) * C.w + (gi >> 1) : 0;
-				uint32_t cd = 0;
+				const int n = group_cells(gi, gj, L.w, L.h);
+				const size_t k = n ? (size_t)gj * L.w + gi : 0;
+				const size_t kc = n ? (size_t)(gj >> 1) * C.w + (gi >> 1) : 0;
+				const uint32_t cd = region_codes4(gload4u8(L.code, k, n, vec), rx, ry);
 				float4 bv = make_float4(0.f, 0.f, 0.f, 0.f), zv = bv;
 				uint8_t cm0 = 0, cm1 = 0;
-				if (in) {
-					cd = *(const uint32_t *)(L.code + k);
-					bv = *(const float4 *)(L.b + k);
-					zv = *(const float4 *)(L.z + k);
+				if (cd) {
+					bv = gload4(L.b, k, n, vec);
+					zv = gload4(L.z, k, n, vec);
 					cm0 = C.mask[kc];
-					cm1 = C.mask[kc + 1];
+					if (n > 2) cm1 = C.mask[kc + 1];
 				}
-				cd = region_codes4(cd, rx, ry);
 				const int c = ry * FR + rx;
 				*(uint32_t *)(sc + c) = cd;
 				const bool m0 = cd & 1u, m1 = cd & 0x100u, m2 = cd & 0x10000u, m3 = cd & 0x1000000u;
@@ -1670,44 +1671,31 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_post5(const ProbDev *__restri
 				addm |= am << (4 * it);
 			}
 		}
-	} else if (fine) {
-		for (int c = threadIdx.x; c < FN; c += SP_THREADS) {
-			const int ry = c / FR, rx = c - ry * FR, gi = x0 + rx, gj = y0 + ry;
-			const bool in = gi >= 0 && gi < L.w && gj >= 0 && gj < L.h;
-			const size_t k = in ? (size_t)gj * L.w + gi : 0;
-			const uint8_t cd = region_code1(in ? L.code[k] : 0, rx, ry);
-			const bool m = cd & 1;
-			sc[c] = cd;
-			sb[c] = m ? L.b[k] : 0.f;
-			sz[c] = m ? L.z[k] : 0.f;
-		}
 	}
 	grid_wait();
 	grid_release();
 	if (!fine) return;
 	// the coarse correction: z + z2 of the coarse cell at the unknown cells
 	// whose coarse cell is unknown (the same sum as before, z + cz)
-	if (vec) {
 #pragma unroll
-		for (int it = 0; it < NV; it++) {
-			const uint32_t am = (addm >> (4 * it)) & 15u;
-			const int f = threadIdx.x + it * SP_THREADS;
-			if (am) {
-				const int ry = f / (FR / 4), rx = 4 * (f - ry * (FR / 4)), gi = x0 + rx, gj = y0 + ry;
-				const float2 cz = *(const float2 *)(C.z2 + (size_t)(gj >> 1) * C.w + (gi >> 1));
-				float *z4 = sz + ry * FR + rx;
-				if (am & 1u) z4[0] = z4[0] + cz.x;
-				if (am & 2u) z4[1] = z4[1] + cz.x;
-				if (am & 4u) z4[2] = z4[2] + cz.y;
-				if (am & 8u) z4[3] = z4[3] + cz.y;
+	for (int it = 0; it < NV; it++) {
+		const uint32_t am = (addm >> (4 * it)) & 15u;
+		const int f = threadIdx.x + it * SP_THREADS;
+		if (am) {
+			const int ry = f / (FR / 4), rx = 4 * (f - ry * (FR / 4)), gi = x0 + rx, gj = y0 + ry;
+			const float *zc = C.z2 + (size_t)(gj >> 1) * C.w + (gi >> 1);
+			float2 cz;
+			if (vec) {   // C.w is even and gi / 2 too: an aligned pair
+				cz = *(const float2 *)zc;
+			} else {
+				cz.x = (am & 3u) ? zc[0] : 0.f;
+				cz.y = (am & 12u) ? zc[1] : 0.f;
 			}
-		}
-	} else {
-		for (int c = threadIdx.x; c < FN; c += SP_THREADS) {
-			if (!(sc[c] & 1)) continue;   // written by this thread before the wait
-			const int ry = c / FR, rx = c - ry * FR, gi = x0 + rx, gj = y0 + ry;
-			const size_t kc = (size_t)(gj >> 1) * C.w + (gi >> 1);
-			if (C.mask[kc]) sz[c] = sz[c] + C.z2[kc];
+			float *z4 = sz + ry * FR + rx;
+			if (am & 1u) z4[0] = z4[0] + cz.x;
+			if (am & 2u) z4[1] = z4[1] + cz.x;
+			if (am & 4u) z4[2] = z4[2] + cz.y;
+			if (am & 8u) z4[3] = z4[3] + cz.y;
 		}
 	}
 	int cells[2][4];
@@ -2049,15 +2037,15 @@ __global__ void __launch_bounds__(1024, 1) k_coarse5(const ProbDev *__restrict__
 // p_new = z + beta p_old on the tile and a 1-pixel halo (as k_pupdate), then
 // q = A p_new and alpha = rho / (p_new . q) (as k_spmv<0>).  p_old and p_new
 // are different buffers (the halo of a neighbour must still see p_old).
-// When the level width is a multiple of 4 the region is 40 x 34 (4-aligned
-// columns) and moves in groups of 4 cells, each thread then applying A to 4
-// cells of a row; the products p.q are summed in k_spmv<0>'s order.
+// The region is 40 x 34 (4-aligned columns) and moves in groups of 4 cells
+// (16-byte accesses when the level width is a multiple of 4), each thread then
+// applying A to 4 cells of a row; the products p.q are summed in k_spmv<0>'s
+// order.
 __global__ void __launch_bounds__(SP_THREADS, 8) k_spmv5(const ProbDev *__restrict__ P, ProbState *st,
 		const int4 *__restrict__ tl, const int *__restrict__ tbeg, const int *__restrict__ tcnt, double *partial,
 		Globals *gl, int new_is_p2)
 {
-	constexpr int R = SP_TILE + 2;                       // scalar region: 34 x 34
-	constexpr int RW = SP_TILE + 8, RH = SP_TILE + 2;    // vector region: 40 x 34
+	constexpr int RW = SP_TILE + 8, RH = SP_TILE + 2;    // region: 40 x 34
 	__shared__ __align__(16) float sp[RW * RH];
 	__shared__ __align__(16) uint8_t sc[RW * RH];
 	__shared__ double sh[32];
@@ -2071,64 +2059,61 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_spmv5(const ProbDev *__restri
 	const float *pold = new_is_p2 ? pr.p : pr.p2;
 	float *pnew = new_is_p2 ? pr.p2 : pr.p;
 	FF pq = {0.f, 0.f};
-	if ((L.w & 3) == 0) {
-		const int x0 = t.y * SP_TILE - 4, y0 = t.z * SP_TILE - 1;
-		constexpr int NV = (RW * RH / 4 + SP_THREADS - 1) / SP_THREADS;
-		// p_old of the region in sp, the codes in sc (p_old is read whatever
-		// beta is: it is only used when beta != 0)
+	const bool vec = (L.w & 3) == 0;
+	const int x0 = t.y * SP_TILE - 4, y0 = t.z * SP_TILE - 1;
+	constexpr int NV = (RW * RH / 4 + SP_THREADS - 1) / SP_THREADS;
+	// p_old of the region in sp, the codes in sc (p_old is read whatever beta
+	// is: it is only used when beta != 0); groups of 4 cells of a row
 #pragma unroll
-		for (int it = 0; it < NV; it++) {
-			const int f = threadIdx.x + it * SP_THREADS;
-			if (f < RW * RH / 4) {
-				const int ry = f / (RW / 4), rx = 4 * (f - ry * (RW / 4)), gi = x0 + rx, gj = y0 + ry;
-				const bool in = gi >= 0 && gi < L.w && gj >= 0 && gj < L.h;
-				const size_t k = in ? (size_t)gj * L.w + gi : 0;
-				uint32_t cd = 0;
-				float4 po = make_float4(0.f, 0.f, 0.f, 0.f);
-				if (in) {
-					cd = *(const uint32_t *)(L.code + k);
-					if (cd) po = *(const float4 *)(pold + k);
-				}
-				const int c = ry * RW + rx;
-				*(uint32_t *)(sc + c) = cd;
-				*(float4 *)(sp + c) = po;
-			}
+	for (int it = 0; it < NV; it++) {
+		const int f = threadIdx.x + it * SP_THREADS;
+		if (f < RW * RH / 4) {
+			const int ry = f / (RW / 4), rx = 4 * (f - ry * (RW / 4)), gi = x0 + rx, gj = y0 + ry;
+			const int n = group_cells(gi, gj, L.w, L.h);
+			const size_t k = n ? (size_t)gj * L.w + gi : 0;
+			const uint32_t cd = gload4u8(L.code, k, n, vec);
+			const float4 po = cd ? gload4(pold, k, n, vec) : make_float4(0.f, 0.f, 0.f, 0.f);
+			const int c = ry * RW + rx;
+			*(uint32_t *)(sc + c) = cd;
+			*(float4 *)(sp + c) = po;
 		}
-		grid_wait();
-		grid_release();
-		const int active = st[prob].inner_active;
-		const double beta64 = st[prob].beta;
-		// z2 of the region, issued with the state's loads
-		float4 zr[NV];
+	}
+	grid_wait();
+	grid_release();
+	const int active = st[prob].inner_active;
+	const double beta64 = st[prob].beta;
+	// z2 of the region, issued with the state's loads
+	float4 zr[NV];
 #pragma unroll
-		for (int it = 0; it < NV; it++) {
-			const int f = threadIdx.x + it * SP_THREADS;
-			zr[it] = make_float4(0.f, 0.f, 0.f, 0.f);
-			if (f < RW * RH / 4) {
-				const int ry = f / (RW / 4), rx = 4 * (f - ry * (RW / 4)), gi = x0 + rx, gj = y0 + ry;
-				const uint32_t cd = *(const uint32_t *)(sc + ry * RW + rx);
-				if (cd) zr[it] = *(const float4 *)(L.z2 + (size_t)gj * L.w + gi);   // in the image
-			}
+	for (int it = 0; it < NV; it++) {
+		const int f = threadIdx.x + it * SP_THREADS;
+		zr[it] = make_float4(0.f, 0.f, 0.f, 0.f);
+		if (f < RW * RH / 4) {
+			const int ry = f / (RW / 4), rx = 4 * (f - ry * (RW / 4)), gi = x0 + rx, gj = y0 + ry;
+			const uint32_t cd = *(const uint32_t *)(sc + ry * RW + rx);
+			if (cd) zr[it] = gload4(L.z2, (size_t)gj * L.w + gi, min(4, L.w - gi), vec);   // in the image
 		}
-		if (!active) return;
-		const float beta = (float)beta64;
+	}
+	if (!active) return;
+	const float beta = (float)beta64;
 #pragma unroll
-		for (int it = 0; it < NV; it++) {
-			const int f = threadIdx.x + it * SP_THREADS;
-			if (f < RW * RH / 4) {
-				const int ry = f / (RW / 4), rx = 4 * (f - ry * (RW / 4));
-				const int c = ry * RW + rx;
-				const uint32_t cd = *(const uint32_t *)(sc + c);
-				const float4 zv = zr[it], po = *(const float4 *)(sp + c);
-				*(float4 *)(sp + c) = make_float4((cd & 1u) ? (beta != 0.f ? zv.x + beta * po.x : zv.x) : 0.f,
-						(cd & 0x100u) ? (beta != 0.f ? zv.y + beta * po.y : zv.y) : 0.f,
-						(cd & 0x10000u) ? (beta != 0.f ? zv.z + beta * po.z : zv.z) : 0.f,
-						(cd & 0x1000000u) ? (beta != 0.f ? zv.w + beta * po.w : zv.w) : 0.f);
-			}
+	for (int it = 0; it < NV; it++) {
+		const int f = threadIdx.x + it * SP_THREADS;
+		if (f < RW * RH / 4) {
+			const int ry = f / (RW / 4), rx = 4 * (f - ry * (RW / 4));
+			const int c = ry * RW + rx;
+			const uint32_t cd = *(const uint32_t *)(sc + c);
+			const float4 zv = zr[it], po = *(const float4 *)(sp + c);
+			*(float4 *)(sp + c) = make_float4((cd & 1u) ? (beta != 0.f ? zv.x + beta * po.x : zv.x) : 0.f,
+					(cd & 0x100u) ? (beta != 0.f ? zv.y + beta * po.y : zv.y) : 0.f,
+					(cd & 0x10000u) ? (beta != 0.f ? zv.z + beta * po.z : zv.z) : 0.f,
+					(cd & 0x1000000u) ? (beta != 0.f ? zv.w + beta * po.w : zv.w) : 0.f);
 		}
-		__syncthreads();
-		// 4 cells of a row per thread (every neighbour is in the region); p.q
-		// summed over them in row order, as k_spmv does for w % 4 == 0
+	}
+	__syncthreads();
+	// 4 cells of a row per thread (every neighbour is in the region); p.q
+	// summed over them in row order, as k_spmv does
+	{
 		const int ty = threadIdx.x >> 3, tx = 4 * (threadIdx.x & 7);
 		const int gi = t.y * SP_TILE + tx, gj = t.z * SP_TILE + ty;
 		const int c = (ty + 1) * RW + tx + 4;
@@ -2144,47 +2129,11 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_spmv5(const ProbDev *__restri
 				ff_add_prod(pq, pk[e], qk[e]);
 			}
 		}
-		if (gi < L.w && gj < L.h) {
+		const int n = group_cells(gi, gj, L.w, L.h);
+		if (n) {
 			const size_t k = (size_t)gj * L.w + gi;
-			*(float4 *)(pnew + k) = make_float4(pk[0], pk[1], pk[2], pk[3]);
-			*(float4 *)(pr.q + k) = make_float4(qk[0], qk[1], qk[2], qk[3]);
-		}
-	} else {
-		grid_wait();
-		grid_release();
-		const int active = st[prob].inner_active;
-		const double beta64 = st[prob].beta;
-		if (!active) return;
-		const float beta = (float)beta64;
-		uint8_t *sm = sc;
-		const int x0 = t.y * SP_TILE - 1, y0 = t.z * SP_TILE - 1;
-#pragma unroll
-		for (int it = 0; it < (R * R + SP_THREADS - 1) / SP_THREADS; it++) {
-			const int c = threadIdx.x + it * SP_THREADS;
-			if (c < R * R) {
-				const int ry = c / R, rx = c - ry * R, gi = x0 + rx, gj = y0 + ry;
-				const bool in = gi >= 0 && gi < L.w && gj >= 0 && gj < L.h;
-				const size_t k = in ? (size_t)gj * L.w + gi : 0;
-				const uint8_t m = in ? L.code[k] : 0;
-				const float zv = in ? L.z2[k] : 0.f;
-				const float po = (in && beta != 0.f) ? pold[k] : 0.f;
-				sm[c] = m;
-				sp[c] = (m & 1) ? (beta != 0.f ? zv + beta * po : zv) : 0.f;
-			}
-		}
-		__syncthreads();
-		for (int c = threadIdx.x; c < SP_TILE * SP_TILE; c += SP_THREADS) {
-			const int ty = c >> 5, tx = c & 31, gi = x0 + 1 + tx, gj = y0 + 1 + ty;
-			const int rc = (ty + 1) * R + tx + 1;
-			if (gi < L.w && gj < L.h && (sm[rc] & 1)) {
-				const size_t k = (size_t)gj * L.w + gi;
-				const float pk = sp[rc];
-				const int code = sm[rc];
-				const float qk = a5_diff(pk, sp[rc + 1], sp[rc - 1], sp[rc + R], sp[rc - R], code);
-				pnew[k] = pk;
-				pr.q[k] = qk;
-				ff_add_prod(pq, pk, qk);
-			}
+			gstore4(pnew, k, n, vec, make_float4(pk[0], pk[1], pk[2], pk[3]));
+			gstore4(pr.q, k, n, vec, make_float4(qk[0], qk[1], qk[2], qk[3]));
 		}
 	}
 	double tot[2];
