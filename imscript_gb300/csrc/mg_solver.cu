@@ -1370,33 +1370,77 @@ __device__ __forceinline__ void own_cells(int x0, int y0, int cells[2][4])
 		for (int k = 0; k < 4; k++) cells[col][k] = g_cells.v[col][k][threadIdx.x];
 }
 
-// Half-sweep of colour col over the cells with ring >= lo.  In the first
+// The smoothing sweeps of a tile kernel: half-sweep s (0 .. 2 NU5 - 1)
+// updates colour s & 1 on the cells of ring >= s in the pre-smoothing
+// (k_pre5), colour 1 - (s & 1) on the cells of ring >= s + 1 in the
+// post-smoothing (k_post5).  Which of a thread's 4 cells of that colour take
+// part is decided once per tile: bit 4 s + k of the masks is set when cell k
+// is unknown and on a deep enough ring.
+template <bool post>
+__device__ __forceinline__ uint32_t sweep_masks(const uint8_t *sc, const int cells[2][4])
+{
+	uint32_t unk = 0;   // bit 4 col + k: the cell is unknown
+#pragma unroll
+	for (int col = 0; col < 2; col++)
+#pragma unroll
+		for (int k = 0; k < 4; k++) {
+			const int e = cells[col][k];
+			if (e >= 0 && (sc[e & 2047] & 1)) unk |= 1u << (4 * col + k);
+		}
+	uint32_t m = 0;
+#pragma unroll
+	for (int s = 0; s < 2 * NU5; s++) {
+		const int col = post ? 1 - (s & 1) : (s & 1), lo = post ? s + 1 : s;
+#pragma unroll
+		for (int k = 0; k < 4; k++)
+			if (((unk >> (4 * col + k)) & 1u) && (cells[col][k] >> 11) >= lo) m |= 1u << (4 * s + k);
+	}
+	return m;
+}
+
+// Half-sweep of colour col over the cells of mask m (4 bits).  In the first
 // half-sweep from z = 0 (zero set) every neighbour is 0: the off-diagonal sum
 // is +0 and b - (+0) is b, so z = b / diag gives the same float.  In the
-// others (lo >= 1) every neighbour of an updated cell lies in the region, and
-// every neighbour off_code skips -- a known cell or one outside the image --
-// holds +0 in the region and is never written; x - (+0) is x for every float
-// (-0 and NaN included), so the four neighbours are subtracted without tests,
-// in off_code's order, with the same result.
-template <bool zero = false>
-__device__ __forceinline__ void sweep_cells(float *sz, const float *sb, const uint8_t *sc, const int cells[2][4],
-		int col, int lo)
+// others every neighbour of an updated cell lies in the region, and every
+// neighbour off_code skips -- a known cell or one outside the image -- holds
+// +0 in the region and is never written; x - (+0) is x for every float (-0
+// and NaN included), so the four neighbours are subtracted without tests, in
+// off_code's order, with the same result.  plain4: no cell of the region has
+// a clamped side (every diagonal is 4), and num * 0.25 is gs_div(num, 4).
+template <bool zero, bool plain4>
+__device__ __forceinline__ void sweep_masked(float *sz, const float *sb, const uint8_t *sc, const int cells[2][4],
+		int col, uint32_t m)
 {
 #pragma unroll
 	for (int k = 0; k < 4; k++) {
-		const int e = cells[col][k];
-		if (e < 0 || (e >> 11) < lo) continue;
-		const int c = e & 2047;
-		const int code = sc[c];
-		if (!(code & 1)) continue;
-		if (zero) {
-			sz[c] = gs_div(sb[c], diag_code(code));
-		} else {
-			const float off = (((0.f - sz[c + 1]) - sz[c - 1]) - sz[c + FR]) - sz[c - FR];
-			sz[c] = gs_div(sb[c] - off, diag_code(code));
-		}
+		if (!((m >> k) & 1u)) continue;
+		const int c = cells[col][k] & 2047;
+		const float num = zero ? sb[c] : sb[c] - ((((0.f - sz[c + 1]) - sz[c - 1]) - sz[c + FR]) - sz[c - FR]);
+		sz[c] = plain4 ? num * 0.25f : gs_div(num, diag_code(sc[c]));
 	}
 }
+
+// The 2 NU5 half-sweeps of k_pre5 (post = false: the first from z = 0) or
+// k_post5, each followed by a block barrier.
+template <bool post, bool plain4>
+__device__ __forceinline__ void run_sweeps(float *sz, const float *sb, const uint8_t *sc, const int cells[2][4],
+		uint32_t ms)
+{
+#pragma unroll
+	for (int s = 0; s < 2 * NU5; s++) {
+		const int col = post ? 1 - (s & 1) : (s & 1);
+		const uint32_t m = (ms >> (4 * s)) & 15u;
+		if (!post && s == 0)
+			sweep_masked<true, plain4>(sz, sb, sc, cells, col, m);
+		else
+			sweep_masked<false, plain4>(sz, sb, sc, cells, col, m);
+		__syncthreads();
+	}
+}
+
+// Clamp-count bits of 4 packed cell codes: nonzero when a cell of the group
+// lies on the image border (its diagonal is below 4).
+constexpr uint32_t CLAMP_BITS4 = 0xE0E0E0E0u;
 
 // Pre-smoothing from z = 0 (NU5 forward red-black sweeps), residual, and its
 // restriction (sum over the children) into b of level l+1.  Writes z of level
@@ -1453,6 +1497,9 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 			}
 		}
 	}
+	uint32_t clampbits = 0;   // any clamp bits in the thread's groups
+#pragma unroll
+	for (int it = 0; it < NV; it++) clampbits |= (fine && !L.tmb) ? cdv[it] : 0u;
 	grid_wait();
 	grid_release();
 	const int active = st[prob].inner_active, pending = st[prob].pending;
@@ -1511,6 +1558,7 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 				const int ry = f / (FR / 4), rx = 4 * (f - ry * (FR / 4));
 				const uint32_t cd = region_codes4(*(const uint32_t *)(stc + ry * 64 + rx + 12), rx, ry);
 				*(uint32_t *)(sc + ry * FR + rx) = cd;
+				clampbits |= cd;
 				if (upd && cd) {
 					const int gi = x0 + rx, gj = y0 + ry;   // a group with an unknown is in the image
 					const float4 qq = *(const float4 *)(qv + (size_t)gj * L.w + gi);
@@ -1558,15 +1606,15 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 	}
 	int cells[2][4];
 	own_cells(x0, y0, cells);
-	__syncthreads();
-	// half-sweep s updates colour s&1 on the cells of ring >= s; at s = 0 every
-	// neighbour is 0, so the outermost ring needs no outside value
-	sweep_cells<true>(sz, sb, sc, cells, 0, 0);
-	__syncthreads();
-	for (int s = 1; s < 2 * NU5; s++) {
-		sweep_cells(sz, sb, sc, cells, s & 1, s);
-		__syncthreads();
-	}
+	// the region holds the b and codes of every cell now; half-sweep s updates
+	// colour s&1 on the cells of ring >= s; at s = 0 every neighbour is 0, so
+	// the outermost ring needs no outside value
+	const bool plain4 = !__syncthreads_or((clampbits & CLAMP_BITS4) != 0);
+	const uint32_t ms = sweep_masks<false>(sc, cells);
+	if (plain4)
+		run_sweeps<false, true>(sz, sb, sc, cells, ms);
+	else
+		run_sweeps<false, false>(sz, sb, sc, cells, ms);
 	// write the pre-smoothed correction of the tile
 	{
 		const Grp g = grp_of(t, L.w, L.h);
@@ -1574,7 +1622,7 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 	}
 	// restriction: one coarse cell per thread.  A known child adds +0 to a sum
 	// that starts at +0 and so is never -0: it is skipped; an unknown one's
-	// neighbours are subtracted without tests (see sweep_cells)
+	// neighbours are subtracted without tests (see sweep_masked)
 	if (cun) {
 		float acc = 0.f;
 		for (int bb = 0; bb < 2; bb++)
@@ -1639,6 +1687,7 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_post5(const ProbDev *__restri
 	constexpr int NV = (FN / 4 + SP_THREADS - 1) / SP_THREADS;
 	const bool vec = (L.w & 3) == 0;
 	uint32_t addm = 0;   // per group (4 bits each) the cells that take the correction
+	uint32_t clampbits = 0;   // any clamp bits in the thread's groups
 	if (fine) {
 		// groups of 4 cells of a row (with w % 4 == 0 wholly inside or outside
 		// the image, every access aligned)
@@ -1651,6 +1700,7 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_post5(const ProbDev *__restri
 				const size_t k = n ? (size_t)gj * L.w + gi : 0;
 				const size_t kc = n ? (size_t)(gj >> 1) * C.w + (gi >> 1) : 0;
 				const uint32_t cd = region_codes4(gload4u8(L.code, k, n, vec), rx, ry);
+				clampbits |= cd;
 				float4 bv = make_float4(0.f, 0.f, 0.f, 0.f), zv = bv;
 				uint8_t cm0 = 0, cm1 = 0;
 				if (cd) {
@@ -1700,12 +1750,13 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_post5(const ProbDev *__restri
 	}
 	int cells[2][4];
 	own_cells(x0, y0, cells);
-	__syncthreads();
 	// half-sweep s updates colour 1 - (s&1) on the cells of ring >= s + 1
-	for (int s = 0; s < 2 * NU5; s++) {
-		sweep_cells(sz, sb, sc, cells, 1 - (s & 1), s + 1);
-		__syncthreads();
-	}
+	const bool plain4 = !__syncthreads_or((clampbits & CLAMP_BITS4) != 0);
+	const uint32_t ms = sweep_masks<true>(sc, cells);
+	if (plain4)
+		run_sweeps<true, true>(sz, sb, sc, cells, ms);
+	else
+		run_sweeps<true, false>(sz, sb, sc, cells, ms);
 	// z2 of the tile and, in k_rz's order, r.z
 	FF rz = {0.f, 0.f};
 	{
