@@ -2634,9 +2634,9 @@ struct KTimer {
 constexpr double BPX_PRE5 = 1 + 4 + 4 + 0.25 + 1;         // mask, b, z; coarse mask, coarse b
 constexpr double BPX_POST5 = 1 + 4 + 4 + 1 + 0.25 + 4;    // mask, b, z, coarse z2, coarse mask; z2
 constexpr double BPX_SPMV5 = 1 + 4 + 4 + 4 + 4;           // mask, z2, p_old; p_new, q
-constexpr double BPX_STEP = 4 + 4 + 4 + 4 + 4;            // k_pre5's PCG step: q, x, p; x, r
-constexpr double BPX_RESID64 = 1 + 8 + 4 + 4 + 4;         // mask, U, rhs; b, x
-constexpr double BPX_UADD = 1 + 8 + 4 + 8;                // mask, U, x; U
+constexpr double BPX_STEP = 4 + 4 + 4 + 4 + 1 + 4 + 4 + 4; // k_pre5's PCG step: q, x, xlo, p, mask; x, xlo, r
+constexpr double BPX_RESID64 = 1 + 8 + 4 + 4 + 4 + 4;     // mask, U, rhs; b, x, xlo
+constexpr double BPX_UADD = 1 + 8 + 4 + 4 + 8;            // mask, U, x, xlo; U
 constexpr double BPC_COARSE5 = 1 + 4 + 4 + 0.34;          // per top coarse cell: mask, b; z2; coarser masks
 
 #define KT_BEGIN(pl, s)                                            \
