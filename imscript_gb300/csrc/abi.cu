@@ -150,57 +150,92 @@ std::string tune_key(const std::vector<MgProblem> &sub, int kind, const MgOption
 	return key;
 }
 
-// Solve the batch once per distinct hand-over size among the default, 32, 64
-// and 128 (sizes that put the same levels in the same kernels are tried
-// once): one untimed solve that captures the solve graph, then the best of
-// two timed ones (CUDA events on the context's stream around the whole call).
-// Every candidate writes the same bits, so the batch is left solved.
+// The autotuner: coordinate descent over the fused V-cycle's two launch
+// choices.  First the hand-over size among the default, 32, 64 and 128 at the
+// given sweeps per side (sizes that put the same levels in the same kernels
+// are tried once; every size gives the same bits), then the sweeps per side,
+// 1, 2 and 3, at the best hand-over (each count its own preconditioner: the
+// iterates differ, every result meets the tolerance).  A candidate gets one
+// untimed solve, which captures its solve graph, and the best of two timed
+// ones (CUDA events on the context's stream around the whole call).  A choice
+// the caller fixed is not tuned.  The batch is left solved with the chosen
+// pair.
 int tune_and_solve(simpois_ctx *ctx, const std::vector<MgProblem> &sub, MgOptions opt, simpois_report *r,
-		int *chosen)
+		bool tune_cm, bool tune_nu, int *chosen_cm, int *chosen_nu)
 {
-	const int cands[] = {mg_default_coarse_max(), 32, 64, 128};
-	std::vector<std::vector<int>> seen;
 	cudaEvent_t a, b;
 	SP_CUDA(ctx, cudaEventCreate(&a));
 	if (cudaEventCreate(&b) != cudaSuccess) {
 		cudaEventDestroy(a);
 		return ctx_fail(ctx, SIMPOIS_ECUDA, "cudaEventCreate");
 	}
-	float best_ms = 0;
-	int best = 0, rc = SIMPOIS_OK;
-	for (int c : cands) {
-		std::vector<int> nf;
-		for (const MgProblem &q : sub) nf.push_back(mg_handover_level(q.w, q.h, c));
-		if (std::find(seen.begin(), seen.end(), nf) != seen.end()) continue;
-		seen.push_back(nf);
-		opt.coarse_max = c;
-		rc = mg_solve(ctx, sub.data(), (int)sub.size(), opt, r);
-		if (rc) break;
-		float t = 0;
-		for (int k = 0; k < 2 && !rc; k++) {
+	int rc = SIMPOIS_OK;
+	int last_cm = -1, last_nu = -1;   // the pair of the last solve
+	auto timed = [&](int cm, int nu, float *best_ms) -> int {
+		opt.coarse_max = cm;
+		opt.nu = nu;
+		int e = mg_solve(ctx, sub.data(), (int)sub.size(), opt, r);
+		for (int k = 0; k < 2 && !e; k++) {
 			float ms = 0;
 			cudaEventRecord(a, ctx->stream);
-			rc = mg_solve(ctx, sub.data(), (int)sub.size(), opt, r);
+			e = mg_solve(ctx, sub.data(), (int)sub.size(), opt, r);
 			cudaEventRecord(b, ctx->stream);
-			if (cudaEventSynchronize(b) != cudaSuccess || cudaEventElapsedTime(&ms, a, b) != cudaSuccess)
-				rc = ctx_fail(ctx, SIMPOIS_ECUDA, "autotuner timing: %s", cudaGetErrorString(cudaGetLastError()));
-			t = k == 0 ? ms : std::min(t, ms);
+			if (!e && (cudaEventSynchronize(b) != cudaSuccess || cudaEventElapsedTime(&ms, a, b) != cudaSuccess))
+				e = ctx_fail(ctx, SIMPOIS_ECUDA, "autotuner timing: %s", cudaGetErrorString(cudaGetLastError()));
+			*best_ms = k == 0 ? ms : std::min(*best_ms, ms);
 		}
-		if (rc) break;
-		if (best == 0 || t < best_ms) {
-			best_ms = t;
-			best = c;
+		last_cm = cm;
+		last_nu = nu;
+		return e;
+	};
+	const int nu0 = opt.nu > 0 ? opt.nu : 2;
+	int best_cm = opt.coarse_max, best_nu = nu0;
+	float best_ms = 0;
+	bool have = false;
+	if (tune_cm) {
+		const int cands[] = {mg_default_coarse_max(), 32, 64, 128};
+		std::vector<std::vector<int>> seen;
+		for (int c : cands) {
+			std::vector<int> nf;
+			for (const MgProblem &q : sub) nf.push_back(mg_handover_level(q.w, q.h, c));
+			if (std::find(seen.begin(), seen.end(), nf) != seen.end()) continue;
+			seen.push_back(nf);
+			float t = 0;
+			if ((rc = timed(c, nu0, &t))) break;
+			if (!have || t < best_ms) {
+				best_ms = t;
+				best_cm = c;
+				have = true;
+			}
 		}
+	}
+	if (!rc && tune_nu) {
+		for (int nu = 1; nu <= 3 && !rc; nu++) {
+			if (have && nu == nu0) continue;   // measured above
+			float t = 0;
+			if ((rc = timed(best_cm, nu, &t))) break;
+			if (!have || t < best_ms) {
+				best_ms = t;
+				best_nu = nu;
+				have = true;
+			}
+		}
+	}
+	if (!rc && (last_cm != best_cm || last_nu != best_nu)) {
+		opt.coarse_max = best_cm;
+		opt.nu = best_nu;
+		rc = mg_solve(ctx, sub.data(), (int)sub.size(), opt, r);
 	}
 	cudaEventDestroy(a);
 	cudaEventDestroy(b);
 	if (rc) return rc;
-	*chosen = best;
+	*chosen_cm = best_cm;
+	*chosen_nu = best_nu;
 	return SIMPOIS_OK;
 }
 
 int run_converged(simpois_ctx *ctx, const simpois_image *im, int n, const simpois_params *p,
-		simpois_report *rep, int tune = 0, int *tuned_cm = nullptr)
+		simpois_report *rep, int tune = 0, int *tuned_cm = nullptr, int *tuned_nu = nullptr)
 {
 	std::vector<MgProblem> probs;
 	std::vector<int> img_of;
@@ -249,24 +284,29 @@ int run_converged(simpois_ctx *ctx, const simpois_image *im, int n, const simpoi
 		MgOptions o = opt;
 		const std::string key = tune_key(sub, kind, opt);
 		const bool tunable = o.fused && o.use_mg && !o.ktimer;
-		if (ctx->coarse_max_fixed > 0) {
-			o.coarse_max = ctx->coarse_max_fixed;
-		} else if (tune && tunable) {
-			int best = 0;
-			rc = tune_and_solve(ctx, sub, o, r.data(), &best);
+		if (ctx->coarse_max_fixed > 0) o.coarse_max = ctx->coarse_max_fixed;
+		if (ctx->sweeps_fixed > 0) o.nu = ctx->sweeps_fixed;
+		const bool tune_cm = ctx->coarse_max_fixed <= 0, tune_nu = ctx->sweeps_fixed <= 0;
+		const bool tuning = tune && tunable && (tune_cm || tune_nu);
+		if (tuning) {
+			int bc = 0, bn = 0;
+			rc = tune_and_solve(ctx, sub, o, r.data(), tune_cm, tune_nu, &bc, &bn);
 			if (rc) return rc;
-			ctx->tuned[key] = best;
-			o.coarse_max = best;
+			ctx->tuned[key] = {bc, bn};
+			o.coarse_max = bc;
+			o.nu = bn;
 		} else {
 			auto it = ctx->tuned.find(key);
-			if (it != ctx->tuned.end()) o.coarse_max = it->second;
-		}
-		if (!(tune && tunable && ctx->coarse_max_fixed <= 0)) {
+			if (it != ctx->tuned.end()) {
+				if (tune_cm) o.coarse_max = it->second.coarse_max;
+				if (tune_nu) o.nu = it->second.nu;
+			}
 			rc = mg_solve(ctx, sub.data(), (int)sub.size(), o, r.data());
 			if (rc) return rc;
 		}
 		if (tuned_cm && (kind == 0 || tuned_cm[0] == 0))
 			tuned_cm[0] = o.coarse_max > 0 ? o.coarse_max : mg_default_coarse_max();
+		if (tuned_nu && (kind == 0 || tuned_nu[0] == 0)) tuned_nu[0] = o.nu > 0 ? o.nu : 2;
 		for (size_t q = 0; q < sub.size(); q++) rep[where[q]] = r[q];
 	}
 	// singular channels: the reference schedule, as the reference would run them
@@ -543,7 +583,7 @@ int simpois_solve(simpois_ctx *ctx, float *out, const float *in, const float *da
 }
 
 static int solve_batch(simpois_ctx *ctx, const simpois_image *images, int n, const simpois_params *params,
-		simpois_report *reports, int tune, int *coarse_max)
+		simpois_report *reports, int tune, int *coarse_max, int *sweeps = nullptr)
 {
 	if (!ctx || (!images && n > 0) || n < 0) return ctx_fail(ctx, SIMPOIS_EINVAL, "bad batch");
 	simpois_params p;
@@ -580,7 +620,7 @@ static int solve_batch(simpois_ctx *ctx, const simpois_image *images, int n, con
 		int nch = 0;
 		for (auto &im : conv) nch += im.pd;
 		std::vector<simpois_report> r(nch);
-		rc = run_converged(ctx, conv.data(), (int)conv.size(), &p, r.data(), tune, coarse_max);
+		rc = run_converged(ctx, conv.data(), (int)conv.size(), &p, r.data(), tune, coarse_max, sweeps);
 		if (rc) return rc;
 		int q = 0;
 		for (size_t k = 0; k < conv.size(); k++)
@@ -646,13 +686,28 @@ int simpois_solve_batch_host(simpois_ctx *ctx, const simpois_image *images, int 
 	return st;
 }
 
+int simpois_autotune_ex(simpois_ctx *ctx, const simpois_image *images, int n, const simpois_params *params,
+		simpois_report *reports, int *coarse_max, int *sweeps)
+{
+	int cm = 0, nu = 0;
+	const int st = solve_batch(ctx, images, n, params, reports, 1, &cm, &nu);
+	if (coarse_max) *coarse_max = cm;
+	if (sweeps) *sweeps = nu;
+	return st;
+}
+
 int simpois_autotune(simpois_ctx *ctx, const simpois_image *images, int n, const simpois_params *params,
 		simpois_report *reports, int *coarse_max)
 {
-	int cm = 0;
-	const int st = solve_batch(ctx, images, n, params, reports, 1, &cm);
-	if (coarse_max) *coarse_max = cm;
-	return st;
+	return simpois_autotune_ex(ctx, images, n, params, reports, coarse_max, nullptr);
+}
+
+int simpois_set_sweeps(simpois_ctx *ctx, int sweeps)
+{
+	if (!ctx) return SIMPOIS_EINVAL;
+	if (sweeps < 0 || sweeps > 3) return ctx_fail(ctx, SIMPOIS_EINVAL, "sweeps per side %d outside 1..3", sweeps);
+	ctx->sweeps_fixed = sweeps;
+	return SIMPOIS_OK;
 }
 
 int simpois_set_coarse_max(simpois_ctx *ctx, int coarse_max)
@@ -733,9 +788,13 @@ int simpois_adjoint_device(simpois_ctx *ctx, const float *grad_out, const float 
 	opt.fused = !(p.flags & SIMPOIS_FLAG_UNFUSED);
 	opt.mode = MG_ADJOINT;
 	opt.coarse_max = ctx->coarse_max_fixed;
-	if (opt.coarse_max <= 0) {   // the forward fill's tuned hand-over, if any
+	opt.nu = ctx->sweeps_fixed;
+	{   // the forward fill's tuned choices, if any
 		auto it = ctx->tuned.find(tune_key(probs, 0, opt));
-		if (it != ctx->tuned.end()) opt.coarse_max = it->second;
+		if (it != ctx->tuned.end()) {
+			if (opt.coarse_max <= 0) opt.coarse_max = it->second.coarse_max;
+			if (opt.nu <= 0) opt.nu = it->second.nu;
+		}
 	}
 	opt.grad_out = go.data();
 	opt.grad_in = gi.data();

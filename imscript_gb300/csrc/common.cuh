@@ -76,7 +76,13 @@ struct simpois_ctx {
 	// fused V-cycle hand-over size: fixed by the caller (0: none), and the
 	// autotuner's choice per batch shape
 	int coarse_max_fixed = 0;
-	std::map<std::string, int> tuned;
+	// smoothing sweeps per side of the fused V-cycle: fixed by the caller (0:
+	// none); with the hand-over, the autotuner's choice per batch shape
+	int sweeps_fixed = 0;
+	struct Tuned {
+		int coarse_max, nu;
+	};
+	std::map<std::string, Tuned> tuned;
 
 	// the AMLE sweeps of the last call and the call they were captured for
 	cudaGraphExec_t amle_exec = nullptr;

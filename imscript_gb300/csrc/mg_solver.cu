@@ -1153,12 +1153,26 @@ __global__ void k_coarsest(const ProbDev *__restrict__ P, const ProbState *__res
 // fused cycle computes what the per-sweep kernels compute, bit for bit (the
 // float operations are issued in the same order as in split<0>).
 
-constexpr int FH = 2 * NU5;           // halo: one pixel per half-sweep
-constexpr int FR = SP_TILE + 2 * FH;  // side of the shared region (40)
-constexpr int FN = FR * FR;
-// the vectorised region loads move aligned groups of 4 cells: the region's
-// first column (tile x - FH) and its width must be multiples of 4
-static_assert(FH % 4 == 0 && FR % 4 == 0, "region columns must stay 4-aligned");
+// Region geometry of the tile kernels for NU sweeps per side (2 NU
+// half-sweeps): the halo FH needs one pixel per half-sweep and stays a
+// multiple of 4 (the region loads move aligned groups of 4 cells: the region's
+// first column, tile x - FH, and its width must be multiples of 4), so NU = 1
+// and 2 use a halo of 4, NU = 3 one of 8.  The pre-smoothing's first
+// half-sweep starts on ring R0 = FH - 2 NU of the region.
+template <int NU>
+struct Geo {
+	static constexpr int FH = NU <= 2 ? 4 : 8;
+	static constexpr int FR = SP_TILE + 2 * FH;   // side of the shared region
+	static constexpr int FN = FR * FR;
+	static constexpr int H = 2 * NU;              // half-sweeps per side
+	static constexpr int R0 = FH - H;
+	static constexpr int KC = (FN / 2 + SP_THREADS - 1) / SP_THREADS;   // cells of a colour per thread
+	static constexpr int NV = (FN / 4 + SP_THREADS - 1) / SP_THREADS;   // 4-cell groups per thread
+	static_assert(FH % 4 == 0 && FR % 4 == 0 && R0 >= 0, "region columns must stay 4-aligned");
+	static_assert(KC * H <= 32, "the sweep masks fit 32 bits");
+};
+// the sweeps-per-side values the fused kernels are built for
+constexpr int NU_MIN = 1, NU_MAX = 3;
 // FP32 inner solves stop at this relative decrease at the latest (the FP32
 // recurrence drifts below it); SIMPOIS_TAU_MIN overrides it for tuning.
 double tau_min()
@@ -1299,6 +1313,7 @@ __device__ __forceinline__ bool mbar_wait0(uint64_t *bar, int *timeout_flag)
 // Region code of a shared region cell: the level's cell code (cell_code) with
 // the neighbour bits that point out of the region cleared (those cells are
 // not in shared memory), for a group of 4 cells of a row (x the lowest byte).
+template <int FR>
 __device__ __forceinline__ uint32_t region_codes4(uint32_t cd, int rx, int ry)
 {
 	if (rx == 0) cd &= ~0x00000004u;        // W of the first column
@@ -1322,35 +1337,41 @@ __device__ __forceinline__ float off_code(const float *z, int c, int R, int code
 
 __device__ __forceinline__ float diag_code(int code) { return 4.f - (float)(code >> 5); }
 
-// The colour cells of the 40x40 region a thread owns: for colour col, cell
-// q = tid + 256 k (k < 4, q < 800) of the compacted class, packed as
-// (region index) | (ring << 11); ring = distance to the region's edge.
+// The colour cells of the FR x FR region a thread owns: for colour col, cell
+// q = tid + 256 k (k < KC, q < FN / 2) of the compacted class, packed as
+// (region index) | (ring << 12); ring = distance to the region's edge.
 // x0 + y0 is even for every tile (both are multiples of 32 minus FH), so
 // the cells depend on the thread alone: a table built at compile time.
+template <int FR>
 struct CellTable {
-	int v[2][4][SP_THREADS];
+	static constexpr int KC = (FR * FR / 2 + SP_THREADS - 1) / SP_THREADS;
+	int v[2][KC][SP_THREADS];
 };
 
-constexpr CellTable make_cell_table()
+template <int FR>
+constexpr CellTable<FR> make_cell_table()
 {
-	CellTable t{};
+	CellTable<FR> t{};
 	for (int col = 0; col < 2; col++)
-		for (int k = 0; k < 4; k++)
+		for (int k = 0; k < CellTable<FR>::KC; k++)
 			for (int tid = 0; tid < SP_THREADS; tid++) {
 				const int q = tid + SP_THREADS * k;
-				if (q >= FN / 2) {
+				if (q >= FR * FR / 2) {
 					t.v[col][k][tid] = -1;
 					continue;
 				}
 				const int ry = q / (FR / 2);
 				const int rx = 2 * (q - ry * (FR / 2)) + ((col ^ ry) & 1);
 				const int a = rx < ry ? rx : ry, b = FR - 1 - rx < FR - 1 - ry ? FR - 1 - rx : FR - 1 - ry;
-				t.v[col][k][tid] = (ry * FR + rx) | ((a < b ? a : b) << 11);
+				t.v[col][k][tid] = (ry * FR + rx) | ((a < b ? a : b) << 12);
 			}
 	return t;
 }
 
-__device__ const CellTable g_cells = make_cell_table();
+__device__ const CellTable<Geo<2>::FR> g_cells40 = make_cell_table<Geo<2>::FR>();
+__device__ const CellTable<Geo<3>::FR> g_cells48 = make_cell_table<Geo<3>::FR>();
+static_assert(Geo<1>::FR == Geo<2>::FR, "NU = 1 and 2 share the region");
+constexpr int CELL_MASK = 4095;   // region index of a cell-table entry
 
 // Programmatic dependent launch.  A kernel launched with programmatic stream
 // serialisation may be scheduled while the kernel before it drains; it calls
@@ -1360,45 +1381,56 @@ __device__ const CellTable g_cells = make_cell_table();
 // kernel be scheduled.  Without the launch attribute both are no-ops.
 __device__ __forceinline__ void grid_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void grid_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
-static_assert(FH % 2 == 0, "x0 + y0 must stay even for the cell table");
 
-__device__ __forceinline__ void own_cells(int x0, int y0, int cells[2][4])
+template <int NU>
+__device__ __forceinline__ void own_cells(int cells[2][Geo<NU>::KC])
 {
+	constexpr int KC = Geo<NU>::KC;
 #pragma unroll
 	for (int col = 0; col < 2; col++)
 #pragma unroll
-		for (int k = 0; k < 4; k++) cells[col][k] = g_cells.v[col][k][threadIdx.x];
+		for (int k = 0; k < KC; k++) {
+			if constexpr (Geo<NU>::FR == 40)
+				cells[col][k] = g_cells40.v[col][k][threadIdx.x];
+			else
+				cells[col][k] = g_cells48.v[col][k][threadIdx.x];
+		}
 }
 
-// The smoothing sweeps of a tile kernel: half-sweep s (0 .. 2 NU5 - 1)
-// updates colour s & 1 on the cells of ring >= s in the pre-smoothing
-// (k_pre5), colour 1 - (s & 1) on the cells of ring >= s + 1 in the
-// post-smoothing (k_post5).  Which of a thread's 4 cells of that colour take
-// part is decided once per tile: bit 4 s + k of the masks is set when cell k
-// is unknown and on a deep enough ring.
-template <bool post>
-__device__ __forceinline__ uint32_t sweep_masks(const uint8_t *sc, const int cells[2][4])
+// The smoothing sweeps of a tile kernel: half-sweep s (0 .. H - 1) updates
+// colour s & 1 on the cells of ring >= R0 + s in the pre-smoothing (k_pre5),
+// colour 1 - (s & 1) on the cells of ring >= R0 + s + 1 in the
+// post-smoothing (k_post5): every cell whose value reaches the tile (ring >=
+// FH) through the remaining half-sweeps, so the tile's values are exact (and
+// after the pre-smoothing ring FH - 1 too, which the restriction's residual
+// reads).  Which of a thread's KC cells of that colour take part is decided
+// once per tile: bit KC s + k of the masks is set when cell k is unknown and
+// on a deep enough ring.
+template <int NU, bool post>
+__device__ __forceinline__ uint32_t sweep_masks(const uint8_t *sc, const int cells[2][Geo<NU>::KC])
 {
-	uint32_t unk = 0;   // bit 4 col + k: the cell is unknown
+	using G = Geo<NU>;
+	constexpr int KC = G::KC;
+	uint32_t unk = 0;   // bit KC col + k: the cell is unknown
 #pragma unroll
 	for (int col = 0; col < 2; col++)
 #pragma unroll
-		for (int k = 0; k < 4; k++) {
+		for (int k = 0; k < KC; k++) {
 			const int e = cells[col][k];
-			if (e >= 0 && (sc[e & 2047] & 1)) unk |= 1u << (4 * col + k);
+			if (e >= 0 && (sc[e & CELL_MASK] & 1)) unk |= 1u << (KC * col + k);
 		}
 	uint32_t m = 0;
 #pragma unroll
-	for (int s = 0; s < 2 * NU5; s++) {
-		const int col = post ? 1 - (s & 1) : (s & 1), lo = post ? s + 1 : s;
+	for (int s = 0; s < G::H; s++) {
+		const int col = post ? 1 - (s & 1) : (s & 1), lo = G::R0 + (post ? s + 1 : s);
 #pragma unroll
-		for (int k = 0; k < 4; k++)
-			if (((unk >> (4 * col + k)) & 1u) && (cells[col][k] >> 11) >= lo) m |= 1u << (4 * s + k);
+		for (int k = 0; k < KC; k++)
+			if (((unk >> (KC * col + k)) & 1u) && (cells[col][k] >> 12) >= lo) m |= 1u << (KC * s + k);
 	}
 	return m;
 }
 
-// Half-sweep of colour col over the cells of mask m (4 bits).  In the first
+// Half-sweep of colour col over the cells of mask m (KC bits).  In the first
 // half-sweep from z = 0 (zero set) every neighbour is 0: the off-diagonal sum
 // is +0 and b - (+0) is b, so z = b / diag gives the same float.  In the
 // others every neighbour of an updated cell lies in the region, and every
@@ -1407,33 +1439,35 @@ __device__ __forceinline__ uint32_t sweep_masks(const uint8_t *sc, const int cel
 // and NaN included), so the four neighbours are subtracted without tests, in
 // off_code's order, with the same result.  plain4: no cell of the region has
 // a clamped side (every diagonal is 4), and num * 0.25 is gs_div(num, 4).
-template <bool zero, bool plain4>
-__device__ __forceinline__ void sweep_masked(float *sz, const float *sb, const uint8_t *sc, const int cells[2][4],
-		int col, uint32_t m)
+template <int NU, bool zero, bool plain4>
+__device__ __forceinline__ void sweep_masked(float *sz, const float *sb, const uint8_t *sc,
+		const int cells[2][Geo<NU>::KC], int col, uint32_t m)
 {
+	constexpr int FR = Geo<NU>::FR;
 #pragma unroll
-	for (int k = 0; k < 4; k++) {
+	for (int k = 0; k < Geo<NU>::KC; k++) {
 		if (!((m >> k) & 1u)) continue;
-		const int c = cells[col][k] & 2047;
+		const int c = cells[col][k] & CELL_MASK;
 		const float num = zero ? sb[c] : sb[c] - ((((0.f - sz[c + 1]) - sz[c - 1]) - sz[c + FR]) - sz[c - FR]);
 		sz[c] = plain4 ? num * 0.25f : gs_div(num, diag_code(sc[c]));
 	}
 }
 
-// The 2 NU5 half-sweeps of k_pre5 (post = false: the first from z = 0) or
+// The H half-sweeps of k_pre5 (post = false: the first from z = 0) or
 // k_post5, each followed by a block barrier.
-template <bool post, bool plain4>
-__device__ __forceinline__ void run_sweeps(float *sz, const float *sb, const uint8_t *sc, const int cells[2][4],
-		uint32_t ms)
+template <int NU, bool post, bool plain4>
+__device__ __forceinline__ void run_sweeps(float *sz, const float *sb, const uint8_t *sc,
+		const int cells[2][Geo<NU>::KC], uint32_t ms)
 {
+	constexpr int KC = Geo<NU>::KC;
 #pragma unroll
-	for (int s = 0; s < 2 * NU5; s++) {
+	for (int s = 0; s < Geo<NU>::H; s++) {
 		const int col = post ? 1 - (s & 1) : (s & 1);
-		const uint32_t m = (ms >> (4 * s)) & 15u;
+		const uint32_t m = (ms >> (KC * s)) & ((1u << KC) - 1u);
 		if (!post && s == 0)
-			sweep_masked<true, plain4>(sz, sb, sc, cells, col, m);
+			sweep_masked<NU, true, plain4>(sz, sb, sc, cells, col, m);
 		else
-			sweep_masked<false, plain4>(sz, sb, sc, cells, col, m);
+			sweep_masked<NU, false, plain4>(sz, sb, sc, cells, col, m);
 		__syncthreads();
 	}
 }
@@ -1451,10 +1485,12 @@ constexpr uint32_t CLAMP_BITS4 = 0xE0E0E0E0u;
 // as neighbouring tiles still read the old r of this tile's cells), with r
 // recomputed on the whole region as the right-hand side of the sweeps, and
 // |r|^2 summed and tested as in k_xr (same operations, same order).
+template <int NU>
 __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *st, const int4 *__restrict__ tl,
 		int l, const int *__restrict__ tbeg, const int *__restrict__ tcnt, double *partial, Globals *gl,
 		int use_p2)
 {
+	constexpr int FH = Geo<NU>::FH, FR = Geo<NU>::FR, FN = Geo<NU>::FN;
 	__shared__ __align__(128) float sb[FN];
 	__shared__ __align__(128) uint8_t stc[FR * 64];   // TMA: the code box (64 bytes a row)
 	__shared__ __align__(16) float sz[FN];
@@ -1479,8 +1515,9 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 	const bool cun = fine && ci < C.w && cj < C.h && C.mask[(size_t)cj * C.w + ci];
 	constexpr int NV = (FN / 4 + SP_THREADS - 1) / SP_THREADS;   // 4-cell groups per thread
 	const bool vec = (L.w & 3) == 0;
+	const bool tma = NU == 2 && L.tmb;   // the TMA boxes are laid out for a halo of 4
 	uint32_t cdv[NV];   // the region codes of the thread's groups
-	if (fine && !L.tmb) {
+	if (fine && !tma) {
 #pragma unroll
 		for (int it = 0; it < NV; it++) {
 			const int f = threadIdx.x + it * SP_THREADS;
@@ -1489,7 +1526,7 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 				const int ry = f / (FR / 4), rx = 4 * (f - ry * (FR / 4)), gi = x0 + rx, gj = y0 + ry;
 				const int n = group_cells(gi, gj, L.w, L.h);
 				const size_t k = n ? (size_t)gj * L.w + gi : 0;
-				const uint32_t cd = region_codes4(gload4u8(L.code, k, n, vec), rx, ry);
+				const uint32_t cd = region_codes4<FR>(gload4u8(L.code, k, n, vec), rx, ry);
 				cdv[it] = cd;
 				const int c = ry * FR + rx;
 				*(uint32_t *)(sc + c) = cd;
@@ -1499,7 +1536,7 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 	}
 	uint32_t clampbits = 0;   // any clamp bits in the thread's groups
 #pragma unroll
-	for (int it = 0; it < NV; it++) clampbits |= (fine && !L.tmb) ? cdv[it] : 0u;
+	for (int it = 0; it < NV; it++) clampbits |= (fine && !tma) ? cdv[it] : 0u;
 	grid_wait();
 	grid_release();
 	const int active = st[prob].inner_active, pending = st[prob].pending;
@@ -1509,7 +1546,7 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 	const float *qv = pr.q;
 	// b (and at level 0 q) of the region: issued with the state's loads, before
 	// the early-return test, so that one round trip follows the wait
-	if (fine && !L.tmb) {
+	if (fine && !tma) {
 #pragma unroll
 		for (int it = 0; it < NV; it++) {
 			const int f = threadIdx.x + it * SP_THREADS;
@@ -1537,7 +1574,7 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 		}
 	}
 	if (!active || !fine) return;
-	if (L.tmb) {
+	if (tma) {
 		// TMA: b as a 40 x 40 box at (x0, y0) straight into sb, the codes as a
 		// 64 x 40 box from x0 - 12 (a 16-byte boundary); out of the image both
 		// read 0 (a known cell).  b stays unmasked: it is read at unknown cells
@@ -1556,7 +1593,7 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 			const int f = threadIdx.x + it * SP_THREADS;
 			if (f < FN / 4) {
 				const int ry = f / (FR / 4), rx = 4 * (f - ry * (FR / 4));
-				const uint32_t cd = region_codes4(*(const uint32_t *)(stc + ry * 64 + rx + 12), rx, ry);
+				const uint32_t cd = region_codes4<FR>(*(const uint32_t *)(stc + ry * 64 + rx + 12), rx, ry);
 				*(uint32_t *)(sc + ry * FR + rx) = cd;
 				clampbits |= cd;
 				if (upd && cd) {
@@ -1604,17 +1641,17 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 			st4(pr.b_alt, g, rk);
 		}
 	}
-	int cells[2][4];
-	own_cells(x0, y0, cells);
+	int cells[2][Geo<NU>::KC];
+	own_cells<NU>(cells);
 	// the region holds the b and codes of every cell now; half-sweep s updates
-	// colour s&1 on the cells of ring >= s; at s = 0 every neighbour is 0, so
-	// the outermost ring needs no outside value
+	// colour s&1 on the cells of ring >= R0 + s; at s = 0 every neighbour is
+	// 0, so the outermost ring needs no outside value
 	const bool plain4 = !__syncthreads_or((clampbits & CLAMP_BITS4) != 0);
-	const uint32_t ms = sweep_masks<false>(sc, cells);
+	const uint32_t ms = sweep_masks<NU, false>(sc, cells);
 	if (plain4)
-		run_sweeps<false, true>(sz, sb, sc, cells, ms);
+		run_sweeps<NU, false, true>(sz, sb, sc, cells, ms);
 	else
-		run_sweeps<false, false>(sz, sb, sc, cells, ms);
+		run_sweeps<NU, false, false>(sz, sb, sc, cells, ms);
 	// write the pre-smoothed correction of the tile
 	{
 		const Grp g = grp_of(t, L.w, L.h);
@@ -1664,10 +1701,12 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 // Coarse correction (injection from z2 of level l+1) and post-smoothing
 // (NU5 backward sweeps); writes z2 of level l.  At level 0 also r.z and the
 // PCG scalars beta, rho (the last tile of the problem to finish).
+template <int NU>
 __global__ void __launch_bounds__(SP_THREADS, 8) k_post5(const ProbDev *__restrict__ P, ProbState *st,
 		const int4 *__restrict__ tl, int l, const int *__restrict__ tbeg, const int *__restrict__ tcnt,
 		double *partial, Globals *gl, int pcg)
 {
+	constexpr int FH = Geo<NU>::FH, FR = Geo<NU>::FR, FN = Geo<NU>::FN;
 	__shared__ __align__(16) float sb[FN], sz[FN];
 	__shared__ __align__(16) uint8_t sc[FN];
 	__shared__ double sh[32];
@@ -1699,7 +1738,7 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_post5(const ProbDev *__restri
 				const int n = group_cells(gi, gj, L.w, L.h);
 				const size_t k = n ? (size_t)gj * L.w + gi : 0;
 				const size_t kc = n ? (size_t)(gj >> 1) * C.w + (gi >> 1) : 0;
-				const uint32_t cd = region_codes4(gload4u8(L.code, k, n, vec), rx, ry);
+				const uint32_t cd = region_codes4<FR>(gload4u8(L.code, k, n, vec), rx, ry);
 				clampbits |= cd;
 				float4 bv = make_float4(0.f, 0.f, 0.f, 0.f), zv = bv;
 				uint8_t cm0 = 0, cm1 = 0;
@@ -1748,15 +1787,15 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_post5(const ProbDev *__restri
 			if (am & 8u) z4[3] = z4[3] + cz.y;
 		}
 	}
-	int cells[2][4];
-	own_cells(x0, y0, cells);
-	// half-sweep s updates colour 1 - (s&1) on the cells of ring >= s + 1
+	int cells[2][Geo<NU>::KC];
+	own_cells<NU>(cells);
+	// half-sweep s updates colour 1 - (s&1) on the cells of ring >= R0 + s + 1
 	const bool plain4 = !__syncthreads_or((clampbits & CLAMP_BITS4) != 0);
-	const uint32_t ms = sweep_masks<true>(sc, cells);
+	const uint32_t ms = sweep_masks<NU, true>(sc, cells);
 	if (plain4)
-		run_sweeps<true, true>(sz, sb, sc, cells, ms);
+		run_sweeps<NU, true, true>(sz, sb, sc, cells, ms);
 	else
-		run_sweeps<true, false>(sz, sb, sc, cells, ms);
+		run_sweeps<NU, true, false>(sz, sb, sc, cells, ms);
 	// z2 of the tile and, in k_rz's order, r.z
 	FF rz = {0.f, 0.f};
 	{
@@ -1863,11 +1902,11 @@ __device__ __forceinline__ void warp_sweep5(float *z, const float *b, const uint
 // cells): the same sweeps, restriction and injection as the block-wide code,
 // synchronised with __syncwarp instead of block barriers.
 __device__ void warp_vcycle5(float *const *Z, float *const *B, const uint8_t *const *M, const int *lw,
-		const int *lh, int l0, int L)
+		const int *lh, int l0, int L, int nu)
 {
 	const int lane = threadIdx.x & 31;
 	for (int l = l0; l + 1 < L; l++) {
-		for (int s = 0; s < NU5; s++) {
+		for (int s = 0; s < nu; s++) {
 			warp_sweep5(Z[l], B[l], M[l], lw[l], lh[l], 0);
 			warp_sweep5(Z[l], B[l], M[l], lw[l], lh[l], 1);
 		}
@@ -1905,7 +1944,7 @@ __device__ void warp_vcycle5(float *const *Z, float *const *B, const uint8_t *co
 			if (M[l][c] && M[l + 1][kc]) Z[l][c] += Z[l + 1][kc];
 		}
 		__syncwarp();
-		for (int s = 0; s < NU5; s++) {
+		for (int s = 0; s < nu; s++) {
 			warp_sweep5(Z[l], B[l], M[l], lw[l], lh[l], 1);
 			warp_sweep5(Z[l], B[l], M[l], lw[l], lh[l], 0);
 		}
@@ -1920,7 +1959,7 @@ __device__ void warp_vcycle5(float *const *Z, float *const *B, const uint8_t *co
 // step first (x += alpha p, r -= alpha q in place, |r|^2 and the convergence
 // test of k_xr, summed in another order) and forms r.z and the PCG scalars.
 __global__ void __launch_bounds__(1024, 1) k_coarse5(const ProbDev *__restrict__ P, ProbState *st, Globals *gl,
-		int pcg, int use_p2, int p0)
+		int pcg, int use_p2, int p0, int nu)
 {
 	extern __shared__ __align__(16) unsigned char smem[];
 	__shared__ double sh[32];
@@ -2018,7 +2057,7 @@ __global__ void __launch_bounds__(1024, 1) k_coarse5(const ProbDev *__restrict__
 		float *z = s_Z[l], *b = s_B[l];
 		const uint8_t *m = s_M[l];
 		const int w = s_w[l], h = s_h[l];
-		for (int s = 0; s < NU5; s++) {
+		for (int s = 0; s < nu; s++) {
 			smem_sweep5(z, b, m, w, h, 0);
 			smem_sweep5(z, b, m, w, h, 1);
 		}
@@ -2042,7 +2081,7 @@ __global__ void __launch_bounds__(1024, 1) k_coarse5(const ProbDev *__restrict__
 			}
 		__syncthreads();
 	}
-	if (threadIdx.x < 32) warp_vcycle5(s_Z, s_B, s_M, s_w, s_h, ls, L);
+	if (threadIdx.x < 32) warp_vcycle5(s_Z, s_B, s_M, s_w, s_h, ls, L, nu);
 	__syncthreads();
 	// up (block-wide levels)
 	for (int l = ls - 1; l >= c0; l--) {
@@ -2057,7 +2096,7 @@ __global__ void __launch_bounds__(1024, 1) k_coarse5(const ProbDev *__restrict__
 				if (m[c] && mc[kc]) z[c] += zc[kc];
 			}
 		__syncthreads();
-		for (int s = 0; s < NU5; s++) {
+		for (int s = 0; s < nu; s++) {
 			smem_sweep5(z, b, m, w, h, 1);
 			smem_sweep5(z, b, m, w, h, 0);
 		}
@@ -2535,6 +2574,7 @@ struct Plan {
 	// states (one synchronisation); the launch count is completed then
 	const Globals *hg = nullptr;
 	int pdl = 0;   // programmatic dependent launches between the V-cycle kernels
+	int nu = NU5;  // 5-point smoothing sweeps per side of the V-cycle
 	// problem groups: contiguous problem ranges solved as concurrent branches
 	// of the solve graph, each with its own loop counters (gls[g]) and its
 	// slice of every level's active tile list (stable compaction keeps a
@@ -2672,7 +2712,7 @@ template <int K>
 void launch_vcycle(const Plan &pl, cudaStream_t s)
 {
 	constexpr int NC = K == 0 ? 2 : 5;
-	constexpr int NU = K == 0 ? NU5 : NU13;
+	const int NU = K == 0 ? pl.nu : NU13;
 	const float rscale = K == 0 ? 1.f : 2.f;
 	const int L = pl.nlev_max;
 	for (int l = 0; l + 1 < L; l++) {
@@ -2738,23 +2778,25 @@ void kt_refresh(const Plan &pl, cudaStream_t s)
 void launch_vcycle_fused(const Plan &pl, cudaStream_t s, int pcg = 1, int use_p2 = 0, int step = 0)
 {
 	kt_refresh(pl, s);
+	auto pre = pl.nu == 1 ? k_pre5<1> : pl.nu == 3 ? k_pre5<3> : k_pre5<2>;
+	auto post = pl.nu == 1 ? k_post5<1> : pl.nu == 3 ? k_post5<3> : k_post5<2>;
 	for (int l = 0; l < pl.nfine_max; l++) {
 		if (!pl.nact[l]) continue;
 		KT_BEGIN(pl, s);
-		launch_k(pl.pdl, k_pre5, pl.nact[l], SP_THREADS, 0, s, pl.dp, pl.dst, (const int4 *)pl.act[l], l,
+		launch_k(pl.pdl, pre, pl.nact[l], SP_THREADS, 0, s, pl.dp, pl.dst, (const int4 *)pl.act[l], l,
 				(const int *)pl.tbeg, (const int *)pl.tcnt, pl.partial, pl.gl, use_p2); ++*pl.nl;
 		KT_END(pl, s, "k_pre5", pl.kt->px(l) * (BPX_PRE5 + (l == 0 && step ? BPX_STEP : 0.0)));
 	}
 	{
 		KT_BEGIN(pl, s);
 		launch_k(pl.pdl, k_coarse5, pl.n, 1024, pl.coarse_smem, s, (const ProbDev *)pl.dp, pl.dst, pl.gl, pcg,
-				use_p2, pl.p0); ++*pl.nl;
+				use_p2, pl.p0, pl.nu); ++*pl.nl;
 		KT_END(pl, s, "k_coarse5", pl.kt->cells() * BPC_COARSE5);
 	}
 	for (int l = pl.nfine_max - 1; l >= 0; l--) {
 		if (!pl.nact[l]) continue;
 		KT_BEGIN(pl, s);
-		launch_k(pl.pdl, k_post5, pl.nact[l], SP_THREADS, 0, s, (const ProbDev *)pl.dp, pl.dst,
+		launch_k(pl.pdl, post, pl.nact[l], SP_THREADS, 0, s, (const ProbDev *)pl.dp, pl.dst,
 				(const int4 *)pl.act[l], l, (const int *)pl.tbeg, (const int *)pl.tcnt, pl.partial, pl.gl, pcg);
 		++*pl.nl;
 		KT_END(pl, s, "k_post5", pl.kt->px(l) * BPX_POST5);
@@ -2814,8 +2856,8 @@ std::string plan_signature(const simpois_ctx *ctx, const Plan &pl, int K, int fu
 {
 	std::string sig;
 	char buf[96];
-	snprintf(buf, sizeof buf, "%p/%d/%d/%d/%d/%d/%d/%d/%d|", (void *)ctx->arena, pl.n, K, (int)fused,
-			pl.nfine_max, pl.nlev_max, pl.coarse_smem, opt.use_mg, pl.pdl);
+	snprintf(buf, sizeof buf, "%p/%d/%d/%d/%d/%d/%d/%d/%d/%d|", (void *)ctx->arena, pl.n, K, (int)fused,
+			pl.nfine_max, pl.nlev_max, pl.coarse_smem, opt.use_mg, pl.pdl, pl.nu);
 	sig += buf;
 	const int ng = fused == MODE_FUSED5 ? pl.ngroups : 1;
 	for (int g = 0; g < ng && ng > 1; g++) {
@@ -3153,6 +3195,8 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	Plan pl;
 	pl.nl = &ctx->launches;
 	pl.n = n;
+	if (opt.nu < 0 || opt.nu > NU_MAX) return ctx_fail(ctx, SIMPOIS_EINVAL, "sweeps per side %d outside 1..%d", opt.nu, NU_MAX);
+	pl.nu = opt.nu > 0 ? opt.nu : NU5;
 	std::vector<ProbDev> hp(n);   // host image of the problem table
 	int kinds = 0;
 	Layout Lo;
@@ -3329,6 +3373,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 				if (L.w % 16 != 0) continue;
 				const int nm = l == 0 ? 3 : 2;
 				// level 0 swaps b with b_alt every PCG step, so both get a map
+				constexpr int FR = Geo<2>::FR;   // the TMA boxes of the halo-4 region
 				if (tma_map(&maps[im], L.b, L.w, L.h, 4, FR, FR) &&
 						tma_map(&maps[im + 1], L.code, L.w, L.h, 1, 64, FR) &&
 						(l != 0 || tma_map(&maps[im + 2], d.b_alt, L.w, L.h, 4, FR, FR))) {

@@ -34,6 +34,7 @@ struct MgOptions {
 	int ktimer = 0;        // time every main-loop launch with CUDA events (no graph)
 	int out_resid = 0;     // FP64 residual of the float output
 	int coarse_max = 0;    // fused V-cycle hand-over size (0: the default)
+	int nu = 0;            // 5-point smoothing sweeps per side, 1..3 (0: the default, 2)
 	int tma = 0;           // tile kernels load their regions through TMA
 	int mode = MG_FILL;
 	// MG_ADJOINT only: grad_out per problem (device), results

@@ -68,7 +68,8 @@ EXPORTS = [
     "simpois_default_params", "simpois_params_from_env", "simpois_create", "simpois_destroy",
     "simpois_strerror", "simpois_last_error", "simpois_solve", "simpois_solve_device",
     "simpois_solve_batch", "simpois_solve_batch_host", "simpois_residual_device", "simpois_residual_device_noalloc",
-    "simpois_adjoint_device", "simpois_autotune", "simpois_set_coarse_max", "simpois_set_memory_limit",
+    "simpois_adjoint_device", "simpois_autotune", "simpois_autotune_ex", "simpois_set_coarse_max",
+    "simpois_set_sweeps", "simpois_set_memory_limit",
     "simpois_amle_device", "simpois_amle", "amle",
     "simpois_launch_count", "simpois_reset_launch_count", "simpois_kernel_stats",
     "simpois_reset_kernel_stats",
@@ -119,7 +120,10 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
         L.simpois_residual_device_noalloc.argtypes = L.simpois_residual_device.argtypes
         L.simpois_adjoint_device.argtypes = [vp, vp, vp, ip, ip, ip, vp, vp, P, R]
         L.simpois_autotune.argtypes = [vp, ctypes.POINTER(Image), ip, P, R, ctypes.POINTER(ip)]
+        L.simpois_autotune_ex.argtypes = [vp, ctypes.POINTER(Image), ip, P, R, ctypes.POINTER(ip),
+                                          ctypes.POINTER(ip)]
         L.simpois_set_coarse_max.argtypes = [vp, ip]
+        L.simpois_set_sweeps.argtypes = [vp, ip]
         L.simpois_set_memory_limit.argtypes = [vp, ctypes.c_size_t]
         dp = ctypes.POINTER(ctypes.c_double)
         L.simpois_amle_device.argtypes = [vp, vp, vp, ip, ip, ip, ip, ip, vp, dp]
@@ -190,6 +194,10 @@ class Context:
     def set_coarse_max(self, coarse_max: int):
         """Fix the fused V-cycle's hand-over size (8..128; 0: tuned or default)."""
         self.check(self._lib.simpois_set_coarse_max(self.handle, int(coarse_max)))
+
+    def set_sweeps(self, sweeps: int):
+        """Fix the tile kernels' smoothing sweeps per side (1..3; 0: tuned or default)."""
+        self.check(self._lib.simpois_set_sweeps(self.handle, int(sweeps)))
 
     def set_memory_limit(self, nbytes: int):
         """Largest device arena this context may hold (0: no limit); a solve

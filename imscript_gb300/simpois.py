@@ -158,11 +158,13 @@ def solve_batch_host(images, *, rtol=1e-6, tstep=0.25, max_iter=0, flags=0, allo
 
 
 def autotune(images, *, rtol=1e-6, tstep=0.25, max_iter=0, flags=0, allow=(_lib.OK,), outs=None):
-    """``solve_batch`` that also times the fused V-cycle's hand-over sizes and
-    keeps the fastest for later batches of the same shapes on this context.
+    """``solve_batch`` that also times the fused V-cycle's launch choices --
+    the hand-over size (no bit of a result depends on it), then the smoothing
+    sweeps per side of the tile kernels (1, 2 or 3) -- and keeps the fastest
+    pair for later batches of the same shapes on this context.
 
-    Returns (outputs, reports, coarse_max); the outputs are the same bits
-    whichever hand-over is chosen."""
+    Returns (outputs, reports, {"coarse_max": .., "sweeps": ..}); the outputs
+    are those of the chosen pair."""
     return _batch(images, rtol, tstep, max_iter, flags, allow, outs, True)
 
 
@@ -195,15 +197,16 @@ def _batch(images, rtol, tstep, max_iter, flags, allow, outs, tune):
     prm = _lib.default_params(rtol=float(rtol), max_iter=int(max_iter), flags=int(flags),
                               tstep=float(tstep))
     ctx = context(dev.index or 0, _torch_stream(items[0][0]))
+    tuned = None
     if tune:
-        cm = ctypes.c_int(0)
-        rc = _lib.load().simpois_autotune(ctx.handle, arr, len(items), ctypes.byref(prm), reps,
-                                          ctypes.byref(cm))
+        cm, nu = ctypes.c_int(0), ctypes.c_int(0)
+        rc = _lib.load().simpois_autotune_ex(ctx.handle, arr, len(items), ctypes.byref(prm), reps,
+                                             ctypes.byref(cm), ctypes.byref(nu))
+        tuned = {"coarse_max": cm.value, "sweeps": nu.value}
     else:
-        cm = None
         rc = _lib.load().simpois_solve_batch(ctx.handle, arr, len(items), ctypes.byref(prm), reps)
     ctx.check(rc, allow)
-    return outs, [r.as_dict() for r in reps], (cm.value if cm is not None else None)
+    return outs, [r.as_dict() for r in reps], tuned
 
 
 def residual(u, g, f=None, kind=0):

@@ -223,18 +223,30 @@ int simpois_amle(simpois_ctx *ctx, float *out, const float *in, int w, int h,
  * knobs).  The converged 5-point V-cycle runs the levels wider than a
  * hand-over size in 32 x 32 tile kernels and the rest in one shared-memory
  * block per channel; the hand-over size (8..128) moves work between the two
- * kernels but changes no bit of any result.
- * simpois_autotune solves the batch like simpois_solve_batch while timing
- * every distinct hand-over among 32, 64 and 128 (plus the default), keeps the
- * fastest for batches of the same channel shapes and operators on this
- * context (later solves of such batches use it), and writes it to
- * *coarse_max (may be NULL; the value of the 5-point channels when the batch
- * mixes operators).  simpois_set_coarse_max fixes the hand-over for every
- * later solve on the context (0 restores tuned-or-default). */
+ * kernels but changes no bit of any result.  Each tile kernel smooths with
+ * 1, 2 or 3 red-black sweeps per side over a shared-memory region of the
+ * tile plus a halo of 4 (1 or 2 sweeps) or 8 (3 sweeps) pixels; the count
+ * is part of the preconditioner, so it changes the iterates (every result
+ * still meets its tolerance).
+ * simpois_autotune_ex solves the batch like simpois_solve_batch while timing
+ * every distinct hand-over among 32, 64 and 128 (plus the default) at 2
+ * sweeps, then 1 and 3 sweeps at the best hand-over; it keeps the fastest
+ * pair for batches of the same channel shapes and operators on this context
+ * (later solves of such batches, and their adjoints, use it), leaves the
+ * batch solved with it, and writes it to *coarse_max and *sweeps (either may
+ * be NULL; the values of the 5-point channels when the batch mixes
+ * operators).  simpois_autotune is simpois_autotune_ex without *sweeps.
+ * simpois_set_coarse_max and simpois_set_sweeps fix one choice for every
+ * later solve on the context (0 restores tuned-or-default: hand-over 64, 2
+ * sweeps); the autotuner then tunes only the other. */
+int simpois_autotune_ex(simpois_ctx *ctx, const simpois_image *images, int n,
+		const simpois_params *params, simpois_report *reports,
+		int *coarse_max, int *sweeps);
 int simpois_autotune(simpois_ctx *ctx, const simpois_image *images, int n,
 		const simpois_params *params, simpois_report *reports,
 		int *coarse_max);
 int simpois_set_coarse_max(simpois_ctx *ctx, int coarse_max);
+int simpois_set_sweeps(simpois_ctx *ctx, int sweeps);
 
 /* Device-memory budget of a context (no counterpart in the reference, whose
  * xmalloc exits on an allocation failure, simpois.c:10-19).  A solve whose

@@ -1,7 +1,10 @@
-"""The autotuner's knob, the fused V-cycle's hand-over size (levels wider than
-it run in the 32 x 32 tile kernels, the others in one shared-memory block per
-channel), moves work between kernels without changing any result bit; the
-tuner picks one of the timed candidates and later solves reuse it."""
+"""The autotuner's knobs.  The fused V-cycle's hand-over size (levels wider
+than it run in the 32 x 32 tile kernels, the others in one shared-memory block
+per channel) moves work between kernels without changing any result bit.  The
+smoothing sweeps per side (1, 2 or 3; the tile kernels' halo is 4 or 8)
+change the preconditioner: each count gives the bits of the per-sweep kernels
+with that count, and meets the FP64 direct solve within 1e-4.  The tuner
+picks one of the timed candidates and later solves reuse it."""
 import numpy as np
 import pytest
 
@@ -78,8 +81,9 @@ def test_handover_size_range_is_checked(sp):
 
 def test_autotune_picks_a_candidate_and_keeps_the_bits(sp):
     imgs = _images(5)
-    a, ra, cm = sp.autotune(imgs, rtol=1e-6)
-    assert cm in (32, 64, 128)
+    a, ra, tuned = sp.autotune(imgs, rtol=1e-6)
+    cm = tuned["coarse_max"]
+    assert cm in (32, 64, 128) and tuned["sweeps"] in (1, 2, 3)
     assert all(r["status"] == 0 and r["rel_residual"] <= 1e-6 for r in ra)
     b, rb = sp.solve_batch(imgs, rtol=1e-6)   # uses the tuned hand-over
     assert [r["iterations"] for r in ra] == [r["iterations"] for r in rb]
@@ -89,9 +93,73 @@ def test_autotune_picks_a_candidate_and_keeps_the_bits(sp):
     ctx = _ctx(sp)
     try:
         ctx.set_coarse_max(32)
-        c, rc, cm2 = sp.autotune(imgs, rtol=1e-6)
-        assert cm2 == 32
+        ctx.set_sweeps(tuned["sweeps"])
+        c, rc, t2 = sp.autotune(imgs, rtol=1e-6)
+        assert t2 == {"coarse_max": 32, "sweeps": tuned["sweeps"]}
         for x, y in zip(a, c):
             assert torch.equal(x.view(torch.int32), y.view(torch.int32))
     finally:
+        ctx.set_coarse_max(0)
+        ctx.set_sweeps(0)
+
+
+def test_sweeps_range_is_checked(sp):
+    from imscript_gb300 import lib
+    ctx = _ctx(sp)
+    with pytest.raises(lib.SimpoisError):
+        ctx.set_sweeps(4)
+    with pytest.raises(lib.SimpoisError):
+        ctx.set_sweeps(-1)
+    ctx.set_sweeps(0)
+
+
+@pytest.mark.parametrize("sweeps", [1, 2, 3])
+def test_every_sweep_count_equals_the_per_sweep_kernels(sp, sweeps):
+    """The fused tile kernels with 1, 2 or 3 sweeps per side compute what the
+    one-launch-per-sweep kernels with that count compute, bit for bit (widths
+    that are and are not multiples of 4, small and large images)."""
+    from imscript_gb300 import lib
+    imgs = _images(23)
+    ctx = _ctx(sp)
+    try:
+        ctx.set_sweeps(sweeps)
+        a, ra = sp.solve_batch(imgs, rtol=1e-6)
+        b, rb = sp.solve_batch(imgs, rtol=1e-6, flags=lib.FLAG_UNFUSED)
+    finally:
+        ctx.set_sweeps(0)
+    assert [r["iterations"] for r in ra] == [r["iterations"] for r in rb]
+    assert all(r["status"] == 0 and r["rel_residual"] <= 1e-6 for r in ra)
+    for x, y in zip(a, b):
+        assert torch.equal(x.view(torch.int32), y.view(torch.int32))
+
+
+@pytest.mark.parametrize("sweeps", [1, 2, 3])
+def test_every_candidate_meets_the_fp64_solve(sp, sweeps):
+    """Every (hand-over, sweeps) candidate of the autotuner on uneven
+    instances of the batched workload and a guided Poisson image: within 1e-4
+    of the FP64 direct solve at rtol 1e-6."""
+    from imscript_gb300 import synth
+    from oracle import fp64
+    insts = synth.config3(seed=7, n=12, smax=512) + [synth.config1(seed=3, size=384, channels=1)]
+    ctx = _ctx(sp)
+    try:
+        ctx.set_sweeps(sweeps)
+        for cm in (32, 64, 128):
+            ctx.set_coarse_max(cm)
+            outs, reps = sp.solve_batch([(_cuda(i.g), None if i.f is None else _cuda(i.f), i.tstep)
+                                         for i in insts], rtol=1e-6)
+            assert all(r["status"] == 0 and r["rel_residual"] <= 1e-6 for r in reps)
+            if cm != 64:
+                continue   # the hand-over changes no bit: one FP64 comparison per sweep count
+            for inst, o in zip(insts, outs):
+                o = o.cpu().numpy()
+                for l in range(inst.g.shape[0]):
+                    m = np.isnan(inst.g[l])
+                    if not m.any():
+                        continue
+                    x = fp64.solve(inst.g[l], None if inst.f is None else inst.f[l], 0)
+                    err = np.abs(o[l][m] - x[m]).max() / np.abs(x[m]).max()
+                    assert err <= 1e-4, (sweeps, inst.meta, err)
+    finally:
+        ctx.set_sweeps(0)
         ctx.set_coarse_max(0)
