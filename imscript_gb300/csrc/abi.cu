@@ -483,6 +483,38 @@ __global__ void k_put_unknowns(const float4 *__restrict__ g, const float4 *__res
 	}
 }
 
+// The same two passes over every image of a batch, one launch each: image
+// blockIdx.y, groups strided over blockIdx.x.  fetch: dst = src at the groups
+// of g holding an unknown (0 elsewhere), src a page-locked host buffer; put:
+// dst (host) = src at those groups.
+struct IoImg {
+	const float4 *g;     // the image on the device
+	const float4 *src;
+	float4 *dst;
+	size_t n4;           // 4-pixel groups
+};
+
+__global__ void k_fetch_rhs_batch(const IoImg *__restrict__ im)
+{
+	const IoImg m = im[blockIdx.y];
+	if (!m.src) return;   // no data term, or whole-buffer copies
+	for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < m.n4; i += (size_t)gridDim.x * blockDim.x) {
+		const float4 v = m.g[i];
+		const bool u = isnan(v.x) || isnan(v.y) || isnan(v.z) || isnan(v.w);
+		m.dst[i] = u ? m.src[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+	}
+}
+
+__global__ void k_put_unknowns_batch(const IoImg *__restrict__ im)
+{
+	const IoImg m = im[blockIdx.y];
+	if (!m.dst) return;   // an image that took whole-buffer copies
+	for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < m.n4; i += (size_t)gridDim.x * blockDim.x) {
+		const float4 v = m.g[i];
+		if (isnan(v.x) || isnan(v.y) || isnan(v.z) || isnan(v.w)) m.dst[i] = m.src[i];
+	}
+}
+
 // The device address of a page-locked host buffer, 16-byte aligned; null for
 // any other buffer.
 static void *direct_ptr(const void *p)
@@ -505,6 +537,17 @@ static bool direct_io_enabled()
 		return !(e && atoi(e) > 0);
 	}();
 	return v;
+}
+
+// The second stream of the host entry points and its events (created once).
+static int ensure_aux(simpois_ctx *ctx)
+{
+	if (ctx->aux_stream) return SIMPOIS_OK;
+	SP_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking));
+	SP_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_in, cudaEventDisableTiming));
+	SP_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_out, cudaEventDisableTiming));
+	SP_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_rhs, cudaEventDisableTiming));
+	return SIMPOIS_OK;
 }
 
 int simpois_solve(simpois_ctx *ctx, float *out, const float *in, const float *dat, int w, int h, int pd,
@@ -531,12 +574,7 @@ int simpois_solve(simpois_ctx *ctx, float *out, const float *in, const float *da
 		if (dat && !hdat) hout = nullptr;
 	}
 	const bool direct = hout != nullptr;
-	if (direct && !ctx->aux_stream) {
-		SP_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking));
-		SP_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_in, cudaEventDisableTiming));
-		SP_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_out, cudaEventDisableTiming));
-		SP_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_rhs, cudaEventDisableTiming));
-	}
+	if (direct && (rc = ensure_aux(ctx))) return rc;
 	const int grid = 8 * (ctx->sm_count > 0 ? ctx->sm_count : 1);
 	SP_CUDA(ctx, cudaMemcpyAsync(din, in, bytes, cudaMemcpyHostToDevice, s));
 	if (direct) {
@@ -644,43 +682,120 @@ int simpois_solve_batch_host(simpois_ctx *ctx, const simpois_image *images, int 
 {
 	if (!ctx || (!images && n > 0) || n < 0) return ctx_fail(ctx, SIMPOIS_EINVAL, "bad batch");
 	if (cudaSetDevice(ctx->device) != cudaSuccess) return ctx_fail(ctx, SIMPOIS_ECUDA, "cudaSetDevice");
-	// device slots of every image's in, dat and out, one after the other
+	simpois_params p;
+	if (params) p = *params; else simpois_default_params(&p);
+	// device slots of every image's in, dat and out, one after the other, then
+	// the tables of the direct passes
 	std::vector<size_t> off(3 * (size_t)n);
 	size_t total = 0;
+	// direct I/O per image (as simpois_solve): converged, its size a multiple
+	// of 4, out and dat page-locked and 16-byte aligned; the other images take
+	// whole-buffer copies
+	const bool may_direct = direct_io_enabled() && n <= 65535;
+	std::vector<char> dir(n, 0);
+	std::vector<IoImg> fetch(n), put(n);
+	int ndir = 0;
+	bool any_fetch = false;
 	for (int k = 0; k < n; k++) {
 		const simpois_image &im = images[k];
 		if (!im.in || !im.out) return ctx_fail(ctx, SIMPOIS_EINVAL, "image %d: null buffer", k);
 		int rc = check_dims(ctx, im.w, im.h, im.pd);
 		if (rc) return rc;
-		const size_t slot = ((size_t)im.w * im.h * im.pd * sizeof(float) + 255) / 256 * 256;
+		const size_t np = (size_t)im.w * im.h * im.pd, slot = (np * sizeof(float) + 255) / 256 * 256;
 		off[3 * k] = total;
 		total += slot;
 		off[3 * k + 1] = total;
 		total += im.dat ? slot : 0;
 		off[3 * k + 2] = total;
 		total += slot;
+		if (may_direct && (im.rtol > 0 || p.rtol > 0) && np % 4 == 0) {
+			const float4 *hd = im.dat ? (const float4 *)direct_ptr(im.dat) : nullptr;
+			float4 *ho = (float4 *)direct_ptr(im.out);
+			if (ho && (!im.dat || hd)) {
+				dir[k] = 1;
+				ndir++;
+				fetch[k].src = hd;
+				any_fetch = any_fetch || hd;
+				put[k].dst = ho;
+			}
+		}
 	}
+	const size_t o_tab = total;
+	total += ndir ? 2 * sizeof(IoImg) * (size_t)n : 0;
 	int rc = ctx_io_reserve(ctx, total > 0 ? total : 256);
 	if (rc) return rc;
 	cudaStream_t s = ctx->stream;
 	std::vector<simpois_image> dev(images, images + n);
+	size_t n4max = 0;
 	for (int k = 0; k < n; k++) {
 		const size_t bytes = (size_t)images[k].w * images[k].h * images[k].pd * sizeof(float);
 		dev[k].in = (const float *)(ctx->io + off[3 * k]);
 		dev[k].dat = images[k].dat ? (const float *)(ctx->io + off[3 * k + 1]) : nullptr;
 		dev[k].out = (float *)(ctx->io + off[3 * k + 2]);
 		SP_CUDA(ctx, cudaMemcpyAsync((void *)dev[k].in, images[k].in, bytes, cudaMemcpyHostToDevice, s));
-		if (images[k].dat)
+		if (images[k].dat && !dir[k])
 			SP_CUDA(ctx, cudaMemcpyAsync((void *)dev[k].dat, images[k].dat, bytes, cudaMemcpyHostToDevice, s));
+		if (dir[k]) {
+			fetch[k].g = put[k].g = (const float4 *)dev[k].in;
+			fetch[k].dst = (float4 *)dev[k].dat;
+			put[k].src = (const float4 *)dev[k].out;
+			fetch[k].n4 = put[k].n4 = bytes / 16;
+			n4max = std::max(n4max, bytes / 16);
+		}
+	}
+	const unsigned gx = (unsigned)std::max<size_t>(1, std::min<size_t>(8, (n4max + 255) / 256));
+	IoImg *dput = nullptr;
+	if (ndir) {
+		if ((rc = ensure_aux(ctx))) return rc;
+		IoImg *dfetch = (IoImg *)(ctx->io + o_tab);
+		dput = dfetch + n;
+		// pageable sources: the copies are staged before the calls return
+		SP_CUDA(ctx, cudaMemcpyAsync(dfetch, fetch.data(), sizeof(IoImg) * n, cudaMemcpyHostToDevice, s));
+		SP_CUDA(ctx, cudaMemcpyAsync(dput, put.data(), sizeof(IoImg) * n, cudaMemcpyHostToDevice, s));
+		// on the second stream, once the inputs are in: the direct images' data
+		// terms at the groups that hold an unknown (overlapping the solve's
+		// setup, which does not read them), then their outputs' known pixels --
+		// those of the inputs -- while the solve runs
+		SP_CUDA(ctx, cudaEventRecord(ctx->ev_in, s));
+		SP_CUDA(ctx, cudaStreamWaitEvent(ctx->aux_stream, ctx->ev_in, 0));
+		if (any_fetch) {
+			k_fetch_rhs_batch<<<dim3(gx, n), 256, 0, ctx->aux_stream>>>(dfetch);
+			ctx->launches++;
+			const cudaError_t e = cudaGetLastError();
+			if (e != cudaSuccess) {
+				cudaStreamSynchronize(ctx->aux_stream);
+				return ctx_fail(ctx, SIMPOIS_ECUDA, "k_fetch_rhs_batch: %s", cudaGetErrorString(e));
+			}
+			SP_CUDA(ctx, cudaEventRecord(ctx->ev_rhs, ctx->aux_stream));
+			ctx->rhs_pending = ctx->ev_rhs;
+		}
+		for (int k = 0; k < n; k++) {
+			if (!dir[k]) continue;
+			const size_t bytes = (size_t)images[k].w * images[k].h * images[k].pd * sizeof(float);
+			SP_CUDA(ctx, cudaMemcpyAsync(images[k].out, dev[k].in, bytes, cudaMemcpyDeviceToHost, ctx->aux_stream));
+		}
+		SP_CUDA(ctx, cudaEventRecord(ctx->ev_out, ctx->aux_stream));
 	}
 	const int st = solve_batch(ctx, dev.data(), n, params, reports, 0, nullptr);
+	if (ctx->rhs_pending) {   // a solve that stopped before its loops
+		cudaStreamWaitEvent(s, ctx->rhs_pending, 0);
+		ctx->rhs_pending = nullptr;
+	}
 	if (st != SIMPOIS_OK && st != SIMPOIS_NOT_CONVERGED && st != SIMPOIS_BREAKDOWN) {
+		if (ndir) cudaStreamSynchronize(ctx->aux_stream);   // the caller may free out
 		cudaStreamSynchronize(s);
 		return st;
 	}
 	for (int k = 0; k < n; k++) {
+		if (dir[k]) continue;
 		const size_t bytes = (size_t)images[k].w * images[k].h * images[k].pd * sizeof(float);
 		SP_CUDA(ctx, cudaMemcpyAsync(images[k].out, dev[k].out, bytes, cudaMemcpyDeviceToHost, s));
+	}
+	if (ndir) {
+		SP_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_out, 0));
+		k_put_unknowns_batch<<<dim3(gx, n), 256, 0, s>>>(dput);
+		ctx->launches++;
+		SP_CUDA(ctx, cudaGetLastError());
 	}
 	SP_CUDA(ctx, cudaStreamSynchronize(s));
 	return st;

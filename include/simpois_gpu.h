@@ -160,7 +160,10 @@ int simpois_solve_batch(simpois_ctx *ctx, const simpois_image *images, int n,
  * batched form of poisson_solver_separable, simpois.c:288-302, over many
  * images): the inputs go to the device, the batch is solved, the outputs come
  * back; the call returns when they are written.  Page-locked buffers move at
- * the link's full rate. */
+ * the link's full rate; with rtol > 0 an image whose w*h*pd is a multiple of
+ * 4 and whose out and dat are page-locked and 16-byte aligned moves as in
+ * simpois_solve: dat only in the 4-pixel groups holding an unknown, out back
+ * whole while the solve runs, then its groups holding an unknown. */
 int simpois_solve_batch_host(simpois_ctx *ctx, const simpois_image *images,
 		int n, const simpois_params *params, simpois_report *reports);
 
