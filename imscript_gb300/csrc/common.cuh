@@ -200,7 +200,10 @@ __device__ __forceinline__ FF ff_add(FF a, FF b)
 }
 
 // Block sum of float-float values (thread 0 gets the result): float-float
-// across each warp, the warps' sums in double.
+// across each warp and across the warps, on the FP32 pipe, and one conversion
+// to double at the end.  (An FP64 instruction holds this GPU's FP64 pipe for
+// tens of cycles: a double per warp made the reductions of the tile kernels
+// occupy up to 30 % of it.)
 template <int NT>
 __device__ __forceinline__ double block_sum_ff(FF v, double *sh)
 {
@@ -212,12 +215,15 @@ __device__ __forceinline__ double block_sum_ff(FF v, double *sh)
 		w.lo = __shfl_down_sync(0xffffffffu, v.lo, o);
 		v = ff_add(v, w);
 	}
-	if (lane == 0) sh[warp] = (double)v.hi + (double)v.lo;
+	float2 *shf = reinterpret_cast<float2 *>(sh);   // NT / 32 <= 32 pairs
+	if (lane == 0) shf[warp] = make_float2(v.hi, v.lo);
 	__syncthreads();
 	double r = 0;
 	if (threadIdx.x == 0) {
+		FF a = {shf[0].x, shf[0].y};
 #pragma unroll
-		for (int k = 0; k < NT / 32; k++) r += sh[k];
+		for (int k = 1; k < NT / 32; k++) a = ff_add(a, FF{shf[k].x, shf[k].y});
+		r = (double)a.hi + (double)a.lo;
 	}
 	__syncthreads();
 	return r;

@@ -129,6 +129,7 @@ struct ProbDev {
 
 struct ProbState {
 	double bnorm2, rho, alpha, beta, rr, tau2, rel, rel_first;
+	float alpha_f, beta_f;   // (float)alpha and (float)beta, rounded once where they are set
 	double cross;   // FP64 biharmonic PCG: r_new . z_old (flexible beta)
 	int iter, total_iter, outer, inner_active, outer_active, status;
 	int pending;    // fused 5-point PCG: alpha is set, x and r await their update
@@ -765,6 +766,7 @@ __global__ void k_resid64(const ProbDev *__restrict__ P, ProbState *st, const in
 			s.tau2 = tau * tau * tot[0];
 			s.rho = 0;
 			s.beta = 0;
+			s.beta_f = (float)s.beta;
 			s.pending = 0;
 			atomicAdd(&gl->inner_count, 1);
 		}
@@ -836,7 +838,7 @@ __global__ void k_pupdate(const ProbDev *__restrict__ P, const ProbState *__rest
 	int4 t = tl[blockIdx.x];
 	if (!st[t.x].inner_active) return;
 	const ProbDev &pr = P[t.x];
-	const float beta = (float)st[t.x].beta;
+	const float beta = st[t.x].beta_f;
 	int i = tile_i(t);
 	for (int r = 0; r < SP_ROWS; r++) {
 		int j = tile_j(t, r);
@@ -907,9 +909,11 @@ __global__ void k_spmv(const ProbDev *__restrict__ P, ProbState *st, const int4 
 			s.status = SIMPOIS_BREAKDOWN;
 			s.inner_active = 0;
 			s.alpha = 0;
+			s.alpha_f = (float)s.alpha;
 			atomicSub(&gl->inner_count, 1);
 		} else {
 			s.alpha = a;
+			s.alpha_f = (float)s.alpha;
 		}
 	}
 }
@@ -925,7 +929,7 @@ __global__ void __launch_bounds__(SP_THREADS) k_xr(const ProbDev *__restrict__ P
 	if (!st[prob].inner_active) return;
 	const ProbDev &pr = P[prob];
 	const LevelDev &L = pr.lv[0];
-	const float a = (float)st[prob].alpha;
+	const float a = st[prob].alpha_f;
 	const float *pv = use_p2 ? pr.p2 : pr.p;
 	FF rr = {0.f, 0.f};
 	const Grp g = grp_of(t, pr.w, pr.h);
@@ -997,6 +1001,7 @@ __global__ void k_rz(const ProbDev *__restrict__ P, ProbState *st, const int4 *_
 			atomicSub(&gl->inner_count, 1);
 		} else {
 			s.beta = s.rho > 0 ? tot[0] / s.rho : 0.0;
+			s.beta_f = (float)s.beta;
 			s.rho = tot[0];
 		}
 	}
@@ -1540,9 +1545,9 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 	grid_wait();
 	grid_release();
 	const int active = st[prob].inner_active, pending = st[prob].pending;
-	const double alpha = st[prob].alpha;
+	const float alpha_f = st[prob].alpha_f;
 	const bool upd = l == 0 && pending;
-	const float a = upd ? (float)alpha : 0.f;
+	const float a = upd ? alpha_f : 0.f;
 	const float *qv = pr.q;
 	// b (and at level 0 q) of the region: issued with the state's loads, before
 	// the early-return test, so that one round trip follows the wait
@@ -1818,6 +1823,7 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_post5(const ProbDev *__restri
 			atomicSub(&gl->inner_count, 1);
 		} else {
 			s.beta = s.rho > 0 ? tot[0] / s.rho : 0.0;
+			s.beta_f = (float)s.beta;
 			s.rho = tot[0];
 		}
 	}
@@ -1976,7 +1982,7 @@ __global__ void __launch_bounds__(1024, 1) k_coarse5(const ProbDev *__restrict__
 	const ProbDev &pr = P[prob];
 	const int c0 = pr.nfine, L = pr.nlev;
 	const bool upd = c0 == 0 && pcg && st[prob].pending;
-	const float a = upd ? (float)st[prob].alpha : 0.f;
+	const float a = upd ? st[prob].alpha_f : 0.f;
 	const float *pv = use_p2 ? pr.p2 : pr.p;
 	FF rr = {0.f, 0.f};
 	if (threadIdx.x < L) {
@@ -2119,6 +2125,7 @@ __global__ void __launch_bounds__(1024, 1) k_coarse5(const ProbDev *__restrict__
 			atomicSub(&gl->inner_count, 1);
 		} else {
 			s.beta = s.rho > 0 ? rz / s.rho : 0.0;
+			s.beta_f = (float)s.beta;
 			s.rho = rz;
 		}
 	}
@@ -2171,7 +2178,7 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_spmv5(const ProbDev *__restri
 	grid_wait();
 	grid_release();
 	const int active = st[prob].inner_active;
-	const double beta64 = st[prob].beta;
+	const float beta = st[prob].beta_f;
 	// z2 of the region, issued with the state's loads
 	float4 zr[NV];
 #pragma unroll
@@ -2185,7 +2192,6 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_spmv5(const ProbDev *__restri
 		}
 	}
 	if (!active) return;
-	const float beta = (float)beta64;
 #pragma unroll
 	for (int it = 0; it < NV; it++) {
 		const int f = threadIdx.x + it * SP_THREADS;
@@ -2234,9 +2240,11 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_spmv5(const ProbDev *__restri
 			s.status = SIMPOIS_BREAKDOWN;
 			s.inner_active = 0;
 			s.alpha = 0;
+			s.alpha_f = (float)s.alpha;
 			atomicSub(&gl->inner_count, 1);
 		} else {
 			s.alpha = a;
+			s.alpha_f = (float)s.alpha;
 			s.pending = 1;   // k_pre5 (or k_coarse5) at level 0 takes the step
 		}
 	}
@@ -2308,6 +2316,7 @@ __global__ void k_rz64(const ProbDev *__restrict__ P, ProbState *st, const int4 
 			// form keeps the FP64 recurrence converging where the classical
 			// r.z / rho_old stalls (small images with holes at the border)
 			s.beta = s.rho > 0 ? (tot[0] - s.cross) / s.rho : 0.0;
+			s.beta_f = (float)s.beta;
 			s.rho = tot[0];
 		}
 	}
@@ -2368,9 +2377,11 @@ __global__ void k_spmv64(const ProbDev *__restrict__ P, ProbState *st, const int
 			s.status = SIMPOIS_BREAKDOWN;
 			s.inner_active = 0;
 			s.alpha = 0;
+			s.alpha_f = (float)s.alpha;
 			atomicSub(&gl->inner_count, 1);
 		} else {
 			s.alpha = a;
+			s.alpha_f = (float)s.alpha;
 		}
 	}
 }
