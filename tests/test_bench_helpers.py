@@ -10,13 +10,13 @@ if ROOT not in sys.path:
 
 def test_roofline_traffic_comes_from_the_committed_summaries():
     import bench
-    for kernel, workload in (("k_pre5", "poisson_guided_2048x2048x3"), ("k_post5", "poisson_guided_2048x2048x3"),
-                             ("k_spmv5", "poisson_guided_2048x2048x3"), ("k_amle_fused", "amle_2048x2048x1")):
+    for kernel, workload in (("k_pre5", "batched_256_uneven"), ("k_post5", "batched_256_uneven"),
+                             ("k_spmv5", "batched_256_uneven"), ("k_amle_fused", "amle_2048x2048x1")):
         t = bench.ncu_traffic(kernel, workload)
         assert t is not None, kernel
         assert t["traffic"] > 1e6, (kernel, t)
         assert t["traffic_source"].startswith(f"profiles/{kernel}_{workload}.md")
-    t = bench.ncu_traffic("k_pre5", "poisson_guided_2048x2048x3")
+    t = bench.ncu_traffic("k_pre5", bench.PROFILE_NAMES["c3"])
     assert t["traffic_algorithmic"] and 0.3 < t["traffic"] / t["traffic_algorithmic"] < 3
     assert bench.ncu_traffic("no_such_kernel", "nowhere") is None
 
