@@ -2996,10 +2996,23 @@ cudaError_t build_solve_graph(simpois_ctx *ctx, Plan &pl, const MgOptions &opt, 
 		}
 	}
 	if (e == cudaSuccess) {
+		// a graph of the same topology as the cached one (a new mask of the
+		// same sizes usually changes only grid sizes and slices) updates it in
+		// place, which costs a fraction of an instantiation; else a new one
+		bool updated = false;
+		if (ctx->solve_exec && ctx->solve_groups == ng) {
+			cudaGraphExecUpdateResultInfo info;
+			if (cudaGraphExecUpdate(ctx->solve_exec, G, &info) == cudaSuccess)
+				updated = true;
+			else
+				cudaGetLastError();
+		}
 		cudaGraphExec_t ex = nullptr;
-		if ((e = cudaGraphInstantiate(&ex, G, 0)) == cudaSuccess) {
+		if (!updated && (e = cudaGraphInstantiate(&ex, G, 0)) == cudaSuccess) {
 			if (ctx->solve_exec) cudaGraphExecDestroy(ctx->solve_exec);
 			ctx->solve_exec = ex;
+		}
+		if (e == cudaSuccess) {
 			ctx->solve_groups = ng;
 			for (int g = 0; g < ng; g++) {
 				ctx->solve_nodes_outer[g] = no[g];

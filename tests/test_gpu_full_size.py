@@ -94,3 +94,19 @@ def test_batch_of_256_uneven_instances(fp64):
         one, _ = simpois.solve(_dev(inst.g), _dev(inst.f), tstep=inst.tstep, rtol=1e-6)
         assert np.array_equal(one.cpu().numpy().view(np.uint32), o.view(np.uint32)), n
     assert k == len(reps)
+
+
+def test_new_masks_of_the_same_size_give_the_bits_of_fresh_contexts():
+    """One context solving images of one size with different masks in turn
+    (its solve graph is updated or rebuilt for each) gives the bits a fresh
+    context gives each image."""
+    import torch
+    insts = [synth.config1(seed=s, size=300, channels=2, rtol=1e-6) for s in (11, 12, 13)]
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):   # a context of its own
+        seq = [simpois.solve(_dev(i.g), _dev(i.f), rtol=1e-6)[0].cpu().numpy() for i in insts + insts[:1]]
+    for k, inst in enumerate(insts + insts[:1]):
+        s2 = torch.cuda.Stream()
+        with torch.cuda.stream(s2):   # a fresh context per image
+            fresh = simpois.solve(_dev(inst.g), _dev(inst.f), rtol=1e-6)[0].cpu().numpy()
+        assert np.array_equal(fresh.view(np.uint32), seq[k].view(np.uint32)), k
