@@ -743,7 +743,10 @@ int simpois_solve_batch_host(simpois_ctx *ctx, const simpois_image *images, int 
 			n4max = std::max(n4max, bytes / 16);
 		}
 	}
-	const unsigned gx = (unsigned)std::max<size_t>(1, std::min<size_t>(8, (n4max + 255) / 256));
+	// blocks per image: about 8 per SM over the whole batch, at most one per
+	// 256 groups of the largest image
+	const size_t per_img = (size_t)std::max(1, 8 * std::max(1, ctx->sm_count) / std::max(1, n));
+	const unsigned gx = (unsigned)std::max<size_t>(1, std::min<size_t>(per_img, (n4max + 255) / 256));
 	IoImg *dput = nullptr;
 	if (ndir) {
 		if ((rc = ensure_aux(ctx))) return rc;
