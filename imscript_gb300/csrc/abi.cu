@@ -483,33 +483,51 @@ __global__ void k_put_unknowns(const float4 *__restrict__ g, const float4 *__res
 	}
 }
 
-// The same two passes over every image of a batch, one launch each: image
-// blockIdx.y, groups strided over blockIdx.x.  fetch: dst = src at the groups
-// of g holding an unknown (0 elsewhere), src a page-locked host buffer; put:
-// dst (host) = src at those groups.
+// The same two passes over every image of a batch, one launch each, the
+// blocks shared out by size: image k takes blocks blk0 .. blk0 + ceil(n4 / ch)
+// - 1 (blk0 ascending; an image with no groups takes none), block b of it the
+// groups (b - blk0) ch .. + ch - 1.  fetch: dst = src at the groups of g
+// holding an unknown (0 elsewhere), src a page-locked host buffer; put: dst
+// (host) = src at those groups.
 struct IoImg {
 	const float4 *g;     // the image on the device
 	const float4 *src;
 	float4 *dst;
 	size_t n4;           // 4-pixel groups
+	unsigned blk0;       // first block
 };
 
-__global__ void k_fetch_rhs_batch(const IoImg *__restrict__ im)
+// The image of block blockIdx.x: the last one whose first block is at or
+// below it (images without blocks share the next one's blk0).
+__device__ __forceinline__ const IoImg &io_image(const IoImg *__restrict__ im, int n)
 {
-	const IoImg m = im[blockIdx.y];
+	int lo = 0, hi = n - 1;
+	while (lo < hi) {
+		const int mid = (lo + hi + 1) >> 1;
+		if (im[mid].blk0 <= blockIdx.x) lo = mid;
+		else hi = mid - 1;
+	}
+	return im[lo];
+}
+
+__global__ void k_fetch_rhs_batch(const IoImg *__restrict__ im, int n, unsigned ch)
+{
+	const IoImg &m = io_image(im, n);
 	if (!m.src) return;   // no data term, or whole-buffer copies
-	for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < m.n4; i += (size_t)gridDim.x * blockDim.x) {
+	const size_t beg = (size_t)(blockIdx.x - m.blk0) * ch, end = min(beg + ch, m.n4);
+	for (size_t i = beg + threadIdx.x; i < end; i += blockDim.x) {
 		const float4 v = m.g[i];
 		const bool u = isnan(v.x) || isnan(v.y) || isnan(v.z) || isnan(v.w);
 		m.dst[i] = u ? m.src[i] : make_float4(0.f, 0.f, 0.f, 0.f);
 	}
 }
 
-__global__ void k_put_unknowns_batch(const IoImg *__restrict__ im)
+__global__ void k_put_unknowns_batch(const IoImg *__restrict__ im, int n, unsigned ch)
 {
-	const IoImg m = im[blockIdx.y];
+	const IoImg &m = io_image(im, n);
 	if (!m.dst) return;   // an image that took whole-buffer copies
-	for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < m.n4; i += (size_t)gridDim.x * blockDim.x) {
+	const size_t beg = (size_t)(blockIdx.x - m.blk0) * ch, end = min(beg + ch, m.n4);
+	for (size_t i = beg + threadIdx.x; i < end; i += blockDim.x) {
 		const float4 v = m.g[i];
 		if (isnan(v.x) || isnan(v.y) || isnan(v.z) || isnan(v.w)) m.dst[i] = m.src[i];
 	}
@@ -726,7 +744,7 @@ int simpois_solve_batch_host(simpois_ctx *ctx, const simpois_image *images, int 
 	if (rc) return rc;
 	cudaStream_t s = ctx->stream;
 	std::vector<simpois_image> dev(images, images + n);
-	size_t n4max = 0;
+	size_t n4tot = 0;
 	for (int k = 0; k < n; k++) {
 		const size_t bytes = (size_t)images[k].w * images[k].h * images[k].pd * sizeof(float);
 		dev[k].in = (const float *)(ctx->io + off[3 * k]);
@@ -740,13 +758,19 @@ int simpois_solve_batch_host(simpois_ctx *ctx, const simpois_image *images, int 
 			fetch[k].dst = (float4 *)dev[k].dat;
 			put[k].src = (const float4 *)dev[k].out;
 			fetch[k].n4 = put[k].n4 = bytes / 16;
-			n4max = std::max(n4max, bytes / 16);
+			n4tot += bytes / 16;
 		}
 	}
-	// blocks per image: about 8 per SM over the whole batch, at most one per
-	// 256 groups of the largest image
-	const size_t per_img = (size_t)std::max(1, 8 * std::max(1, ctx->sm_count) / std::max(1, n));
-	const unsigned gx = (unsigned)std::max<size_t>(1, std::min<size_t>(per_img, (n4max + 255) / 256));
+	// blocks shared out by size: chunks of ch groups (a multiple of 1024, so
+	// that each of the 256 threads takes 4 or more), about 32 blocks per SM
+	// over the whole batch (at most 65535 images: nblk stays far below 2^31)
+	const size_t target = 32 * (size_t)std::max(1, ctx->sm_count);
+	const size_t ch = std::max<size_t>(1024, (n4tot / target + 1023) / 1024 * 1024);
+	size_t nblk = 0;
+	for (int k = 0; k < n; k++) {
+		fetch[k].blk0 = put[k].blk0 = (unsigned)nblk;
+		nblk += (fetch[k].n4 + ch - 1) / ch;
+	}
 	IoImg *dput = nullptr;
 	if (ndir) {
 		if ((rc = ensure_aux(ctx))) return rc;
@@ -762,7 +786,7 @@ int simpois_solve_batch_host(simpois_ctx *ctx, const simpois_image *images, int 
 		SP_CUDA(ctx, cudaEventRecord(ctx->ev_in, s));
 		SP_CUDA(ctx, cudaStreamWaitEvent(ctx->aux_stream, ctx->ev_in, 0));
 		if (any_fetch) {
-			k_fetch_rhs_batch<<<dim3(gx, n), 256, 0, ctx->aux_stream>>>(dfetch);
+			k_fetch_rhs_batch<<<(unsigned)nblk, 256, 0, ctx->aux_stream>>>(dfetch, n, (unsigned)ch);
 			ctx->launches++;
 			const cudaError_t e = cudaGetLastError();
 			if (e != cudaSuccess) {
@@ -796,7 +820,7 @@ int simpois_solve_batch_host(simpois_ctx *ctx, const simpois_image *images, int 
 	}
 	if (ndir) {
 		SP_CUDA(ctx, cudaStreamWaitEvent(s, ctx->ev_out, 0));
-		k_put_unknowns_batch<<<dim3(gx, n), 256, 0, s>>>(dput);
+		k_put_unknowns_batch<<<(unsigned)nblk, 256, 0, s>>>(dput, n, (unsigned)ch);
 		ctx->launches++;
 		SP_CUDA(ctx, cudaGetLastError());
 	}
