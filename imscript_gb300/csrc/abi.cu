@@ -7,7 +7,10 @@
 #include <string.h>
 
 #include <algorithm>
+#include <map>
 #include <mutex>
+#include <stdio.h>
+#include <unistd.h>
 
 #include "common.cuh"
 #include "solvers.h"
@@ -234,6 +237,87 @@ int tune_and_solve(simpois_ctx *ctx, const std::vector<MgProblem> &sub, MgOption
 	return SIMPOIS_OK;
 }
 
+// ---------------------------------------------------------------- tuning file
+// The autotuner's choices kept on disk, per device model: a text file
+//
+//   simpois-tune 1
+//   device <compute capability> <SMs> <device name>
+//   <hand-over> <sweeps> <batch-shape key>
+//   ...
+//
+// A file written on another device model is read as empty (its timings do not
+// carry over); a file whose first line is not the header, or with a malformed
+// choice line, is an error.  Saving merges the file's current choices with the
+// context's (the context's win) and replaces the file through a temporary one
+// in the same directory, so concurrent writers lose at most each other's new
+// entries, never the file.
+static std::string device_line(const simpois_ctx *ctx)
+{
+	cudaDeviceProp pr;
+	if (cudaGetDeviceProperties(&pr, ctx->device) != cudaSuccess) {
+		cudaGetLastError();
+		return "device unknown";
+	}
+	char buf[400];
+	snprintf(buf, sizeof buf, "device %d.%d %d %s", pr.major, pr.minor, pr.multiProcessorCount, pr.name);
+	return buf;
+}
+
+// Read the choices of `path` written for this device into `out`.  Returns
+// SIMPOIS_OK (also for a missing file or another device's file).
+static int tune_read(simpois_ctx *ctx, const std::string &path, std::map<std::string, simpois_ctx::Tuned> &out)
+{
+	FILE *f = fopen(path.c_str(), "r");
+	if (!f) return SIMPOIS_OK;
+	std::string line;
+	auto getline = [&](std::string &l) -> bool {
+		l.clear();
+		int c;
+		while ((c = fgetc(f)) != EOF && c != '\n') l.push_back((char)c);
+		return c != EOF || !l.empty();
+	};
+	int rc = SIMPOIS_OK;
+	if (!getline(line) || line != "simpois-tune 1") {
+		rc = ctx_fail(ctx, SIMPOIS_EINVAL, "%s: not a tuning file", path.c_str());
+	} else if (getline(line) && line == device_line(ctx)) {
+		int ln = 2;
+		while (getline(line)) {
+			ln++;
+			if (line.empty()) continue;
+			int cm = 0, nu = 0, used = 0;
+			if (sscanf(line.c_str(), "%d %d %n", &cm, &nu, &used) != 2 || used <= 0 ||
+					(size_t)used >= line.size() || cm < 8 || cm > 128 || nu < 1 || nu > 3) {
+				rc = ctx_fail(ctx, SIMPOIS_EINVAL, "%s:%d: malformed choice", path.c_str(), ln);
+				break;
+			}
+			out[line.substr(used)] = {cm, nu};
+		}
+	}
+	fclose(f);
+	return rc;
+}
+
+static int tune_write(simpois_ctx *ctx)
+{
+	std::map<std::string, simpois_ctx::Tuned> all;
+	tune_read(ctx, ctx->tune_path, all);   // a broken file is replaced
+	for (const auto &kv : ctx->tuned) all[kv.first] = kv.second;
+	char suffix[64];
+	snprintf(suffix, sizeof suffix, ".tmp%ld.%p", (long)getpid(), (void *)ctx);
+	const std::string tmp = ctx->tune_path + suffix;
+	FILE *f = fopen(tmp.c_str(), "w");
+	if (!f) return ctx_fail(ctx, SIMPOIS_EINVAL, "%s: cannot write", tmp.c_str());
+	bool ok = fprintf(f, "simpois-tune 1\n%s\n", device_line(ctx).c_str()) > 0;
+	for (const auto &kv : all)
+		ok = ok && fprintf(f, "%d %d %s\n", kv.second.coarse_max, kv.second.nu, kv.first.c_str()) > 0;
+	ok = (fclose(f) == 0) && ok;
+	if (!ok || rename(tmp.c_str(), ctx->tune_path.c_str()) != 0) {
+		remove(tmp.c_str());
+		return ctx_fail(ctx, SIMPOIS_EINVAL, "%s: cannot write", ctx->tune_path.c_str());
+	}
+	return SIMPOIS_OK;
+}
+
 int run_converged(simpois_ctx *ctx, const simpois_image *im, int n, const simpois_params *p,
 		simpois_report *rep, int tune = 0, int *tuned_cm = nullptr, int *tuned_nu = nullptr)
 {
@@ -287,7 +371,9 @@ int run_converged(simpois_ctx *ctx, const simpois_image *im, int n, const simpoi
 		if (ctx->coarse_max_fixed > 0) o.coarse_max = ctx->coarse_max_fixed;
 		if (ctx->sweeps_fixed > 0) o.nu = ctx->sweeps_fixed;
 		const bool tune_cm = ctx->coarse_max_fixed <= 0, tune_nu = ctx->sweeps_fixed <= 0;
-		const bool tuning = tune && tunable && (tune_cm || tune_nu);
+		// with a tuning file, a shape whose choice is known is not timed again
+		const bool known = !ctx->tune_path.empty() && ctx->tuned.count(key);
+		const bool tuning = tune && tunable && (tune_cm || tune_nu) && !known;
 		if (tuning) {
 			int bc = 0, bn = 0;
 			rc = tune_and_solve(ctx, sub, o, r.data(), tune_cm, tune_nu, &bc, &bn);
@@ -295,6 +381,7 @@ int run_converged(simpois_ctx *ctx, const simpois_image *im, int n, const simpoi
 			ctx->tuned[key] = {bc, bn};
 			o.coarse_max = bc;
 			o.nu = bn;
+			if (!ctx->tune_path.empty() && (rc = tune_write(ctx))) return rc;
 		} else {
 			auto it = ctx->tuned.find(key);
 			if (it != ctx->tuned.end()) {
@@ -405,6 +492,10 @@ int simpois_create(simpois_ctx **out, int device, void *stream)
 		delete c;
 		return SIMPOIS_ECUDA;
 	}
+	// SIMPOIS_TUNE_CACHE=path: every context keeps its tuning in that file
+	const char *tc = getenv("SIMPOIS_TUNE_CACHE");
+	if (tc && *tc && simpois_set_tune_cache(c, tc) != SIMPOIS_OK)
+		fprintf(stderr, "simpois: SIMPOIS_TUNE_CACHE ignored: %s\n", c->last_error.c_str());
 	*out = c;
 	return SIMPOIS_OK;
 }
@@ -865,6 +956,21 @@ int simpois_set_memory_limit(simpois_ctx *ctx, size_t bytes)
 {
 	if (!ctx) return SIMPOIS_EINVAL;
 	ctx->arena_limit = bytes;
+	return SIMPOIS_OK;
+}
+
+int simpois_set_tune_cache(simpois_ctx *ctx, const char *path)
+{
+	if (!ctx) return SIMPOIS_EINVAL;
+	ctx->tune_path = path ? path : "";
+	if (ctx->tune_path.empty()) return SIMPOIS_OK;
+	std::map<std::string, simpois_ctx::Tuned> got;
+	const int rc = tune_read(ctx, ctx->tune_path, got);
+	if (rc) {
+		ctx->tune_path.clear();
+		return rc;
+	}
+	for (const auto &kv : got) ctx->tuned.insert(kv);   // the context's own choices stay
 	return SIMPOIS_OK;
 }
 

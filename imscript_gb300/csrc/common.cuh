@@ -83,6 +83,8 @@ struct simpois_ctx {
 		int coarse_max, nu;
 	};
 	std::map<std::string, Tuned> tuned;
+	// file the autotuner's choices are kept in ("": none)
+	std::string tune_path;
 
 	// the AMLE sweeps of the last call and the call they were captured for
 	cudaGraphExec_t amle_exec = nullptr;

@@ -118,7 +118,8 @@ struct ProbDev {
 	float *b_alt;        // fused path: the other level-0 residual buffer (k_pre5
 	                     // writes the updated r there, then swaps it with lv[0].b)
 	const CUtensorMap *tmb_alt;   // the TMA map of b_alt (swapped with lv[0].tmb)
-	double *r64, *p64, *q64;   // 13-point: FP64 Krylov vectors (else null)
+	double *r64, *p64, *p64b, *q64;   // 13-point: FP64 Krylov vectors (else null); p64 and p64b
+	                                 // hold p_new of even and odd iterations
 	double tau_min;            // FP32 inner solve: smallest relative decrease
 	double rtol;
 	LevelDev lv[MAXLEV];
@@ -333,15 +334,15 @@ __device__ __forceinline__ void gstore4(float *p, size_t k, int n, bool vec, flo
 	}
 }
 
-// Per-problem deterministic reduction of up to two values over the level-0
-// tiles of the problem.  Returns true in the last tile's block (all threads);
-// the sums are then in tot[0..1] (thread 0).
-__device__ bool problem_sum2(double v0, double v1, int prob, const int *__restrict__ tbeg,
+// Per-problem deterministic reduction of two float-float values over the
+// level-0 tiles of the problem.  Returns true in the last tile's block (all
+// threads); the sums are then in tot[0..1] (thread 0).
+__device__ bool problem_sum2_ff(FF v0, FF v1, int prob, const int *__restrict__ tbeg,
 		const int *__restrict__ tcnt, double *partial, ProbState *st, double *tot, double *sh)
 {
 	__shared__ bool am_last;
-	double s0 = block_sum<SP_THREADS>(v0, sh);
-	double s1 = block_sum<SP_THREADS>(v1, sh);
+	double s0 = block_sum_ff<SP_THREADS>(v0, sh);
+	double s1 = block_sum_ff<SP_THREADS>(v1, sh);
 	if (threadIdx.x == 0) {
 		partial[2 * blockIdx.x] = s0;
 		partial[2 * blockIdx.x + 1] = s1;
@@ -368,7 +369,7 @@ __device__ bool problem_sum2(double v0, double v1, int prob, const int *__restri
 	return true;
 }
 
-// problem_sum2 for a single value whose block sum s0 thread 0 holds.
+// problem_sum2_ff for a single value whose block sum s0 thread 0 holds.
 __device__ bool problem_sum1_block(double s0, int prob, const int *__restrict__ tbeg, const int *__restrict__ tcnt,
 		double *partial, ProbState *st, double *tot, double *sh)
 {
@@ -689,7 +690,8 @@ __global__ void k_compact(const int4 *const *__restrict__ all, const int *const 
 
 // ------------------------------------------------------------------ refinement kernels
 
-// r = rhs_sign*rhs - A U (FP64) at the unknowns; b0 = (float)r; x = 0.
+// r = rhs_sign*rhs - A U (FP64) at the unknowns; b0 = (float)r; x = 0 (the
+// biharmonic PCG: r64 = r and b0).
 // The last tile of a problem decides: converged, or start an inner solve.
 template <int K>
 __global__ void k_resid64(const ProbDev *__restrict__ P, ProbState *st, const int4 *__restrict__ tl,
@@ -734,6 +736,8 @@ __global__ void k_resid64(const ProbDev *__restrict__ P, ProbState *st, const in
 			const float rf = (float)rk;
 			if (pr.r64) {
 				pr.r64[k] = rk;     // the FP64 PCG starts from this residual
+				L.b[k] = rf;        // and the first V-cycle from its float copy,
+				pr.x[k] = rf;       // which r . z reads from x (unused by this PCG)
 			} else {
 				L.b[k] = rf;
 				pr.x[k] = 0.f;
@@ -2262,49 +2266,83 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_spmv5(const ProbDev *__restri
 // the coarse grids resolve the smooth modes that FP32 cannot see on the fine
 // one.
 
-#define TILE_LOOP_UNKNOWN(pr, t, body)                                      \
-	{                                                                   \
-		const int i_ = tile_i(t);                                   \
-		for (int r_ = 0; r_ < SP_ROWS; r_++) {                      \
-			const int j_ = tile_j(t, r_);                       \
-			if (i_ < (pr).w && j_ < (pr).h) {                   \
-				const size_t k = (size_t)j_ * (pr).w + i_;  \
-				if ((pr).lv[0].mask[k]) { body }            \
-			}                                                   \
-		}                                                           \
+// Every kernel of the loop takes one level-0 tile per block, each thread a
+// 4-pixel row group of it (grp_of), and follows the programmatic-dependent-
+// launch protocol of the tile kernels: what an earlier kernel than the one
+// just before it wrote may be loaded before grid_wait() (every kernel of the
+// chain waits before it releases, so those have completed), the rest after.
+
+__device__ __forceinline__ void ld4d(const double *p, const Grp &g, double v[4])
+{
+	if (g.vec) {
+		const double2 a = *(const double2 *)(p + g.k), b = *(const double2 *)(p + g.k + 2);
+		v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+	} else {
+#pragma unroll
+		for (int e = 0; e < 4; e++) v[e] = e < g.n ? p[g.k + e] : 0.0;
 	}
-
-// b0 = (float) r64: the first V-cycle's right-hand side
-__global__ void k_cast_r(const ProbDev *__restrict__ P, const ProbState *__restrict__ st, const int4 *__restrict__ tl)
-{
-	const int4 t = tl[blockIdx.x];
-	if (!st[t.x].inner_active) return;
-	const ProbDev &pr = P[t.x];
-	TILE_LOOP_UNKNOWN(pr, t, pr.lv[0].b[k] = (float)pr.r64[k];)
 }
 
-// b0 = z2_0: the second V-cycle's right-hand side
-__global__ void k_z2_to_b(const ProbDev *__restrict__ P, const ProbState *__restrict__ st, const int4 *__restrict__ tl)
+__device__ __forceinline__ void st4d(double *p, const Grp &g, const double v[4])
 {
-	const int4 t = tl[blockIdx.x];
-	if (!st[t.x].inner_active) return;
-	const ProbDev &pr = P[t.x];
-	TILE_LOOP_UNKNOWN(pr, t, pr.lv[0].b[k] = pr.lv[0].z2[k];)
+	if (g.vec) {
+		*(double2 *)(p + g.k) = make_double2(v[0], v[1]);
+		*(double2 *)(p + g.k + 2) = make_double2(v[2], v[3]);
+	} else {
+#pragma unroll
+		for (int e = 0; e < 4; e++)
+			if (e < g.n) p[g.k + e] = v[e];
+	}
 }
 
-// rho = r64 . z; beta = rho / rho_old (0 on the first iteration)
-__global__ void k_rz64(const ProbDev *__restrict__ P, ProbState *st, const int4 *__restrict__ tl,
-		const int *__restrict__ tbeg, const int *__restrict__ tcnt, double *partial, Globals *gl)
+// b0 = z2_0: the second V-cycle's right-hand side, on the row groups that
+// hold an unknown (b0 is read at the unknowns only)
+__global__ void __launch_bounds__(SP_THREADS) k_z2b(const ProbDev *__restrict__ P, const ProbState *__restrict__ st,
+		const int4 *__restrict__ tl)
+{
+	const int4 t = tl[blockIdx.x];
+	const ProbDev &pr = P[t.x];
+	const Grp g = grp_of(t, pr.w, pr.h);
+	uint8_t m[4] = {0, 0, 0, 0};
+	if (g.n) ldm4(pr.lv[0].mask, g, m);
+	grid_wait();
+	grid_release();
+	if (!st[t.x].inner_active || !(m[0] | m[1] | m[2] | m[3])) return;
+	float z[4];
+	ld4(pr.lv[0].z2, g, z);
+	st4(pr.lv[0].b, g, z);
+}
+
+// rho = r . z (the float r, kept in x, against the float z, summed in
+// float-float: the scalars need ~1e-7, not FP64); flexible beta = (rho - r . z_old) / rho_old
+// (0 on the first iteration of an inner solve).
+__global__ void __launch_bounds__(SP_THREADS) k_rz13(const ProbDev *__restrict__ P, ProbState *st,
+		const int4 *__restrict__ tl, const int *__restrict__ tbeg, const int *__restrict__ tcnt, double *partial,
+		Globals *gl)
 {
 	__shared__ double sh[32];
 	const int4 t = tl[blockIdx.x];
 	const int prob = t.x;
-	if (!st[prob].inner_active) return;
 	const ProbDev &pr = P[prob];
-	double rz = 0;
-	TILE_LOOP_UNKNOWN(pr, t, rz += pr.r64[k] * (double)pr.lv[0].z2[k];)
+	const Grp g = grp_of(t, pr.w, pr.h);
+	uint8_t m[4] = {0, 0, 0, 0};
+	float r[4];
+	if (g.n) ldm4(pr.lv[0].mask, g, m);
+	const bool any = m[0] | m[1] | m[2] | m[3];
+	if (any) ld4(pr.x, g, r);   // (float) r, written by k_xr13 or k_resid64 two kernels back or more
+	grid_wait();
+	grid_release();
+	if (!st[prob].inner_active) return;
+	FF rz = {0.f, 0.f};
+	if (any) {
+		float z[4];
+		ld4(pr.lv[0].z2, g, z);
+#pragma unroll
+		for (int e = 0; e < 4; e++)
+			if (m[e]) ff_add_prod(rz, r[e], z[e]);
+	}
 	double tot[2];
-	if (problem_sum1(rz, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
+	if (problem_sum1_ff(rz, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
 		ProbState &s = st[prob];
 		if (!(tot[0] > 0) || !isfinite(tot[0])) {
 			if (tot[0] != 0) s.status = SIMPOIS_BREAKDOWN;
@@ -2322,52 +2360,159 @@ __global__ void k_rz64(const ProbDev *__restrict__ P, ProbState *st, const int4 
 	}
 }
 
-// p64 = z + beta p64
-__global__ void k_pupd64(const ProbDev *__restrict__ P, const ProbState *__restrict__ st, const int4 *__restrict__ tl)
+// Exclusive prefix sum of one count per thread over the block (thread order);
+// returns the thread's offset, the total in *total.
+__device__ __forceinline__ int block_scan(int v, int *sw, int *total)
 {
-	const int4 t = tl[blockIdx.x];
-	if (!st[t.x].inner_active) return;
-	const ProbDev &pr = P[t.x];
-	const double beta = st[t.x].beta;
-	TILE_LOOP_UNKNOWN(pr, t, {
-		const double z = (double)pr.lv[0].z2[k];
-		pr.p64[k] = beta != 0 ? z + beta * pr.p64[k] : z;
-	})
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	int x = v;
+#pragma unroll
+	for (int o = 1; o < 32; o <<= 1) {
+		const int y = __shfl_up_sync(0xffffffffu, x, o);
+		if (lane >= o) x += y;
+	}
+	if (lane == 31) sw[warp] = x;
+	__syncthreads();
+	int base = 0, all = 0;
+#pragma unroll
+	for (int k = 0; k < SP_THREADS / 32; k++) {
+		const int c = sw[k];
+		base += k < warp ? c : 0;
+		all += c;
+	}
+	__syncthreads();   // sw may be reused
+	*total = all;
+	return base + x - v;
 }
 
-// q64 = A p64 with the 13-point clamped operator in FP64; alpha = rho / (p.q)
-__global__ void k_spmv64(const ProbDev *__restrict__ P, ProbState *st, const int4 *__restrict__ tl,
-		const int *__restrict__ tbeg, const int *__restrict__ tcnt, double *partial, Globals *gl)
+// p_new = z + beta p_old (z alone on the first iteration of an inner solve);
+// q = A p_new with the 13-point single-clamp operator (cleant_cgpois.c:91-121)
+// in FP64; alpha = rho / (p.q).  Iteration parity par writes p_new into
+// p64 (par 0) or p64b (par 1) and reads p_old from the other: neighbouring
+// tiles still read p_old in their halo.  The region is the tile with 2 rows and
+// 4 columns of halo (40 x 36, 4-aligned column groups), loaded in row groups
+// (p_old, z and 0 at the known pixels).  An FP64 instruction occupies this
+// GPU's FP64 pipe for a whole warp whatever its active lanes, so the FP64 work
+// runs over compacted lists instead of the pixel grid: the unknown cells of the
+// region (p_new) and of the tile (A p_new, p.q), in row order.  A neighbour
+// outside the image is the clamped pixel, which lies in the region (the single
+// clamp of the reference's 13-point operator); tiles 2 or more pixels from
+// every image side take the constant offsets instead.
+__global__ void __launch_bounds__(SP_THREADS) k_pspmv13(const ProbDev *__restrict__ P, ProbState *st,
+		const int4 *__restrict__ tl, const int *__restrict__ tbeg, const int *__restrict__ tcnt, double *partial,
+		Globals *gl, int par)
 {
+	constexpr int RW = SP_TILE + 8, RH = SP_TILE + 4;   // region: 40 x 36
+	constexpr int NG = RW * RH / 4;                      // 4-cell groups
+	constexpr int NV = (NG + SP_THREADS - 1) / SP_THREADS;
+	__shared__ __align__(16) double sp[RW * RH];
+	__shared__ __align__(16) float sz[RW * RH];
+	__shared__ __align__(16) uint8_t sc[RW * RH];
+	__shared__ uint16_t lreg[RW * RH], lown[SP_TILE * SP_TILE];
 	__shared__ double sh[32];
+	__shared__ int sw[SP_THREADS / 32];
 	const int4 t = tl[blockIdx.x];
 	const int prob = t.x;
-	if (!st[prob].inner_active) return;
 	const ProbDev &pr = P[prob];
-	const uint8_t *m = pr.lv[0].mask;
+	const LevelDev &L = pr.lv[0];
 	const int w = pr.w, h = pr.h;
-	double pq = 0;
-	const int i = tile_i(t);
-	for (int r = 0; r < SP_ROWS; r++) {
-		const int j = tile_j(t, r);
-		if (i >= w || j >= h) continue;
-		const size_t k = (size_t)j * w + i;
-		if (!m[k]) continue;
-		double diag = 20.0, off = 0.0;
+	const double *pold = par ? pr.p64 : pr.p64b;
+	double *pnew = par ? pr.p64b : pr.p64;
+	const bool vec = (w & 3) == 0;
+	const int x0 = t.y * SP_TILE - 4, y0 = t.z * SP_TILE - 2;
+	// before the dependency wait: the codes, z (written by the last V-cycle's
+	// level-0 kernel, two launches back) and p_old (the previous SpMV's), into
+	// the region with 0 at the known pixels
+	int nreg = 0;
 #pragma unroll
-		for (int s2 = 0; s2 < 12; s2++) {
-			const int qi = clampi(i + c_di13[s2], w), qj = clampi(j + c_dj13[s2], h);
-			if (qi == i && qj == j) {
-				diag += c_cf13[s2];
-			} else {
-				const size_t q = (size_t)qj * w + qi;
-				if (m[q]) off += (double)c_cf13[s2] * pr.p64[q];
+	for (int it = 0; it < NV; it++) {
+		const int f = threadIdx.x + it * SP_THREADS;
+		if (f < NG) {
+			const int ry = f / (RW / 4), rx = 4 * (f - ry * (RW / 4)), gi = x0 + rx, gj = y0 + ry;
+			const int n = group_cells(gi, gj, w, h);
+			const size_t k = n ? (size_t)gj * w + gi : 0;
+			const uint32_t cd = gload4u8(L.code, k, n, vec) & 0x01010101u;   // the unknown bits
+			const int c = ry * RW + rx;
+			*(uint32_t *)(sc + c) = cd;
+			float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+			double2 pa = make_double2(0.0, 0.0), pb = make_double2(0.0, 0.0);
+			if (cd) {
+				z = gload4(L.z2, k, n, vec);
+				if (vec) {
+					pa = *(const double2 *)(pold + k);
+					pb = *(const double2 *)(pold + k + 2);
+				} else {
+					pa.x = pold[k];
+					if (n > 1) pa.y = pold[k + 1];
+					if (n > 2) pb.x = pold[k + 2];
+					if (n > 3) pb.y = pold[k + 3];
+				}
+				nreg += __popc(cd);
+			}
+			*(float4 *)(sz + c) = make_float4((cd & 1u) ? z.x : 0.f, (cd & 0x100u) ? z.y : 0.f,
+					(cd & 0x10000u) ? z.z : 0.f, (cd & 0x1000000u) ? z.w : 0.f);
+			*(double2 *)(sp + c) = make_double2((cd & 1u) ? pa.x : 0.0, (cd & 0x100u) ? pa.y : 0.0);
+			*(double2 *)(sp + c + 2) = make_double2((cd & 0x10000u) ? pb.x : 0.0, (cd & 0x1000000u) ? pb.y : 0.0);
+		}
+	}
+	// the lists: unknown region cells in group order, unknown tile cells in row order
+	const int ty = threadIdx.x >> 3, tx = 4 * (threadIdx.x & 7);
+	const int cown = (ty + 2) * RW + tx + 4;   // the thread's 4 tile cells
+	__syncthreads();   // sc
+	const uint32_t mown = *(const uint32_t *)(sc + cown);
+	int nr = 0, no = 0;
+	int offr = block_scan(nreg, sw, &nr);
+#pragma unroll
+	for (int it = 0; it < NV; it++) {
+		const int f = threadIdx.x + it * SP_THREADS;
+		if (f < NG) {
+			const int ry = f / (RW / 4), rx = 4 * (f - ry * (RW / 4)), c = ry * RW + rx;
+			const uint32_t cd = *(const uint32_t *)(sc + c);
+#pragma unroll
+			for (int e = 0; e < 4; e++)
+				if ((cd >> (8 * e)) & 1u) lreg[offr++] = (uint16_t)(c + e);
+		}
+	}
+	int offo = block_scan(__popc(mown), sw, &no);
+#pragma unroll
+	for (int e = 0; e < 4; e++)
+		if ((mown >> (8 * e)) & 1u) lown[offo++] = (uint16_t)(cown + e);
+	grid_wait();
+	grid_release();
+	if (!st[prob].inner_active) return;
+	const double beta = st[prob].beta;
+	__syncthreads();   // lreg, lown
+	for (int k = threadIdx.x; k < nr; k += SP_THREADS) {
+		const int c = lreg[k];
+		sp[c] = beta != 0 ? fma(beta, sp[c], (double)sz[c]) : (double)sz[c];
+	}
+	__syncthreads();
+	const bool inner = t.y * SP_TILE >= 2 && t.y * SP_TILE + SP_TILE + 2 <= w && t.z * SP_TILE >= 2 &&
+			t.z * SP_TILE + SP_TILE + 2 <= h;
+	constexpr int DI[12] = {1, 0, -1, 0, 1, 1, -1, -1, 2, 0, -2, 0};
+	constexpr int DJ[12] = {0, 1, 0, -1, 1, -1, 1, -1, 0, 2, 0, -2};
+	constexpr double CF[12] = {-8, -8, -8, -8, 2, 2, 2, 2, 1, 1, 1, 1};
+	double pq = 0.0;
+	for (int k = threadIdx.x; k < no; k += SP_THREADS) {
+		const int c = lown[k];
+		const int ry = c / RW, rx = c - ry * RW, i = x0 + rx, j = y0 + ry;
+		const double pk = sp[c];
+		double off = 0.0;
+		if (inner) {
+#pragma unroll
+			for (int s2 = 0; s2 < 12; s2++) off = fma(CF[s2], sp[c + DJ[s2] * RW + DI[s2]], off);
+		} else {
+#pragma unroll
+			for (int s2 = 0; s2 < 12; s2++) {
+				const int qi = clampi(i + DI[s2], w), qj = clampi(j + DJ[s2], h);
+				off = fma(CF[s2], sp[(qj - y0) * RW + (qi - x0)], off);
 			}
 		}
-		const double pk = pr.p64[k];
-		const double qk = diag * pk + off;
-		pr.q64[k] = qk;
-		pq += pk * qk;
+		const double qk = fma(20.0, pk, off);
+		pq = fma(pk, qk, pq);
+		const size_t g = (size_t)j * w + i;   // p and q are read at the unknowns only
+		pnew[g] = pk;
+		pr.q64[g] = qk;
 	}
 	double tot[2];
 	if (problem_sum1(pq, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
@@ -2386,26 +2531,57 @@ __global__ void k_spmv64(const ProbDev *__restrict__ P, ProbState *st, const int
 	}
 }
 
-// U += alpha p64 (the FP64 solution itself); r64 -= alpha q64; r.r; stop test
-__global__ void k_xr64(const ProbDev *__restrict__ P, ProbState *st, const int4 *__restrict__ tl,
-		const int *__restrict__ tbeg, const int *__restrict__ tcnt, double *partial, Globals *gl)
+// U += alpha p_new (the FP64 solution itself); r -= alpha q; b0 = (float) r,
+// the first V-cycle's right-hand side (and a copy in x for k_rz13); |r|^2 and
+// r . z_old (flexible beta)
+// from the float r in float-float (the stop test and the scalars need ~1e-7);
+// the stop test.
+__global__ void __launch_bounds__(SP_THREADS) k_xr13(const ProbDev *__restrict__ P, ProbState *st,
+		const int4 *__restrict__ tl, const int *__restrict__ tbeg, const int *__restrict__ tcnt, double *partial,
+		Globals *gl, int par)
 {
 	__shared__ double sh[32];
 	const int4 t = tl[blockIdx.x];
 	const int prob = t.x;
-	if (!st[prob].inner_active) return;
 	const ProbDev &pr = P[prob];
+	const Grp g = grp_of(t, pr.w, pr.h);
+	uint8_t m[4] = {0, 0, 0, 0};
+	double u[4], r[4];
+	float zo[4];
+	if (g.n) ldm4(pr.lv[0].mask, g, m);
+	const bool any = m[0] | m[1] | m[2] | m[3];   // row groups without an unknown move nothing
+	if (any) {   // written two or more launches back
+		ld4d(pr.U, g, u);
+		ld4d(pr.r64, g, r);
+		ld4(pr.lv[0].z2, g, zo);
+	}
+	grid_wait();
+	grid_release();
+	if (!st[prob].inner_active) return;
 	const double a = st[prob].alpha;
-	double rr = 0, cross = 0;
-	TILE_LOOP_UNKNOWN(pr, t, {
-		pr.U[k] += a * pr.p64[k];
-		const double rk = pr.r64[k] - a * pr.q64[k];
-		pr.r64[k] = rk;
-		rr += rk * rk;
-		cross += rk * (double)pr.lv[0].z2[k];   // z2 still holds the previous z
-	})
+	FF rr = {0.f, 0.f}, cross = {0.f, 0.f};
+	if (any) {
+		double pv[4], qv[4];
+		ld4d(par ? pr.p64b : pr.p64, g, pv);
+		ld4d(pr.q64, g, qv);
+		float rf[4];
+#pragma unroll
+		for (int e = 0; e < 4; e++) {
+			rf[e] = 0.f;
+			if (!m[e]) continue;
+			u[e] = fma(a, pv[e], u[e]);
+			r[e] = fma(-a, qv[e], r[e]);
+			rf[e] = (float)r[e];
+			ff_add_prod(rr, rf[e], rf[e]);
+			ff_add_prod(cross, rf[e], zo[e]);
+		}
+		st4d(pr.U, g, u);
+		st4d(pr.r64, g, r);
+		st4(pr.lv[0].b, g, rf);
+		st4(pr.x, g, rf);   // for r . z (k_rz13): x is not used by this PCG
+	}
 	double tot[2];
-	if (problem_sum2(rr, cross, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
+	if (problem_sum2_ff(rr, cross, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
 		ProbState &s = st[prob];
 		s.rr = tot[0];
 		s.cross = tot[1];
@@ -2688,6 +2864,10 @@ constexpr double BPX_SPMV5 = 1 + 4 + 4 + 4 + 4;           // mask, z2, p_old; p_
 constexpr double BPX_STEP = 4 + 4 + 4 + 4 + 1 + 4 + 4 + 4; // k_pre5's PCG step: q, x, xlo, p, mask; x, xlo, r
 constexpr double BPX_RESID64 = 1 + 8 + 4 + 4 + 4 + 4;     // mask, U, rhs; b, x, xlo
 constexpr double BPX_UADD = 1 + 8 + 4 + 4 + 8;            // mask, U, x, xlo; U
+constexpr double BPX_PSPMV13 = 1 + 4 + 8 + 8 + 8;        // mask, z2, p_old; p_new, q (FP64)
+constexpr double BPX_XR13 = 1 + 8 + 8 + 4 + 8 + 8 + 8 + 8 + 4 + 4; // mask, U, r, z2, p, q; U, r, b, x
+constexpr double BPX_Z2B = 4 + 4;                         // z2; b
+constexpr double BPX_RZ13 = 1 + 4 + 4;                    // mask, (float) r, z2
 constexpr double BPC_COARSE5 = 1 + 4 + 4 + 0.34;          // per top coarse cell: mask, b; z2; coarser masks
 
 #define KT_BEGIN(pl, s)                                            \
@@ -2814,32 +2994,50 @@ void launch_vcycle_fused(const Plan &pl, cudaStream_t s, int pcg = 1, int use_p2
 	}
 }
 
-// Biharmonic preconditioner: z = V(V(r)) with V the fused 5-point V-cycle,
-// then rho = r . z and beta.
+// Biharmonic preconditioner: z = V(V(r)) with V the fused 5-point V-cycle on
+// b0 = (float) r (written by k_resid64 or k_xr13), then rho = r . z and beta.
 void launch_precond_bih(const Plan &pl, cudaStream_t s)
 {
 	const int nt = pl.nact[0];
-	k_cast_r<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0]); ++*pl.nl;
 	launch_vcycle_fused(pl, s, 0);
-	k_z2_to_b<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0]); ++*pl.nl;
+	{
+		KT_BEGIN(pl, s);
+		launch_k(pl.pdl, k_z2b, nt, SP_THREADS, 0, s, (const ProbDev *)pl.dp, (const ProbState *)pl.dst,
+				(const int4 *)pl.act[0]); ++*pl.nl;
+		KT_END(pl, s, "k_z2b", pl.kt->px(0) * BPX_Z2B);
+	}
 	launch_vcycle_fused(pl, s, 0);
-	k_rz64<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl); ++*pl.nl;
+	{
+		KT_BEGIN(pl, s);
+		launch_k(pl.pdl, k_rz13, nt, SP_THREADS, 0, s, (const ProbDev *)pl.dp, pl.dst, (const int4 *)pl.act[0],
+				(const int *)pl.tbeg, (const int *)pl.tcnt, pl.partial, pl.gl); ++*pl.nl;
+		KT_END(pl, s, "k_rz13", pl.kt->px(0) * BPX_RZ13);
+	}
 }
 
-// One FP64 biharmonic PCG iteration.
+// Two FP64 biharmonic PCG iterations (the search direction alternates between
+// p64 and p64b).
 void launch_iteration_bih(const Plan &pl, cudaStream_t s)
 {
 	const int nt = pl.nact[0];
-	kt_refresh(pl, s);
-	k_pupd64<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0]); ++*pl.nl;
-	{
-		KT_BEGIN(pl, s);
-		k_spmv64<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl);
-		++*pl.nl;
-		KT_END(pl, s, "k_spmv64", pl.kt->px(0) * (1 + 8 + 8));
+	for (int par = 0; par < 2; par++) {
+		kt_refresh(pl, s);
+		{
+			KT_BEGIN(pl, s);
+			// the first launch of the loop body follows no kernel of the body
+			launch_k(par ? pl.pdl : 0, k_pspmv13, nt, SP_THREADS, 0, s, (const ProbDev *)pl.dp, pl.dst,
+					(const int4 *)pl.act[0], (const int *)pl.tbeg, (const int *)pl.tcnt, pl.partial, pl.gl,
+					par); ++*pl.nl;
+			KT_END(pl, s, "k_pspmv13", pl.kt->px(0) * BPX_PSPMV13);
+		}
+		{
+			KT_BEGIN(pl, s);
+			launch_k(pl.pdl, k_xr13, nt, SP_THREADS, 0, s, (const ProbDev *)pl.dp, pl.dst, (const int4 *)pl.act[0],
+					(const int *)pl.tbeg, (const int *)pl.tcnt, pl.partial, pl.gl, par); ++*pl.nl;
+			KT_END(pl, s, "k_xr13", pl.kt->px(0) * BPX_XR13);
+		}
+		launch_precond_bih(pl, s);
 	}
-	k_xr64<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl); ++*pl.nl;
-	launch_precond_bih(pl, s);
 }
 
 // Two fused PCG iterations (the search direction alternates between p and p2).
@@ -3226,7 +3424,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	Layout Lo;
 	std::vector<size_t> off_mask[MAXLEV], off_code[MAXLEV], off_b[MAXLEV], off_z[MAXLEV], off_z2[MAXLEV];
 	std::vector<size_t> off_U(n), off_x(n), off_xlo(n), off_p(n), off_q(n), off_p2(n), off_balt(n);
-	std::vector<size_t> off_r64(n, 0), off_p64(n, 0), off_q64(n, 0);
+	std::vector<size_t> off_r64(n, 0), off_p64(n, 0), off_p64b(n, 0), off_q64(n, 0);
 	size_t ntl[MAXLEV] = {};   // tiles per level over all problems
 	std::string lkey;          // the problem sizes, which alone decide the tile lists
 	const int cmax = opt.coarse_max > 0 ? clamp_coarse_max(opt.coarse_max) : default_coarse_max();
@@ -3286,6 +3484,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 		if (q.kind == 1 && opt.fused && opt.use_mg) {   // FP64 Krylov vectors of the biharmonic PCG
 			off_r64[k] = Lo.take(px * 8);
 			off_p64[k] = Lo.take(px * 8);
+			off_p64b[k] = Lo.take(px * 8);
 			off_q64[k] = Lo.take(px * 8);
 		}
 	}
@@ -3374,6 +3573,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 		d.b_alt = (float *)(A + off_balt[k]);
 		d.r64 = off_r64[k] ? (double *)(A + off_r64[k]) : nullptr;
 		d.p64 = off_p64[k] ? (double *)(A + off_p64[k]) : nullptr;
+		d.p64b = off_p64b[k] ? (double *)(A + off_p64b[k]) : nullptr;
 		d.q64 = off_q64[k] ? (double *)(A + off_q64[k]) : nullptr;
 		for (int l = 0; l < d.nlev; l++) {
 			d.lv[l].mask = (uint8_t *)(A + off_mask[l][k]);

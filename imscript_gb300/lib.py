@@ -69,7 +69,7 @@ EXPORTS = [
     "simpois_strerror", "simpois_last_error", "simpois_solve", "simpois_solve_device",
     "simpois_solve_batch", "simpois_solve_batch_host", "simpois_residual_device", "simpois_residual_device_noalloc",
     "simpois_adjoint_device", "simpois_autotune", "simpois_autotune_ex", "simpois_set_coarse_max",
-    "simpois_set_sweeps", "simpois_set_memory_limit",
+    "simpois_set_sweeps", "simpois_set_memory_limit", "simpois_set_tune_cache",
     "simpois_amle_device", "simpois_amle", "amle",
     "simpois_launch_count", "simpois_reset_launch_count", "simpois_kernel_stats",
     "simpois_reset_kernel_stats",
@@ -125,6 +125,7 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
         L.simpois_set_coarse_max.argtypes = [vp, ip]
         L.simpois_set_sweeps.argtypes = [vp, ip]
         L.simpois_set_memory_limit.argtypes = [vp, ctypes.c_size_t]
+        L.simpois_set_tune_cache.argtypes = [vp, ctypes.c_char_p]
         dp = ctypes.POINTER(ctypes.c_double)
         L.simpois_amle_device.argtypes = [vp, vp, vp, ip, ip, ip, ip, ip, vp, dp]
         L.simpois_amle.argtypes = [vp, vp, vp, ip, ip, ip, ip, ip, vp, dp]
@@ -203,6 +204,12 @@ class Context:
         """Largest device arena this context may hold (0: no limit); a solve
         that needs more returns ENOMEM before it touches anything."""
         self.check(self._lib.simpois_set_memory_limit(self.handle, int(nbytes)))
+
+    def set_tune_cache(self, path):
+        """Keep the autotuner's choices in the file ``path`` (None: stop); the
+        choices it holds for this device are loaded now, and a batch shape
+        whose choice is known is not timed again."""
+        self.check(self._lib.simpois_set_tune_cache(self.handle, None if path is None else str(path).encode()))
 
     def last_error(self) -> str:
         return self._lib.simpois_last_error(self.handle).decode()

@@ -251,6 +251,17 @@ int simpois_autotune(simpois_ctx *ctx, const simpois_image *images, int n,
 int simpois_set_coarse_max(simpois_ctx *ctx, int coarse_max);
 int simpois_set_sweeps(simpois_ctx *ctx, int sweeps);
 
+/* Keeps the autotuner's choices in a text file across processes (NULL or ""
+ * stops).  The call reads the choices the file holds for this context's device
+ * model (a file written on another model reads as empty; a missing file is
+ * fine; a file that is not a tuning file, or holds a malformed choice, gives
+ * SIMPOIS_EINVAL and leaves the context without a file).  From then on
+ * simpois_autotune_ex solves a batch whose shapes have a known choice with it
+ * instead of timing the candidates again, and writes every new choice back
+ * (the file is replaced through a temporary file in its directory).
+ * SIMPOIS_TUNE_CACHE=path does the same for every new context. */
+int simpois_set_tune_cache(simpois_ctx *ctx, const char *path);
+
 /* Device-memory budget of a context (no counterpart in the reference, whose
  * xmalloc exits on an allocation failure, simpois.c:10-19).  A solve whose
  * working set would take the context's device arena above `bytes` returns

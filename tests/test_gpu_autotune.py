@@ -163,3 +163,95 @@ def test_every_candidate_meets_the_fp64_solve(sp, sweeps):
     finally:
         ctx.set_sweeps(0)
         ctx.set_coarse_max(0)
+
+
+_STREAMS = []
+
+
+def _on_new_stream(fn):
+    """Run fn on a stream of its own: simpois.context caches one context per
+    stream, so this gives a context that has not tuned anything yet."""
+    s = torch.cuda.Stream()
+    _STREAMS.append(s)   # the cached context keeps the handle: keep the stream
+    with torch.cuda.stream(s):
+        out = fn()
+    torch.cuda.synchronize()
+    return out
+
+
+def test_tuning_file_keeps_the_choice_across_contexts(sp, tmp_path):
+    """A context with a tuning file writes its choice there; a new context
+    reading the file solves the same shapes with the file's choice without
+    timing (a choice planted in the file is the one reported and used)."""
+    from imscript_gb300 import lib
+    imgs = _images(31)
+    path = tmp_path / "tune.txt"
+
+    def first():
+        sp.context(0, torch.cuda.current_stream().cuda_stream).set_tune_cache(path)
+        return sp.autotune(imgs, rtol=1e-6)
+    _, ra, tuned = _on_new_stream(first)
+    assert all(r["status"] == 0 for r in ra)
+    lines = path.read_text().splitlines()
+    assert lines[0] == "simpois-tune 1" and lines[1].startswith("device ") and len(lines) == 3
+    cm, nu, key = lines[2].split(" ", 2)
+    assert (int(cm), int(nu)) == (tuned["coarse_max"], tuned["sweeps"])
+    # plant another choice for the same shapes
+    path.write_text("\n".join(lines[:2] + [f"32 3 {key}"]) + "\n")
+
+    def second():
+        ctx = sp.context(0, torch.cuda.current_stream().cuda_stream)
+        ctx.set_tune_cache(path)
+        outs, reps, t2 = sp.autotune(imgs, rtol=1e-6)
+        ctx.set_coarse_max(32)
+        ctx.set_sweeps(3)
+        try:
+            ref, _ = sp.solve_batch(imgs, rtol=1e-6)
+        finally:
+            ctx.set_coarse_max(0)
+            ctx.set_sweeps(0)
+        return outs, reps, t2, ref
+    outs, reps, t2, ref = _on_new_stream(second)
+    assert t2 == {"coarse_max": 32, "sweeps": 3}
+    assert all(r["status"] == 0 and r["rel_residual"] <= 1e-6 for r in reps)
+    for x, y in zip(outs, ref):
+        assert torch.equal(x.view(torch.int32), y.view(torch.int32))
+
+
+def test_tuning_file_errors(sp, tmp_path):
+    """Not a tuning file, or a malformed choice: SIMPOIS_EINVAL and no file on
+    the context; another device model's file reads as empty and is rewritten
+    with this device's choice."""
+    from imscript_gb300 import lib
+    ctx = _ctx(sp)
+    bad = tmp_path / "bad.txt"
+    bad.write_text("hello\n")
+    with pytest.raises(lib.SimpoisError):
+        ctx.set_tune_cache(bad)
+    dev = None
+    good = tmp_path / "t.txt"
+    imgs = _images(37)
+
+    def tune():
+        c = sp.context(0, torch.cuda.current_stream().cuda_stream)
+        c.set_tune_cache(good)
+        return sp.autotune(imgs, rtol=1e-6)
+    _on_new_stream(tune)
+    lines = good.read_text().splitlines()
+    dev = lines[1]
+    bad.write_text(f"simpois-tune 1\n{dev}\n32 x 0fm|10x10\n")
+    with pytest.raises(lib.SimpoisError):
+        ctx.set_tune_cache(bad)
+    other = tmp_path / "other.txt"
+    other.write_text("simpois-tune 1\ndevice 1.0 1 another GPU\n32 3 " + lines[2].split(" ", 2)[2] + "\n")
+
+    def retune():
+        c = sp.context(0, torch.cuda.current_stream().cuda_stream)
+        c.set_tune_cache(other)
+        return sp.autotune(imgs, rtol=1e-6)
+    _, reps, t3 = _on_new_stream(retune)
+    assert all(r["status"] == 0 for r in reps)
+    rewritten = other.read_text().splitlines()
+    assert rewritten[1] == dev and len(rewritten) == 3
+    assert rewritten[2].split(" ", 2)[:2] == [str(t3["coarse_max"]), str(t3["sweeps"])]
+    ctx.set_tune_cache(None)
