@@ -164,7 +164,7 @@ std::string tune_key(const std::vector<MgProblem> &sub, int kind, const MgOption
 // the caller fixed is not tuned.  The batch is left solved with the chosen
 // pair.
 int tune_and_solve(simpois_ctx *ctx, const std::vector<MgProblem> &sub, MgOptions opt, simpois_report *r,
-		bool tune_cm, bool tune_nu, int *chosen_cm, int *chosen_nu)
+		double *bnorm2, bool tune_cm, bool tune_nu, int *chosen_cm, int *chosen_nu)
 {
 	cudaEvent_t a, b;
 	SP_CUDA(ctx, cudaEventCreate(&a));
@@ -177,11 +177,11 @@ int tune_and_solve(simpois_ctx *ctx, const std::vector<MgProblem> &sub, MgOption
 	auto timed = [&](int cm, int nu, float *best_ms) -> int {
 		opt.coarse_max = cm;
 		opt.nu = nu;
-		int e = mg_solve(ctx, sub.data(), (int)sub.size(), opt, r);
+		int e = mg_solve(ctx, sub.data(), (int)sub.size(), opt, r, bnorm2);
 		for (int k = 0; k < 2 && !e; k++) {
 			float ms = 0;
 			cudaEventRecord(a, ctx->stream);
-			e = mg_solve(ctx, sub.data(), (int)sub.size(), opt, r);
+			e = mg_solve(ctx, sub.data(), (int)sub.size(), opt, r, bnorm2);
 			cudaEventRecord(b, ctx->stream);
 			if (!e && (cudaEventSynchronize(b) != cudaSuccess || cudaEventElapsedTime(&ms, a, b) != cudaSuccess))
 				e = ctx_fail(ctx, SIMPOIS_ECUDA, "autotuner timing: %s", cudaGetErrorString(cudaGetLastError()));
@@ -227,7 +227,7 @@ int tune_and_solve(simpois_ctx *ctx, const std::vector<MgProblem> &sub, MgOption
 	if (!rc && (last_cm != best_cm || last_nu != best_nu)) {
 		opt.coarse_max = best_cm;
 		opt.nu = best_nu;
-		rc = mg_solve(ctx, sub.data(), (int)sub.size(), opt, r);
+		rc = mg_solve(ctx, sub.data(), (int)sub.size(), opt, r, bnorm2);
 	}
 	cudaEventDestroy(a);
 	cudaEventDestroy(b);
@@ -318,6 +318,293 @@ static int tune_write(simpois_ctx *ctx)
 	return SIMPOIS_OK;
 }
 
+// ---------------------------------------------------------------- hole components
+// A biharmonic channel whose unknowns form several groups that no stencil
+// couples is several independent systems: the 13-point operator reaches 2
+// pixels, the 5-point V-cycles of its preconditioner 1 (and their coarse
+// levels only join cells whose children are all unknown).  Solved as one
+// problem, every group iterates until the slowest converges (a thin scratch
+// needs ~10 PCG iterations, a 1024-pixel hole hundreds); solved as separate
+// problems in separate problem groups, each retires on its own.  The groups
+// are found on a map of 8 x 8 pixel blocks: blocks holding an unknown, joined
+// to their 8 neighbours (unknowns in blocks that do not touch are at least 9
+// pixels apart).  Each group becomes a crop: its blocks' bounding box grown by
+// the 13-point reach (2) and clipped to the image, so the known pixels its
+// equations read are in the crop, and the image sides stay where they are (the
+// operator's clamp).  In the crop, another group's unknowns read as known
+// zeros: no equation of this group reaches them.  Each crop converges to the
+// channel's relative residual, so the channel does: |r|^2 is the sum over the
+// crops of |r_k|^2 <= rtol^2 |b_k|^2.
+constexpr int HB = 8;   // block side of the component map
+constexpr int SPLIT_MAX = 256;   // most components a channel is split into
+constexpr size_t SPLIT_TOTAL = 2048;   // and a batch
+
+__global__ void k_block_any(const float *__restrict__ g, int w, int h, int bw, uint8_t *__restrict__ out)
+{
+	const int bx = blockIdx.x % bw, by = blockIdx.x / bw;
+	const int x = bx * HB + (threadIdx.x & 7), y = by * HB + (threadIdx.x >> 3);
+	const bool u = x < w && y < h && isnan(g[(size_t)y * w + x]);
+	const int any = __syncthreads_or(u);
+	if (threadIdx.x == 0) out[blockIdx.x] = (uint8_t)(any != 0);
+}
+
+struct CropDev {
+	const float *g, *f;         // the channel (device)
+	float *out;                 // the channel's output
+	float *cg, *cf, *cout;      // the crop's input, data term, output
+	const int *label;           // the channel's block labels
+	int w, x0, y0, cw, ch, bw, comp;
+};
+
+// crop input: the channel's pixels, another group's unknowns as known zeros
+__global__ void k_crop_gather(const CropDev *__restrict__ cr)
+{
+	const CropDev c = cr[blockIdx.y];
+	const size_t n = (size_t)c.cw * c.ch;
+	for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+		const int y = (int)(k / c.cw), x = (int)(k - (size_t)y * c.cw);
+		const int gx = c.x0 + x, gy = c.y0 + y;
+		const size_t q = (size_t)gy * c.w + gx;
+		float v = c.g[q];
+		if (isnan(v) && c.label[(gy / HB) * c.bw + gx / HB] != c.comp) v = 0.f;
+		c.cg[k] = v;
+		if (c.cf) c.cf[k] = c.f[q];
+	}
+}
+
+// the crop's unknowns into the channel's output
+__global__ void k_crop_scatter(const CropDev *__restrict__ cr)
+{
+	const CropDev c = cr[blockIdx.y];
+	const size_t n = (size_t)c.cw * c.ch;
+	for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+		const int y = (int)(k / c.cw), x = (int)(k - (size_t)y * c.cw);
+		const int gx = c.x0 + x, gy = c.y0 + y;
+		const size_t q = (size_t)gy * c.w + gx;
+		if (isnan(c.g[q]) && c.label[(gy / HB) * c.bw + gx / HB] == c.comp) c.out[q] = c.cout[k];
+	}
+}
+
+struct HoleSplit {
+	std::vector<MgProblem> probs;   // the problems to solve: whole channels and crops
+	std::vector<int> owner;         // the channel (index into the input list) of each
+	CropDev *table = nullptr;       // the crops (device), ncrop of them
+	int ncrop = 0;
+	unsigned gx = 1;                // blocks per crop of the gather and scatter
+};
+
+// SIMPOIS_SPLIT=0: biharmonic channels are solved whole
+static bool split_enabled()
+{
+	static bool v = [] {
+		const char *e = getenv("SIMPOIS_SPLIT");
+		return !(e && atoi(e) == 0);
+	}();
+	return v;
+}
+
+// Split the channels of `sub` (one operator kind) into hole components;
+// channels with one component stay whole.  The crops' inputs are gathered and
+// the split channels' outputs hold their inputs (the known pixels) on return.
+static int split_holes(simpois_ctx *ctx, const std::vector<MgProblem> &sub, HoleSplit &hs)
+{
+	cudaStream_t s = ctx->stream;
+	const int n = (int)sub.size();
+	std::vector<size_t> moff(n + 1, 0);
+	std::vector<int> bws(n), bhs(n);
+	for (int k = 0; k < n; k++) {
+		bws[k] = (sub[k].w + HB - 1) / HB;
+		bhs[k] = (sub[k].h + HB - 1) / HB;
+		moff[k + 1] = moff[k] + (size_t)bws[k] * bhs[k];
+	}
+	int rc = ctx_pinned_reserve(ctx, moff[n] + 16);
+	if (rc) return rc;
+	uint8_t *maps = (uint8_t *)ctx->pinned;   // written by the kernel straight into page-locked memory
+	for (int k = 0; k < n; k++) {
+		k_block_any<<<(unsigned)(moff[k + 1] - moff[k]), HB * HB, 0, s>>>(sub[k].g, sub[k].w, sub[k].h, bws[k],
+				maps + moff[k]);
+		ctx->launches++;
+	}
+	SP_LAUNCH_CHECK(ctx);
+	SP_CUDA(ctx, cudaStreamSynchronize(s));
+	// components (8-neighbour flood fill) and their bounding boxes in blocks
+	struct Comp { int ch, id, bx0, by0, bx1, by1; };
+	std::vector<Comp> comps;
+	std::vector<std::vector<int>> labels(n);
+	std::vector<int> ncomp(n, 0), stack;
+	for (int k = 0; k < n; k++) {
+		const int bw = bws[k], bh = bhs[k];
+		const uint8_t *m = maps + moff[k];
+		std::vector<int> &lab = labels[k];
+		lab.assign((size_t)bw * bh, -1);
+		const size_t first = comps.size();
+		for (int b0 = 0; b0 < bw * bh; b0++) {
+			if (!m[b0] || lab[b0] >= 0) continue;
+			Comp c = {k, ncomp[k]++, b0 % bw, b0 / bw, b0 % bw, b0 / bw};
+			lab[b0] = c.id;
+			stack.assign(1, b0);
+			while (!stack.empty()) {
+				const int b = stack.back();
+				stack.pop_back();
+				const int bx = b % bw, by = b / bw;
+				c.bx0 = std::min(c.bx0, bx); c.bx1 = std::max(c.bx1, bx);
+				c.by0 = std::min(c.by0, by); c.by1 = std::max(c.by1, by);
+				for (int dy = -1; dy <= 1; dy++)
+					for (int dx = -1; dx <= 1; dx++) {
+						const int x = bx + dx, y = by + dy;
+						if (x < 0 || y < 0 || x >= bw || y >= bh) continue;
+						const int q = y * bw + x;
+						if (m[q] && lab[q] < 0) {
+							lab[q] = c.id;
+							stack.push_back(q);
+						}
+					}
+			}
+			comps.push_back(c);
+		}
+		// one component (or none), or so many that the problems' overheads
+		// would outweigh the retirements: solved whole
+		if (ncomp[k] < 2 || ncomp[k] > SPLIT_MAX || comps.size() > SPLIT_TOTAL) {
+			comps.resize(first);
+			ncomp[k] = 1;
+		}
+	}
+	hs.probs.clear();
+	hs.owner.clear();
+	hs.ncrop = (int)comps.size();
+	for (int k = 0; k < n; k++)
+		if (ncomp[k] < 2) {
+			hs.probs.push_back(sub[k]);
+			hs.owner.push_back(k);
+		}
+	if (!hs.ncrop) return SIMPOIS_OK;
+	// device layout: labels of the split channels, the crops' buffers, the table
+	Layout lo;
+	std::vector<size_t> loff(n, 0), coff(comps.size());
+	std::vector<CropDev> tab(comps.size());
+	for (int k = 0; k < n; k++)
+		if (ncomp[k] >= 2) loff[k] = lo.take(sizeof(int) * labels[k].size());
+	for (size_t c = 0; c < comps.size(); c++) {
+		const Comp &q = comps[c];
+		const MgProblem &ch = sub[q.ch];
+		CropDev &d = tab[c];
+		d.x0 = std::max(0, q.bx0 * HB - 2);
+		d.y0 = std::max(0, q.by0 * HB - 2);
+		d.cw = std::min(ch.w, (q.bx1 + 1) * HB + 2) - d.x0;
+		d.ch = std::min(ch.h, (q.by1 + 1) * HB + 2) - d.y0;
+		d.w = ch.w;
+		d.bw = bws[q.ch];
+		d.comp = q.id;
+		const size_t px = (size_t)d.cw * d.ch;
+		coff[c] = lo.take(px * sizeof(float) * (ch.f ? 3 : 2));
+	}
+	const size_t otab = lo.take(sizeof(CropDev) * comps.size());
+	if (lo.off > ctx->split_cap) {
+		if (ctx->split) {
+			cudaStreamSynchronize(s);
+			cudaFree(ctx->split);
+			ctx->split = nullptr;
+			ctx->split_cap = 0;
+		}
+		const size_t cap = lo.off + lo.off / 8;
+		if (cudaMalloc((void **)&ctx->split, cap) != cudaSuccess) {
+			cudaGetLastError();
+			return ctx_fail(ctx, SIMPOIS_ENOMEM, "cannot allocate %zu bytes of device memory", cap);
+		}
+		ctx->split_cap = cap;
+	}
+	char *B = ctx->split;
+	for (int k = 0; k < n; k++) {
+		if (ncomp[k] < 2) continue;
+		SP_CUDA(ctx, cudaMemcpyAsync(B + loff[k], labels[k].data(), sizeof(int) * labels[k].size(),
+				cudaMemcpyHostToDevice, s));
+		// the known pixels of the output; the crops fill in the unknowns
+		SP_CUDA(ctx, cudaMemcpyAsync(sub[k].out, sub[k].g, sizeof(float) * sub[k].w * sub[k].h,
+				cudaMemcpyDeviceToDevice, s));
+	}
+	size_t most = 1;
+	for (size_t c = 0; c < comps.size(); c++) {
+		const MgProblem &ch = sub[comps[c].ch];
+		CropDev &d = tab[c];
+		const size_t px = (size_t)d.cw * d.ch;
+		d.g = ch.g;
+		d.f = ch.f;
+		d.out = ch.out;
+		d.label = (const int *)(B + loff[comps[c].ch]);
+		d.cg = (float *)(B + coff[c]);
+		d.cout = d.cg + px;
+		d.cf = ch.f ? d.cout + px : nullptr;
+		most = std::max(most, px);
+		MgProblem q = ch;
+		q.g = d.cg;
+		q.f = d.cf;
+		q.out = d.cout;
+		q.w = d.cw;
+		q.h = d.ch;
+		hs.probs.push_back(q);
+		hs.owner.push_back(comps[c].ch);
+	}
+	hs.table = (CropDev *)(B + otab);
+	SP_CUDA(ctx, cudaMemcpyAsync(hs.table, tab.data(), sizeof(CropDev) * tab.size(), cudaMemcpyHostToDevice, s));
+	hs.gx = (unsigned)std::min<size_t>(256, (most + 255) / 256);
+	k_crop_gather<<<dim3(hs.gx, hs.ncrop), 256, 0, s>>>(hs.table);
+	ctx->launches++;
+	SP_LAUNCH_CHECK(ctx);
+	return SIMPOIS_OK;
+}
+
+// After the solve: the crops' unknowns into their channels' outputs, and one
+// report per channel: the worst status, the largest iteration and refinement
+// counts, the summed unknowns, and the channel's relative residual from its
+// crops' (|r|^2 = sum |r_k|^2, |b|^2 = sum |b_k|^2); the residual of the float
+// output, when asked for, is computed again on the whole channel.
+static int split_finish(simpois_ctx *ctx, const HoleSplit &hs, const std::vector<simpois_report> &r,
+		const std::vector<double> &bn2, const std::vector<MgProblem> &sub, simpois_report *out)
+{
+	const int n = (int)sub.size();
+	if (hs.ncrop) {
+		k_crop_scatter<<<dim3(hs.gx, hs.ncrop), 256, 0, ctx->stream>>>(hs.table);
+		ctx->launches++;
+		SP_LAUNCH_CHECK(ctx);
+	}
+	std::vector<int> parts(n, 0);
+	std::vector<double> rr(n, 0.0), bb(n, 0.0);
+	for (size_t q = 0; q < hs.probs.size(); q++) {
+		const int c = hs.owner[q];
+		simpois_report &o = out[c];
+		const simpois_report &a = r[q];
+		rr[c] += a.rel_residual * a.rel_residual * bn2[q];
+		bb[c] += bn2[q];
+		if (!parts[c]++) {
+			o = a;
+			continue;
+		}
+		if (a.status != SIMPOIS_OK && (o.status == SIMPOIS_OK || a.status == SIMPOIS_SINGULAR)) o.status = a.status;
+		o.unknowns += a.unknowns;
+		o.iterations = std::max(o.iterations, a.iterations);
+		o.refinements = std::max(o.refinements, a.refinements);
+	}
+	std::vector<MgProblem> again;
+	std::vector<int> which;
+	for (int c = 0; c < n; c++) {
+		if (parts[c] < 2) continue;
+		out[c].rel_residual = bb[c] > 0 ? sqrt(rr[c] / bb[c]) : 0.0;
+		if (out[c].rel_residual_out >= 0) {
+			again.push_back(sub[c]);
+			which.push_back(c);
+		}
+	}
+	if (!again.empty()) {
+		std::vector<const float *> u(again.size());
+		std::vector<double> rel(again.size()), bn(again.size());
+		for (size_t k = 0; k < again.size(); k++) u[k] = again[k].out;
+		const int rc = mg_residual(ctx, again.data(), u.data(), (int)again.size(), rel.data(), bn.data());
+		if (rc) return rc;
+		for (size_t k = 0; k < again.size(); k++) out[which[k]].rel_residual_out = rel[k];
+	}
+	return SIMPOIS_OK;
+}
+
 int run_converged(simpois_ctx *ctx, const simpois_image *im, int n, const simpois_params *p,
 		simpois_report *rep, int tune = 0, int *tuned_cm = nullptr, int *tuned_nu = nullptr)
 {
@@ -364,9 +651,19 @@ int run_converged(simpois_ctx *ctx, const simpois_image *im, int n, const simpoi
 				where.push_back((int)q);
 			}
 		if (sub.empty()) continue;
-		std::vector<simpois_report> r(sub.size());
 		MgOptions o = opt;
 		const std::string key = tune_key(sub, kind, opt);
+		// biharmonic channels: each hole component its own problem
+		HoleSplit hs;
+		const bool split = kind == 1 && o.fused && o.use_mg && split_enabled();
+		if (split) {
+			if ((rc = split_holes(ctx, sub, hs))) return rc;
+		} else {
+			hs.probs = sub;
+			for (size_t q = 0; q < sub.size(); q++) hs.owner.push_back((int)q);
+		}
+		std::vector<simpois_report> r(hs.probs.size());
+		std::vector<double> bn2(hs.probs.size(), 0.0);
 		const bool tunable = o.fused && o.use_mg && !o.ktimer;
 		if (ctx->coarse_max_fixed > 0) o.coarse_max = ctx->coarse_max_fixed;
 		if (ctx->sweeps_fixed > 0) o.nu = ctx->sweeps_fixed;
@@ -376,7 +673,7 @@ int run_converged(simpois_ctx *ctx, const simpois_image *im, int n, const simpoi
 		const bool tuning = tune && tunable && (tune_cm || tune_nu) && !known;
 		if (tuning) {
 			int bc = 0, bn = 0;
-			rc = tune_and_solve(ctx, sub, o, r.data(), tune_cm, tune_nu, &bc, &bn);
+			rc = tune_and_solve(ctx, hs.probs, o, r.data(), bn2.data(), tune_cm, tune_nu, &bc, &bn);
 			if (rc) return rc;
 			ctx->tuned[key] = {bc, bn};
 			o.coarse_max = bc;
@@ -388,13 +685,15 @@ int run_converged(simpois_ctx *ctx, const simpois_image *im, int n, const simpoi
 				if (tune_cm) o.coarse_max = it->second.coarse_max;
 				if (tune_nu) o.nu = it->second.nu;
 			}
-			rc = mg_solve(ctx, sub.data(), (int)sub.size(), o, r.data());
+			rc = mg_solve(ctx, hs.probs.data(), (int)hs.probs.size(), o, r.data(), bn2.data());
 			if (rc) return rc;
 		}
+		std::vector<simpois_report> rs(sub.size());
+		if ((rc = split_finish(ctx, hs, r, bn2, sub, rs.data()))) return rc;
 		if (tuned_cm && (kind == 0 || tuned_cm[0] == 0))
 			tuned_cm[0] = o.coarse_max > 0 ? o.coarse_max : mg_default_coarse_max();
 		if (tuned_nu && (kind == 0 || tuned_nu[0] == 0)) tuned_nu[0] = o.nu > 0 ? o.nu : 2;
-		for (size_t q = 0; q < sub.size(); q++) rep[where[q]] = r[q];
+		for (size_t q = 0; q < sub.size(); q++) rep[where[q]] = rs[q];
 	}
 	// singular channels: the reference schedule, as the reference would run them
 	for (size_t q = 0; q < probs.size(); q++) {
@@ -507,6 +806,7 @@ int simpois_destroy(simpois_ctx *ctx)
 	cudaStreamSynchronize(ctx->stream);
 	if (ctx->arena) cudaFree(ctx->arena);
 	if (ctx->io) cudaFree(ctx->io);
+	if (ctx->split) cudaFree(ctx->split);
 	if (ctx->pinned) cudaFreeHost(ctx->pinned);
 	if (ctx->lists_host) cudaFreeHost(ctx->lists_host);
 	if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);

@@ -37,6 +37,9 @@ struct simpois_ctx {
 	// staging for the host-pointer entry point
 	char *io = nullptr;
 	size_t io_cap = 0;
+	// the hole components of split biharmonic channels: labels, crops, table
+	char *split = nullptr;
+	size_t split_cap = 0;
 	// its second stream (the output's known pixels go back while the solve
 	// runs) and the events that order it with `stream`
 	cudaStream_t aux_stream = nullptr;

@@ -3068,7 +3068,7 @@ std::string plan_signature(const simpois_ctx *ctx, const Plan &pl, int K, int fu
 	snprintf(buf, sizeof buf, "%p/%d/%d/%d/%d/%d/%d/%d/%d/%d|", (void *)ctx->arena, pl.n, K, (int)fused,
 			pl.nfine_max, pl.nlev_max, pl.coarse_smem, opt.use_mg, pl.pdl, pl.nu);
 	sig += buf;
-	const int ng = fused == MODE_FUSED5 ? pl.ngroups : 1;
+	const int ng = fused == MODE_FUSED5 || fused == MODE_BIH64 ? pl.ngroups : 1;
 	for (int g = 0; g < ng && ng > 1; g++) {
 		snprintf(buf, sizeof buf, "g%d:%d+%d:%d|", g, pl.gp0[g], pl.gpn[g], pl.gnfine[g]);
 		sig += buf;
@@ -3168,7 +3168,7 @@ cudaError_t add_solve_loops(cudaGraph_t G, cudaStream_t cs, Plan &pl, const MgOp
 }
 
 // Build the whole converged solve as one graph: per problem group (one group
-// unless the fused 5-point batch was split), two nested device-side WHILE
+// unless the fused batch was split), two nested device-side WHILE
 // loops -- refinement steps (k_resid64, first V-cycle, the PCG loop, U += x)
 // while a problem of the group is still refining, and PCG iterations while a
 // problem's inner solve runs.  The groups' loops are independent branches, so
@@ -3183,7 +3183,7 @@ cudaError_t build_solve_graph(simpois_ctx *ctx, Plan &pl, const MgOptions &opt, 
 	cudaError_t e = cudaGraphCreate(&G, 0);
 	if (e != cudaSuccess) return e;
 	const long long n0 = *pl.nl;
-	const int ng = mode == MODE_FUSED5 ? pl.ngroups : 1;
+	const int ng = mode == MODE_FUSED5 || mode == MODE_BIH64 ? pl.ngroups : 1;
 	long long no[GMAX] = {}, ni[GMAX] = {};
 	for (int g = 0; g < ng && e == cudaSuccess; g++) {
 		if (ng > 1) {
@@ -3410,7 +3410,8 @@ int mg_handover_level(int w, int h, int coarse_max)
 
 int mg_default_coarse_max() { return default_coarse_max(); }
 
-int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &opt, simpois_report *rep)
+int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &opt, simpois_report *rep,
+		double *bnorm2)
 {
 	if (n <= 0) return SIMPOIS_OK;
 	cudaStream_t s = ctx->stream;
@@ -3716,7 +3717,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	SP_CUDA(ctx, cudaMemcpyAsync(hn, pl.dnact, sizeof(int) * MAXLEV, cudaMemcpyDeviceToHost, s));
 	int *hpc = (int *)stage;   // the uploads above are done with the staging by now (stream order)
 	const bool grouped = n > 1 && groups_max() > 1 && opt.use_graph && !opt.ktimer && !verbose() && opt.use_mg &&
-			pl.fused && K == 0;
+			pl.fused;
 	if (grouped)
 		SP_CUDA(ctx, cudaMemcpyAsync(hpc, pl.pcnt, sizeof(int) * MAXLEV * n, cudaMemcpyDeviceToHost, s));
 	SP_CUDA(ctx, cudaStreamSynchronize(s));
@@ -3822,6 +3823,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 		rep[k].refinements = hs[k].outer;
 		rep[k].rel_residual = hs[k].rel;
 		rep[k].rel_residual_out = -1;
+		if (bnorm2) bnorm2[k] = hs[k].bnorm2;
 	}
 	if (opt.out_resid && opt.mode == MG_FILL) {
 		std::vector<const float *> u(n);

@@ -43,9 +43,10 @@ struct MgOptions {
 	float *const *grad_dat = nullptr;
 };
 
-// Batched converged solve of n problems; rep receives n records.
+// Batched converged solve of n problems; rep receives n records and bnorm2,
+// when given, each problem's |b|^2 (the denominator of its relative residual).
 int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &opt,
-		simpois_report *rep);
+		simpois_report *rep, double *bnorm2 = nullptr);
 
 // Number of levels of a w x h problem that the fused V-cycle runs in the tile
 // kernels for hand-over size coarse_max (0: the default).
