@@ -337,7 +337,6 @@ static int tune_write(simpois_ctx *ctx)
 // crops of |r_k|^2 <= rtol^2 |b_k|^2.
 constexpr int HB = 8;   // block side of the component map
 constexpr int SPLIT_MAX = 256;   // most components a channel is split into
-constexpr size_t SPLIT_TOTAL = 2048;   // and a batch
 
 __global__ void k_block_any(const float *__restrict__ g, int w, int h, int bw, uint8_t *__restrict__ out)
 {
@@ -393,14 +392,15 @@ struct HoleSplit {
 	unsigned gx = 1;                // blocks per crop of the gather and scatter
 };
 
-// SIMPOIS_SPLIT=0: biharmonic channels are solved whole
-static bool split_enabled()
+// Which operators' channels are split: SIMPOIS_SPLIT=0 none, 1 the
+// biharmonic (the default), 2 both.
+static bool split_enabled(int kind)
 {
-	static bool v = [] {
+	static int v = [] {
 		const char *e = getenv("SIMPOIS_SPLIT");
-		return !(e && atoi(e) == 0);
+		return e ? atoi(e) : 1;
 	}();
-	return v;
+	return v >= 2 || (v == 1 && kind == 1);
 }
 
 // Split the channels of `sub` (one operator kind) into hole components;
@@ -463,8 +463,9 @@ static int split_holes(simpois_ctx *ctx, const std::vector<MgProblem> &sub, Hole
 			comps.push_back(c);
 		}
 		// one component (or none), or so many that the problems' overheads
-		// would outweigh the retirements: solved whole
-		if (ncomp[k] < 2 || ncomp[k] > SPLIT_MAX || comps.size() > SPLIT_TOTAL) {
+		// would outweigh the retirements: solved whole (decided per channel,
+		// so a channel's bits do not depend on the rest of the batch)
+		if (ncomp[k] < 2 || ncomp[k] > SPLIT_MAX) {
 			comps.resize(first);
 			ncomp[k] = 1;
 		}
@@ -547,8 +548,10 @@ static int split_holes(simpois_ctx *ctx, const std::vector<MgProblem> &sub, Hole
 	hs.table = (CropDev *)(B + otab);
 	SP_CUDA(ctx, cudaMemcpyAsync(hs.table, tab.data(), sizeof(CropDev) * tab.size(), cudaMemcpyHostToDevice, s));
 	hs.gx = (unsigned)std::min<size_t>(256, (most + 255) / 256);
-	k_crop_gather<<<dim3(hs.gx, hs.ncrop), 256, 0, s>>>(hs.table);
-	ctx->launches++;
+	for (int c0 = 0; c0 < hs.ncrop; c0 += 65535) {   // the grid's y extent
+		k_crop_gather<<<dim3(hs.gx, std::min(65535, hs.ncrop - c0)), 256, 0, s>>>(hs.table + c0);
+		ctx->launches++;
+	}
 	SP_LAUNCH_CHECK(ctx);
 	return SIMPOIS_OK;
 }
@@ -562,11 +565,11 @@ static int split_finish(simpois_ctx *ctx, const HoleSplit &hs, const std::vector
 		const std::vector<double> &bn2, const std::vector<MgProblem> &sub, simpois_report *out)
 {
 	const int n = (int)sub.size();
-	if (hs.ncrop) {
-		k_crop_scatter<<<dim3(hs.gx, hs.ncrop), 256, 0, ctx->stream>>>(hs.table);
+	for (int c0 = 0; c0 < hs.ncrop; c0 += 65535) {
+		k_crop_scatter<<<dim3(hs.gx, std::min(65535, hs.ncrop - c0)), 256, 0, ctx->stream>>>(hs.table + c0);
 		ctx->launches++;
-		SP_LAUNCH_CHECK(ctx);
 	}
+	SP_LAUNCH_CHECK(ctx);
 	std::vector<int> parts(n, 0);
 	std::vector<double> rr(n, 0.0), bb(n, 0.0);
 	for (size_t q = 0; q < hs.probs.size(); q++) {
@@ -655,7 +658,7 @@ int run_converged(simpois_ctx *ctx, const simpois_image *im, int n, const simpoi
 		const std::string key = tune_key(sub, kind, opt);
 		// biharmonic channels: each hole component its own problem
 		HoleSplit hs;
-		const bool split = kind == 1 && o.fused && o.use_mg && split_enabled();
+		const bool split = o.fused && o.use_mg && split_enabled(kind);
 		if (split) {
 			if ((rc = split_holes(ctx, sub, hs))) return rc;
 		} else {

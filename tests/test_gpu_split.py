@@ -67,3 +67,21 @@ def test_split_solves_repeat_bit_for_bit(sp):
     b, rb = sp.solve(gt, None, tstep=-0.08, rtol=1e-6)
     assert ra == rb
     assert torch.equal(a.view(torch.int32), b.view(torch.int32))
+
+
+def test_a_channel_splits_the_same_in_a_batch(sp):
+    """Whether and how a channel is split depends on the channel alone: in a
+    batch with other biharmonic images it gives the bits it gives alone."""
+    from imscript_gb300 import synth
+    rng = np.random.default_rng(29)
+    h, w = 260, 400
+    imgs = []
+    for k in range(3):
+        g = synth.gaussian_field(rng, h, w, 12).astype(np.float32)
+        g[_holes(rng, h, w) if k != 1 else synth.disk_mask(rng, h, w, 0.2, rmin=3, rmax=12)] = np.nan
+        imgs.append(torch.from_numpy(g[None]).cuda())
+    outs, reps = sp.solve_batch([(g, None, -0.08) for g in imgs], rtol=1e-6)
+    for k, g in enumerate(imgs):
+        one, r1 = sp.solve(g, None, tstep=-0.08, rtol=1e-6)
+        assert r1[0] == reps[k]
+        assert torch.equal(one.view(torch.int32), outs[k].view(torch.int32)), k
