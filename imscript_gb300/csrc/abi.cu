@@ -338,13 +338,29 @@ static int tune_write(simpois_ctx *ctx)
 constexpr int HB = 8;   // block side of the component map
 constexpr int SPLIT_MAX = 256;   // most components a channel is split into
 
-__global__ void k_block_any(const float *__restrict__ g, int w, int h, int bw, uint8_t *__restrict__ out)
+// The block map: a thread per 8-pixel row of a block (two 16-byte loads when
+// the image and its width keep rows aligned), the 8 rows of a block in 8
+// consecutive lanes.
+__global__ void k_block_any(const float *__restrict__ g, int w, int h, int bw, int nb, uint8_t *__restrict__ out)
 {
-	const int bx = blockIdx.x % bw, by = blockIdx.x / bw;
-	const int x = bx * HB + (threadIdx.x & 7), y = by * HB + (threadIdx.x >> 3);
-	const bool u = x < w && y < h && isnan(g[(size_t)y * w + x]);
-	const int any = __syncthreads_or(u);
-	if (threadIdx.x == 0) out[blockIdx.x] = (uint8_t)(any != 0);
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	const int b = t >> 3, r = t & 7;
+	bool u = false;
+	if (b < nb) {
+		const int bx = b % bw, by = b / bw, x = bx * HB, y = by * HB + r;
+		if (y < h) {
+			const float *row = g + (size_t)y * w + x;
+			if ((w & 3) == 0 && ((uintptr_t)g & 15) == 0 && x + HB <= w) {
+				const float4 a = *(const float4 *)row, c = *(const float4 *)(row + 4);
+				u = isnan(a.x) || isnan(a.y) || isnan(a.z) || isnan(a.w) || isnan(c.x) || isnan(c.y) ||
+						isnan(c.z) || isnan(c.w);
+			} else {
+				for (int k = 0; k < HB && x + k < w; k++) u = u || isnan(row[k]);
+			}
+		}
+	}
+	const unsigned any = __ballot_sync(0xffffffffu, u);
+	if (r == 0 && b < nb) out[b] = (uint8_t)(((any >> (threadIdx.x & 24)) & 0xffu) != 0);
 }
 
 struct CropDev {
@@ -421,8 +437,9 @@ static int split_holes(simpois_ctx *ctx, const std::vector<MgProblem> &sub, Hole
 	if (rc) return rc;
 	uint8_t *maps = (uint8_t *)ctx->pinned;   // written by the kernel straight into page-locked memory
 	for (int k = 0; k < n; k++) {
-		k_block_any<<<(unsigned)(moff[k + 1] - moff[k]), HB * HB, 0, s>>>(sub[k].g, sub[k].w, sub[k].h, bws[k],
-				maps + moff[k]);
+		const int nb = (int)(moff[k + 1] - moff[k]);
+		k_block_any<<<(unsigned)((8 * (size_t)nb + 255) / 256), 256, 0, s>>>(sub[k].g, sub[k].w, sub[k].h, bws[k],
+				nb, maps + moff[k]);
 		ctx->launches++;
 	}
 	SP_LAUNCH_CHECK(ctx);
