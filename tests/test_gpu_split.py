@@ -85,3 +85,37 @@ def test_a_channel_splits_the_same_in_a_batch(sp):
         one, r1 = sp.solve(g, None, tstep=-0.08, rtol=1e-6)
         assert r1[0] == reps[k]
         assert torch.equal(one.view(torch.int32), outs[k].view(torch.int32)), k
+
+
+def test_data_term_and_many_components(sp):
+    """A biharmonic image with a data term is split like one without (the
+    crops carry their part of f); a channel with more than 256 hole
+    components is solved whole; both within 1e-4 of the FP64 solve."""
+    from imscript_gb300 import synth
+    from oracle import fp64
+    rng = np.random.default_rng(41)
+    cases = []
+    h, w = 260, 400
+    g = synth.gaussian_field(rng, h, w, 10).astype(np.float32)
+    f = (0.01 * synth.gaussian_field(rng, h, w, 10)).astype(np.float32)
+    m = _holes(rng, h, w)
+    cases.append((g, f, m))
+    # 400 single-pixel holes 20 pixels apart (no two in touching 8 x 8 blocks)
+    # and a rectangle: more components than a channel is split into
+    h, w = 400, 400
+    g = synth.gaussian_field(rng, h, w, 10).astype(np.float32)
+    m = np.zeros((h, w), bool)
+    m[5::20, 5::20] = True
+    m[100:140, 100:160] = True
+    cases.append((g, None, m))
+    for g, f, m in cases:
+        g = g.copy()
+        g[m] = np.nan
+        gt = torch.from_numpy(g[None]).cuda()
+        ft = None if f is None else torch.from_numpy(f[None]).cuda()
+        out, reps = sp.solve(gt, ft, tstep=-0.08, rtol=1e-8)
+        assert reps[0]["status"] == 0 and reps[0]["unknowns"] == int(m.sum()), reps
+        o = out[0].cpu().numpy()
+        x = fp64.solve(g, f, 1)
+        err = np.abs(o[m] - x[m]).max() / np.abs(x[m]).max()
+        assert err <= 1e-4, err
