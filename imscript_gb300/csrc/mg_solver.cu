@@ -718,6 +718,45 @@ __global__ void k_resid64(const ProbDev *__restrict__ P, ProbState *st, const in
 		const size_t k = in ? (size_t)j * w + i : 0;
 		const uint8_t m = in ? L.mask[k] : 0;
 		double rk = 0;
+		if (first) {
+			// U is 0 at every unknown: r = rhs_sign*rhs - A_UK g_K, the known
+			// neighbours' weighted values (exact products of small integer
+			// weights and floats) summed in float-float -- no FP64 operation,
+			// which issues at a small fraction of the FP32 rate on this GPU,
+			// until U holds a solution
+			if (m) {
+				FF acc = {pr.rhs ? pr.rhs_sign * pr.rhs[k] : 0.f, 0.f};   // exact sign flip
+				if (!pr.known_zero) {
+					if (K == 0) {
+						const int qi[4] = {i + 1 < w ? i + 1 : i, i, i > 0 ? i - 1 : i, i};
+						const int qj[4] = {j, j + 1 < h ? j + 1 : j, j, j > 0 ? j - 1 : j};
+#pragma unroll
+						for (int e = 0; e < 4; e++) {
+							const size_t q = (size_t)qj[e] * w + qi[e];
+							if (!L.mask[q]) acc = ff_add(acc, FF{pr.g[q], 0.f});
+						}
+					} else {
+#pragma unroll
+						for (int e = 0; e < 12; e++) {
+							const size_t q = (size_t)clampi(j + c_dj13[e], h) * w + clampi(i + c_di13[e], w);
+							if (!L.mask[q]) ff_add_prod(acc, -c_cf13[e], pr.g[q]);
+						}
+					}
+				}
+				const float rf = acc.hi;   // acc is normalised: hi is the float nearest hi + lo
+				if (pr.r64) {
+					pr.r64[k] = (double)acc.hi + (double)acc.lo;
+					L.b[k] = rf;
+					pr.x[k] = rf;
+				} else {
+					L.b[k] = rf;
+					pr.x[k] = 0.f;
+					pr.xlo[k] = 0.f;
+				}
+				ff_add_prod(rr, rf, rf);
+			}
+			continue;
+		}
 		if (K == 0 && m) {
 			const int ie = i + 1 < w ? i + 1 : i, iw = i > 0 ? i - 1 : i;
 			const int js = j + 1 < h ? j + 1 : j, jn = j > 0 ? j - 1 : j;
