@@ -608,7 +608,7 @@ def run_ours(args):
         "higher_is_better": True,
         "scaling": "strong" if (args.shard and world > 1) else "weak",
         "vs_baseline": None,
-        "dtype": "f32 (FP64 refinement and reductions)",
+        "dtype": "f32 (float-float refinement and dot products; FP64 Krylov vectors for the 13-point operator)",
         "data": "synthetic (seeded; shapes and distributions of the benchmark workload)",
         "config": bench_config(args, sets),
         "plain": {"value": round(value_plain, 3), "unit": "filled Mpx/s", "ms_per_step": ms_plain / args.steps,

@@ -1,5 +1,6 @@
 // mg_solver.cu -- the converged schedule: batched multigrid-preconditioned
-// conjugate gradient in FP32 inside an FP64 iterative refinement.
+// conjugate gradient in FP32 inside an iterative refinement carried in
+// float-float (5-point) or FP64 (13-point).
 //
 // Problem.  For every channel of every image, the unknowns U are the NaN
 // pixels of g.  The system is the one the reference's CG solves
@@ -7,13 +8,15 @@
 // cleant_cgpois.c:67-89) or the 13-point bilaplacian with a single clamp
 // (kind 1, cleant_cgpois.c:91-121), restricted to U, and b = -f_U - A_UK g_K.
 //
-// Refinement (FP64).  The solution of the unknowns lives in FP64 (U; known
-// pixels are read from g).  Each refinement step computes r = b - A u in
-// FP64 and its norm (the FP64 relative residual reported to the caller),
-// stops when it is <= rtol, otherwise solves A d = (float)r and adds d in
-// FP64.  FP64 issues at about 1/70 of the FP32 rate on this GPU, so it is
-// spent only there: the FP32 PCG's dot products sum their per-pixel terms as
-// float-float pairs and go to double once per warp.
+// Refinement.  The solution of the unknowns lives in U (known pixels are read
+// from g): float-float pairs (~48 bits) for the 5-point operator, FP64 for the
+// 13-point one.  Each refinement step computes r = b - A u in that precision
+// (the 5-point one in difference form) and its norm (the relative residual
+// reported to the caller), stops when it is <= rtol, otherwise solves
+// A d = (float)r and adds d.  FP64 issues at a small fraction of the FP32
+// rate on this GPU, so it is spent only where float-float is not enough: the
+// FP32 PCG's dot products sum their per-pixel terms as float-float pairs and
+// go to double once per block; the first step (U = 0) needs no FP64 at all.
 //
 // Inner solve, 5-point (FP32).  Preconditioned CG; the preconditioner is one
 // V(2,2)-cycle of geometric multigrid on the masked grid:
@@ -108,8 +111,9 @@ struct ProbDev {
 	int vec4;            // w % 4 == 0 and g, out 16-byte aligned: setup and
 	                     // finalize move 4-pixel groups with vector accesses
 	float *out;
-	double *U;           // FP64 solution at the unknown pixels (the known ones
-	                     // are read from g: see known_at)
+	double *U;           // the solution at the unknown pixels (the known ones
+	                     // are read from g): FP64 for the 13-point operator,
+	                     // float-float pairs (hi, lo) for the 5-point one (uff)
 	float *x, *p, *q;    // level-0 PCG vectors
 	float *xlo;          // x is carried as x + xlo (float-float): an FP32 x
 	                     // alone cannot hold a solution much larger than the
@@ -127,6 +131,20 @@ struct ProbDev {
 	// z and the cell codes), planned on the host
 	int coff_b[MAXLEV], coff_z[MAXLEV], coff_m[MAXLEV];
 };
+
+// The 5-point solution as float-float pairs: its refinement residual, the
+// iterate update and the output then take no FP64 operation, which issues at
+// a small fraction of the FP32 rate on this GPU; 48 bits hold the solution
+// far below any residual the refinement is asked for.
+__device__ __forceinline__ float2 *uff(const ProbDev &pr) { return reinterpret_cast<float2 *>(pr.U); }
+
+// a - b for float-float values: the high parts' difference exact (TwoSum),
+// the low parts' rounded once
+__device__ __forceinline__ FF ff_sub(FF a, FF b)
+{
+	const FF s = ff_two_sum(a.hi, -b.hi);
+	return ff_norm(s.hi, __fadd_rn(s.lo, __fsub_rn(a.lo, b.lo)));
+}
 
 struct ProbState {
 	double bnorm2, rho, alpha, beta, rr, tau2, rel, rel_first;
@@ -758,15 +776,34 @@ __global__ void k_resid64(const ProbDev *__restrict__ P, ProbState *st, const in
 			continue;
 		}
 		if (K == 0 && m) {
-			const int ie = i + 1 < w ? i + 1 : i, iw = i > 0 ? i - 1 : i;
-			const int js = j + 1 < h ? j + 1 : j, jn = j > 0 ? j - 1 : j;
-			const double uc = pr.U[k];
-			const double ue = known_at(pr.U, L.mask, pr.g, pr.known_zero, (size_t)j * w + ie);
-			const double us = known_at(pr.U, L.mask, pr.g, pr.known_zero, (size_t)js * w + i);
-			const double uw = known_at(pr.U, L.mask, pr.g, pr.known_zero, (size_t)j * w + iw);
-			const double un = known_at(pr.U, L.mask, pr.g, pr.known_zero, (size_t)jn * w + i);
-			const double s = pr.rhs ? (double)(pr.rhs_sign * pr.rhs[k]) : 0.0;   // exact sign flip
-			rk = s - (fma(4.0, uc, -ue) - us - uw - un);
+			// float-float, in difference form: r = s + sum over the in-image
+			// neighbours of (u_n - u_c) (a neighbour clamped onto the pixel
+			// adds 0), u_n the solution or the known value
+			const float2 *U2 = uff(pr);
+			const FF uc = {U2[k].x, U2[k].y};
+			const int qi[4] = {i + 1 < w ? i + 1 : i, i, i > 0 ? i - 1 : i, i};
+			const int qj[4] = {j, j + 1 < h ? j + 1 : j, j, j > 0 ? j - 1 : j};
+			FF acc = {0.f, 0.f};
+#pragma unroll
+			for (int e = 0; e < 4; e++) {
+				const size_t q = (size_t)qj[e] * w + qi[e];
+				if (q == k) continue;
+				FF un = {0.f, 0.f};
+				if (L.mask[q]) {
+					const float2 v = U2[q];
+					un = FF{v.x, v.y};
+				} else if (!pr.known_zero) {
+					un = FF{pr.g[q], 0.f};
+				}
+				acc = ff_add(acc, ff_sub(un, uc));
+			}
+			const FF r = ff_add(FF{pr.rhs ? pr.rhs_sign * pr.rhs[k] : 0.f, 0.f}, acc);   // exact sign flip
+			const float rf = r.hi;
+			L.b[k] = rf;
+			pr.x[k] = 0.f;
+			pr.xlo[k] = 0.f;
+			ff_add_prod(rr, rf, rf);
+			continue;
 		} else if (m) {
 			const double s = pr.rhs ? (double)(pr.rhs_sign * pr.rhs[k]) : 0.0;
 			rk = s - apply64<K>(pr.U, L.mask, pr.g, pr.known_zero, w, h, i, j);
@@ -868,7 +905,14 @@ __global__ void k_uadd(const ProbDev *__restrict__ P, const ProbState *__restric
 		int j = tile_j(t, r);
 		if (i < pr.w && j < pr.h) {
 			size_t k = (size_t)j * pr.w + i;
-			if (pr.lv[0].mask[k]) pr.U[k] += (double)pr.x[k] + (double)pr.xlo[k];
+			if (!pr.lv[0].mask[k]) continue;
+			if (pr.kind == 0) {
+				float2 &u = uff(pr)[k];
+				const FF v = ff_add(FF{u.x, u.y}, FF{pr.x[k], pr.xlo[k]});
+				u = make_float2(v.hi, v.lo);
+			} else {
+				pr.U[k] += (double)pr.x[k] + (double)pr.xlo[k];
+			}
 		}
 	}
 }
@@ -2673,8 +2717,9 @@ __global__ void __launch_bounds__(SP_THREADS) k_finalize(const ProbDev *__restri
 		const ProbDev &pr = P[tt[q].x];
 		float v[4];
 #pragma unroll
-		for (int e = 0; e < 4; e++)   // U is read (and converted) at the unknowns only
-			v[e] = ((mw[q] >> (8 * e)) & 1u) ? (float)pr.U[kk[q] + e] : gv[q][e];
+		for (int e = 0; e < 4; e++)   // U is read (and rounded) at the unknowns only
+			v[e] = ((mw[q] >> (8 * e)) & 1u) ? (pr.kind == 0 ? uff(pr)[kk[q] + e].x : (float)pr.U[kk[q] + e])
+					: gv[q][e];
 		if (nv[q] == 4 && pr.vec4)
 			*(float4 *)(pr.out + kk[q]) = make_float4(v[0], v[1], v[2], v[3]);
 		else
@@ -2700,20 +2745,21 @@ __global__ void k_adjoint_scatter(const ProbDev *__restrict__ P, const int4 *__r
 			const int j = tile_j(t, r);
 			if (i >= w || j >= h) continue;
 			const size_t k = (size_t)j * w + i;
+			const float2 *U2 = uff(pr);   // the adjoint is of the 5-point fill
 			if (m[k]) {
 				gin[t.x][k] = 0.f;
-				if (gdat[t.x]) gdat[t.x][k] = -(float)pr.U[k];
+				if (gdat[t.x]) gdat[t.x][k] = -U2[k].x;
 				continue;
 			}
 			const bool e = i + 1 < w && m[k + 1], wn = i > 0 && m[k - 1];
 			const bool sn = j + 1 < h && m[k + w], nn = j > 0 && m[k - w];
-			if (e || wn || sn || nn) {   // FP64 only next to an unknown
-				double s = gout[t.x][k];
-				if (e) s += pr.U[k + 1];
-				if (wn) s += pr.U[k - 1];
-				if (sn) s += pr.U[k + w];
-				if (nn) s += pr.U[k - w];
-				gin[t.x][k] = (float)s;
+			if (e || wn || sn || nn) {   // float-float sums only next to an unknown
+				FF s = {gout[t.x][k], 0.f};
+				if (e) s = ff_add(s, FF{U2[k + 1].x, U2[k + 1].y});
+				if (wn) s = ff_add(s, FF{U2[k - 1].x, U2[k - 1].y});
+				if (sn) s = ff_add(s, FF{U2[k + w].x, U2[k + w].y});
+				if (nn) s = ff_add(s, FF{U2[k - w].x, U2[k - w].y});
+				gin[t.x][k] = s.hi;
 			} else {
 				gin[t.x][k] = gout[t.x][k];   // (float)(double)v == v
 			}
