@@ -908,17 +908,31 @@ struct IoImg {
 	unsigned blk0;       // first block
 };
 
-// The image of block blockIdx.x: the last one whose first block is at or
-// below it (images without blocks share the next one's blk0).
-__device__ __forceinline__ const IoImg &io_image(const IoImg *__restrict__ im, int n)
+// The image of chunk b: the last one whose first chunk is at or below it
+// (images without chunks share the next one's blk0).
+__device__ __forceinline__ const IoImg &io_image(const IoImg *__restrict__ im, int n, unsigned b = blockIdx.x)
 {
 	int lo = 0, hi = n - 1;
 	while (lo < hi) {
 		const int mid = (lo + hi + 1) >> 1;
-		if (im[mid].blk0 <= blockIdx.x) lo = mid;
+		if (im[mid].blk0 <= b) lo = mid;
 		else hi = mid - 1;
 	}
 	return im[lo];
+}
+
+// The outputs' known pixels -- the inputs' -- straight into the page-locked
+// host outputs, while the solve runs: one launch for the whole batch instead
+// of a copy per image; one block per two SMs (the host link, not the SMs,
+// sets the pace; the solve keeps the rest) strides over the chunks.
+__global__ void k_put_known_batch(const IoImg *__restrict__ im, int n, unsigned ch, unsigned nblk)
+{
+	for (unsigned b = blockIdx.x; b < nblk; b += gridDim.x) {
+		const IoImg &m = io_image(im, n, b);
+		if (!m.dst) continue;
+		const size_t beg = (size_t)(b - m.blk0) * ch, end = min(beg + ch, m.n4);
+		for (size_t i = beg + threadIdx.x; i < end; i += blockDim.x) m.dst[i] = m.g[i];
+	}
 }
 
 __global__ void k_fetch_rhs_batch(const IoImg *__restrict__ im, int n, unsigned ch)
@@ -1137,6 +1151,24 @@ int simpois_solve_batch_host(simpois_ctx *ctx, const simpois_image *images, int 
 		total += im.dat ? slot : 0;
 		off[3 * k + 2] = total;
 		total += slot;
+	}
+	const size_t o_tab = total;
+	total += may_direct ? 2 * sizeof(IoImg) * (size_t)n : 0;
+	int rc = ctx_io_reserve(ctx, total > 0 ? total : 256);
+	if (rc) return rc;
+	cudaStream_t s = ctx->stream;
+	std::vector<simpois_image> dev(images, images + n);
+	// the inputs first: the pointer checks below run while they move
+	for (int k = 0; k < n; k++) {
+		const size_t bytes = (size_t)images[k].w * images[k].h * images[k].pd * sizeof(float);
+		dev[k].in = (const float *)(ctx->io + off[3 * k]);
+		dev[k].dat = images[k].dat ? (const float *)(ctx->io + off[3 * k + 1]) : nullptr;
+		dev[k].out = (float *)(ctx->io + off[3 * k + 2]);
+		SP_CUDA(ctx, cudaMemcpyAsync((void *)dev[k].in, images[k].in, bytes, cudaMemcpyHostToDevice, s));
+	}
+	for (int k = 0; k < n; k++) {
+		const simpois_image &im = images[k];
+		const size_t np = (size_t)im.w * im.h * im.pd;
 		if (may_direct && (im.rtol > 0 || p.rtol > 0) && np % 4 == 0) {
 			const float4 *hd = im.dat ? (const float4 *)direct_ptr(im.dat) : nullptr;
 			float4 *ho = (float4 *)direct_ptr(im.out);
@@ -1149,19 +1181,9 @@ int simpois_solve_batch_host(simpois_ctx *ctx, const simpois_image *images, int 
 			}
 		}
 	}
-	const size_t o_tab = total;
-	total += ndir ? 2 * sizeof(IoImg) * (size_t)n : 0;
-	int rc = ctx_io_reserve(ctx, total > 0 ? total : 256);
-	if (rc) return rc;
-	cudaStream_t s = ctx->stream;
-	std::vector<simpois_image> dev(images, images + n);
 	size_t n4tot = 0;
 	for (int k = 0; k < n; k++) {
 		const size_t bytes = (size_t)images[k].w * images[k].h * images[k].pd * sizeof(float);
-		dev[k].in = (const float *)(ctx->io + off[3 * k]);
-		dev[k].dat = images[k].dat ? (const float *)(ctx->io + off[3 * k + 1]) : nullptr;
-		dev[k].out = (float *)(ctx->io + off[3 * k + 2]);
-		SP_CUDA(ctx, cudaMemcpyAsync((void *)dev[k].in, images[k].in, bytes, cudaMemcpyHostToDevice, s));
 		if (images[k].dat && !dir[k])
 			SP_CUDA(ctx, cudaMemcpyAsync((void *)dev[k].dat, images[k].dat, bytes, cudaMemcpyHostToDevice, s));
 		if (dir[k]) {
@@ -1207,11 +1229,10 @@ int simpois_solve_batch_host(simpois_ctx *ctx, const simpois_image *images, int 
 			SP_CUDA(ctx, cudaEventRecord(ctx->ev_rhs, ctx->aux_stream));
 			ctx->rhs_pending = ctx->ev_rhs;
 		}
-		for (int k = 0; k < n; k++) {
-			if (!dir[k]) continue;
-			const size_t bytes = (size_t)images[k].w * images[k].h * images[k].pd * sizeof(float);
-			SP_CUDA(ctx, cudaMemcpyAsync(images[k].out, dev[k].in, bytes, cudaMemcpyDeviceToHost, ctx->aux_stream));
-		}
+		k_put_known_batch<<<(unsigned)std::min<size_t>(nblk, (size_t)std::max(1, ctx->sm_count / 2)), 256, 0,
+				ctx->aux_stream>>>(dput, n, (unsigned)ch, (unsigned)nblk);
+		ctx->launches++;
+		SP_LAUNCH_CHECK(ctx);
 		SP_CUDA(ctx, cudaEventRecord(ctx->ev_out, ctx->aux_stream));
 	}
 	const int st = solve_batch(ctx, dev.data(), n, params, reports, 0, nullptr);
