@@ -921,20 +921,6 @@ __device__ __forceinline__ const IoImg &io_image(const IoImg *__restrict__ im, i
 	return im[lo];
 }
 
-// The outputs' known pixels -- the inputs' -- straight into the page-locked
-// host outputs, while the solve runs: one launch for the whole batch instead
-// of a copy per image; one block per two SMs (the host link, not the SMs,
-// sets the pace; the solve keeps the rest) strides over the chunks.
-__global__ void k_put_known_batch(const IoImg *__restrict__ im, int n, unsigned ch, unsigned nblk)
-{
-	for (unsigned b = blockIdx.x; b < nblk; b += gridDim.x) {
-		const IoImg &m = io_image(im, n, b);
-		if (!m.dst) continue;
-		const size_t beg = (size_t)(b - m.blk0) * ch, end = min(beg + ch, m.n4);
-		for (size_t i = beg + threadIdx.x; i < end; i += blockDim.x) m.dst[i] = m.g[i];
-	}
-}
-
 __global__ void k_fetch_rhs_batch(const IoImg *__restrict__ im, int n, unsigned ch)
 {
 	const IoImg &m = io_image(im, n);
@@ -1229,10 +1215,13 @@ int simpois_solve_batch_host(simpois_ctx *ctx, const simpois_image *images, int 
 			SP_CUDA(ctx, cudaEventRecord(ctx->ev_rhs, ctx->aux_stream));
 			ctx->rhs_pending = ctx->ev_rhs;
 		}
-		k_put_known_batch<<<(unsigned)std::min<size_t>(nblk, (size_t)std::max(1, ctx->sm_count / 2)), 256, 0,
-				ctx->aux_stream>>>(dput, n, (unsigned)ch, (unsigned)nblk);
-		ctx->launches++;
-		SP_LAUNCH_CHECK(ctx);
+		// (copies on the copy engines: a kernel writing them competes with the
+		// solve's kernels for the SMs and loses the overlap)
+		for (int k = 0; k < n; k++) {
+			if (!dir[k]) continue;
+			const size_t bytes = (size_t)images[k].w * images[k].h * images[k].pd * sizeof(float);
+			SP_CUDA(ctx, cudaMemcpyAsync(images[k].out, dev[k].in, bytes, cudaMemcpyDeviceToHost, ctx->aux_stream));
+		}
 		SP_CUDA(ctx, cudaEventRecord(ctx->ev_out, ctx->aux_stream));
 	}
 	const int st = solve_batch(ctx, dev.data(), n, params, reports, 0, nullptr);
