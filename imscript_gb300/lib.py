@@ -50,6 +50,17 @@ class Report(ctypes.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+def report_dicts(reps, n=None):
+    """The first n records of a Report array as dicts (as Report.as_dict),
+    read through one numpy view: a batch's hundreds of records convert in a
+    fraction of the per-field ctypes reads."""
+    import numpy as np
+    n = len(reps) if n is None else n
+    rows = np.frombuffer(reps, dtype=REPORT_DTYPE, count=n).tolist()
+    return [{"status": a, "unknowns": b, "iterations": c, "refinements": d, "rel_residual": e,
+             "rel_residual_out": f} for a, b, c, d, e, f in rows]
+
+
 class Image(ctypes.Structure):
     _fields_ = [
         ("inp", ctypes.c_void_p),
@@ -61,6 +72,30 @@ class Image(ctypes.Structure):
         ("tstep", ctypes.c_float),
         ("rtol", ctypes.c_double),
     ]
+
+
+def _np_dtypes():
+    import numpy as np
+    img = np.dtype([("inp", np.uint64), ("dat", np.uint64), ("out", np.uint64), ("w", np.int32),
+                    ("h", np.int32), ("pd", np.int32), ("tstep", np.float32), ("rtol", np.float64)], align=True)
+    rep = np.dtype([("status", np.int32), ("unknowns", np.int32), ("iterations", np.int32),
+                    ("refinements", np.int32), ("rel_residual", np.float64), ("rel_residual_out", np.float64)],
+                   align=True)
+    assert img.itemsize == ctypes.sizeof(Image) and rep.itemsize == ctypes.sizeof(Report)
+    return img, rep
+
+
+# numpy views of simpois_image and simpois_report (the batch entry points fill
+# and read hundreds of them per call)
+IMAGE_DTYPE, REPORT_DTYPE = _np_dtypes()
+
+
+def image_array(rows):
+    """A simpois_image array from (in, dat, out, w, h, pd, tstep, rtol) rows
+    (pointers as ints, 0 for none); returns (numpy array, ctypes pointer)."""
+    import numpy as np
+    a = np.array(rows, dtype=IMAGE_DTYPE)
+    return a, a.ctypes.data_as(ctypes.POINTER(Image))
 
 
 # every symbol include/simpois_gpu.h declares

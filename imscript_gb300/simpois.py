@@ -140,21 +140,21 @@ def solve_batch_host(images, *, rtol=1e-6, tstep=0.25, max_iter=0, flags=0, allo
         items.append((g, f, t))
     if outs is None:
         outs = [np.empty_like(g) for g, _, _ in items]
-    arr = (_lib.Image * len(items))()
+    rows = []
     total = 0
     for k, (g, f, t) in enumerate(items):
         pd, h, w = _shape3(g)
         if outs[k].shape != g.shape or outs[k].dtype != np.float32 or not outs[k].flags.c_contiguous:
             raise ValueError(f"output {k} must match image {k}")
-        arr[k] = _lib.Image(g.ctypes.data, f.ctypes.data if f is not None else None, outs[k].ctypes.data,
-                            w, h, pd, float(t), float(rtol))
+        rows.append((g.ctypes.data, f.ctypes.data if f is not None else 0, outs[k].ctypes.data, w, h, pd, t, rtol))
         total += pd
+    keep, arr = _lib.image_array(rows)
     reps = (_lib.Report * max(1, total))()
     prm = _lib.default_params(rtol=float(rtol), max_iter=int(max_iter), flags=int(flags), tstep=float(tstep))
     ctx = context(device)
     rc = _lib.load().simpois_solve_batch_host(ctx.handle, arr, len(items), ctypes.byref(prm), reps)
     ctx.check(rc, allow)
-    return outs, [reps[k].as_dict() for k in range(total)]
+    return outs, _lib.report_dicts(reps, total)
 
 
 def autotune(images, *, rtol=1e-6, tstep=0.25, max_iter=0, flags=0, allow=(_lib.OK,), outs=None):
@@ -186,13 +186,13 @@ def _batch(images, rtol, tstep, max_iter, flags, allow, outs, tune):
         return [], [], None
     dev = items[0][0].device
     outs = [torch.empty_like(g) for g, _, _ in items] if outs is None else outs
-    arr = (_lib.Image * len(items))()
+    rows = []
     total = 0
     for k, (g, f, t) in enumerate(items):
         pd, h, w = _shape3(g)
-        arr[k] = _lib.Image(g.data_ptr(), f.data_ptr() if f is not None else None,
-                            outs[k].data_ptr(), w, h, pd, float(t), float(rtol))
+        rows.append((g.data_ptr(), f.data_ptr() if f is not None else 0, outs[k].data_ptr(), w, h, pd, t, rtol))
         total += pd
+    keep, arr = _lib.image_array(rows)
     reps = (_lib.Report * total)()
     prm = _lib.default_params(rtol=float(rtol), max_iter=int(max_iter), flags=int(flags),
                               tstep=float(tstep))
@@ -206,7 +206,7 @@ def _batch(images, rtol, tstep, max_iter, flags, allow, outs, tune):
     else:
         rc = _lib.load().simpois_solve_batch(ctx.handle, arr, len(items), ctypes.byref(prm), reps)
     ctx.check(rc, allow)
-    return outs, [r.as_dict() for r in reps], tuned
+    return outs, _lib.report_dicts(reps), tuned
 
 
 def residual(u, g, f=None, kind=0):
