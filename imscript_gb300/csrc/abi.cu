@@ -828,7 +828,6 @@ int simpois_destroy(simpois_ctx *ctx)
 	if (ctx->io) cudaFree(ctx->io);
 	if (ctx->split) cudaFree(ctx->split);
 	if (ctx->pinned) cudaFreeHost(ctx->pinned);
-	if (ctx->lists_host) cudaFreeHost(ctx->lists_host);
 	if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
 	if (ctx->aux_stream) cudaStreamDestroy(ctx->aux_stream);
 	if (ctx->ev_in) cudaEventDestroy(ctx->ev_in);

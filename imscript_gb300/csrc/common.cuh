@@ -49,11 +49,6 @@ struct simpois_ctx {
 	// does not read f)
 	cudaEvent_t rhs_pending = nullptr;
 
-	// the solver's tile lists (every level's, problem after problem) for the
-	// last sequence of problem sizes, page-locked: uploaded with one copy
-	std::string lists_key;
-	int4 *lists_host = nullptr;
-	size_t lists_cap = 0;
 
 	// kernel launches issued (graph replays count their kernel nodes)
 	long long launches = 0;

@@ -443,6 +443,30 @@ __device__ __forceinline__ int group_of(const ProbDev &pr, int4 t, size_t &k)
 	return min(4, pr.w - i);
 }
 
+// The tile lists of every level, problem after problem, tiles in row order:
+// entry e of level l (lbeg[l] <= e < lbeg[l + 1]) is tile e - lbeg[l] - off[k]
+// of the last problem k whose first entry off[k] (loff, n + 1 per level) is at
+// or below it (problems without the level share the next one's offset).
+__global__ void k_fill_lists(const ProbDev *__restrict__ P, int n, int nlev, const int *__restrict__ lbeg,
+		const int *__restrict__ loff, int4 *__restrict__ lists)
+{
+	const int total = lbeg[nlev];
+	for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+		int l = 0;
+		while (lbeg[l + 1] <= e) l++;
+		const int *o = loff + (size_t)l * (n + 1);
+		const int r = e - lbeg[l];
+		int lo = 0, hi = n - 1;
+		while (lo < hi) {
+			const int mid = (lo + hi + 1) >> 1;
+			if (o[mid] <= r) lo = mid;
+			else hi = mid - 1;
+		}
+		const int t = r - o[lo], tw = (P[lo].lv[l].w + SP_TILE - 1) / SP_TILE;
+		lists[e] = make_int4(lo, t % tw, t / tw, 0);
+	}
+}
+
 // Level 0 over all tiles: mask = isnan(g); U = 0 at the unknowns; flag =
 // tile holds an unknown; per-problem pixel counts.
 __global__ void __launch_bounds__(SP_THREADS) k_setup0(const ProbDev *__restrict__ P, ProbState *st,
@@ -3512,7 +3536,6 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	std::vector<size_t> off_U(n), off_x(n), off_xlo(n), off_p(n), off_q(n), off_p2(n), off_balt(n);
 	std::vector<size_t> off_r64(n, 0), off_p64(n, 0), off_p64b(n, 0), off_q64(n, 0);
 	size_t ntl[MAXLEV] = {};   // tiles per level over all problems
-	std::string lkey;          // the problem sizes, which alone decide the tile lists
 	const int cmax = opt.coarse_max > 0 ? clamp_coarse_max(opt.coarse_max) : default_coarse_max();
 	for (int k = 0; k < n; k++) {
 		const MgProblem &q = probs[k];
@@ -3539,7 +3562,6 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 			off_z2[l].push_back(Lo.take(px * 4));
 			ntl[l] += (size_t)ntiles(lh[l]) * ntiles(lw[l]);
 		}
-		lkey += std::to_string(q.w) + "x" + std::to_string(q.h) + ",";
 		for (int l = nl; l < MAXLEV; l++) {
 			off_mask[l].push_back(0);
 			off_code[l].push_back(0);
@@ -3594,6 +3616,7 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	const size_t t_dnact = Tl.take(sizeof(int) * MAXLEV, 16), t_dall = Tl.take(sizeof(int4 *) * MAXLEV, 16);
 	const size_t t_dact = Tl.take(sizeof(int4 *) * MAXLEV, 16), t_dflag = Tl.take(sizeof(int *) * MAXLEV, 16);
 	const size_t t_tbeg = Tl.take(sizeof(int) * n, 16), t_tcnt = Tl.take(sizeof(int) * n, 16);
+	const size_t t_loff = Tl.take(sizeof(int) * (MAXLEV * ((size_t)n + 1) + MAXLEV + 1), 16);
 	const size_t tab_bytes = (Tl.off + 15) / 16 * 16;
 	const size_t o_tab = Lo.take(tab_bytes);
 	const size_t o_dp = o_tab + t_dp, o_st = o_tab + t_st, o_gl = o_tab + t_gl, o_pcnt = o_tab + t_pcnt;
@@ -3744,39 +3767,28 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 		memcpy(tab + t_dflag, pl.flag, sizeof(int *) * MAXLEV);
 		int *tb = (int *)(tab + t_tbeg);
 		for (int k = 0; k < n; k++) tb[k] = INT_MAX;
+		// the tile lists' layout: every level's first entry, then per level
+		// each problem's first entry within it (a problem without the level
+		// has none)
+		int *lb = (int *)(tab + t_loff), *lo = lb + MAXLEV + 1;
+		for (int l = 0; l <= MAXLEV; l++) lb[l] = (int)lbeg[std::min(l, pl.nlev_max)];
+		for (int l = 0; l < pl.nlev_max; l++) {
+			int *o = lo + (size_t)l * (n + 1);
+			o[0] = 0;
+			for (int k = 0; k < n; k++)
+				o[k + 1] = o[k] + (l < hp[k].nlev ? ntiles(hp[k].lv[l].w) * ntiles(hp[k].lv[l].h) : 0);
+		}
 		SP_CUDA(ctx, cudaMemcpyAsync(A + o_tab, tab, tab_bytes, cudaMemcpyHostToDevice, s));
 	}
 	if (nmaps) SP_CUDA(ctx, put(A + o_tmap, maps.data(), sizeof(CUtensorMap) * nmaps));
-	// the tile lists, problem after problem in every level: rebuilt only when
-	// the sequence of problem sizes changes (the previous call's copy from
-	// this buffer completed before it returned)
+	// the tile lists, problem after problem in every level, written on the device
 	const size_t nlist = lbeg[pl.nlev_max];
-	if (ctx->lists_key != lkey || !ctx->lists_host) {
-		ctx->lists_key.clear();
-		if (nlist > ctx->lists_cap) {
-			if (ctx->lists_host) cudaFreeHost(ctx->lists_host);
-			ctx->lists_host = nullptr;
-			ctx->lists_cap = 0;
-			if (cudaMallocHost((void **)&ctx->lists_host, sizeof(int4) * nlist) != cudaSuccess) {
-				cudaGetLastError();
-				return ctx_fail(ctx, SIMPOIS_ENOMEM, "cannot allocate %zu bytes of pinned memory",
-						sizeof(int4) * nlist);
-			}
-			ctx->lists_cap = nlist;
-		}
-		for (int l = 0; l < pl.nlev_max; l++) {
-			int4 *o = ctx->lists_host + lbeg[l];
-			for (int k = 0; k < n; k++) {
-				const int tw = ntiles(hp[k].lv[l].w), th = ntiles(hp[k].lv[l].h);
-				if (l >= hp[k].nlev) continue;
-				for (int ty = 0; ty < th; ty++)
-					for (int tx = 0; tx < tw; tx++) *o++ = make_int4(k, tx, ty, 0);
-			}
-		}
-		ctx->lists_key = lkey;
+	if (nlist) {
+		const int *dlb = (const int *)(A + o_tab + t_loff);
+		k_fill_lists<<<(unsigned)std::min<size_t>((nlist + 255) / 256, 8 * (size_t)std::max(1, ctx->sm_count)), 256,
+				0, s>>>(pl.dp, n, pl.nlev_max, dlb, dlb + MAXLEV + 1, (int4 *)(A + o_lists));
+		++*pl.nl;
 	}
-	if (nlist)
-		SP_CUDA(ctx, cudaMemcpyAsync(A + o_lists, ctx->lists_host, sizeof(int4) * nlist, cudaMemcpyHostToDevice, s));
 
 	if (opt.mode == MG_ADJOINT) {
 		pl.gout = (const float **)(A + o_gptr);
