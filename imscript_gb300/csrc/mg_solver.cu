@@ -57,8 +57,9 @@
 // independent branch with its own two nested device-driven WHILE loops
 // (refinement steps, PCG iterations) over its slices of the tile lists, so
 // one group's latency-bound coarse levels overlap another's fine ones.  The
-// graph is captured once per plan and replayed; the tile lists are kept per
-// sequence of problem sizes, the small tables go up in one copy.
+// graph is captured once per plan (a new plan of the same topology updates it
+// in place) and replayed; the small tables go up in one copy, and the tile
+// lists of every level are written on the device from per-problem offsets.
 //
 // Launches.  The V-cycle kernels use programmatic dependent launch: each
 // waits (griddepcontrol.wait) before its first dependent access and any early
