@@ -2516,7 +2516,9 @@ __global__ void __launch_bounds__(SP_THREADS) k_pspmv13(const ProbDev *__restric
 	__shared__ __align__(16) double sp[RW * RH];
 	__shared__ __align__(16) float sz[RW * RH];
 	__shared__ __align__(16) uint8_t sc[RW * RH];
-	__shared__ uint16_t lreg[RW * RH], lown[SP_TILE * SP_TILE];
+	__shared__ uint16_t lreg[RW * RH], lown[SP_TILE * SP_TILE], lnb[RW * RH];
+	__shared__ __align__(16) double sy[RW * RH];   // inner tiles: y = L p at the cells in lnb
+	__shared__ __align__(16) uint8_t fnb[RW * RH];
 	__shared__ double sh[32];
 	__shared__ int sw[SP_THREADS / 32];
 	const int4 t = tl[blockIdx.x];
@@ -2585,6 +2587,49 @@ __global__ void __launch_bounds__(SP_THREADS) k_pspmv13(const ProbDev *__restric
 #pragma unroll
 	for (int e = 0; e < 4; e++)
 		if ((mown >> (8 * e)) & 1u) lown[offo++] = (uint16_t)(cown + e);
+	// A tile 2 or more pixels from every image side applies the 13-point
+	// operator as L L (L = 4 - the 4 neighbours: L^2 has the weights 20, -8,
+	// 2, 1 of the 13 points): y = L p on the tile's unknowns and their 4
+	// neighbours (p is 0 at the known pixels, so y there is what the 13-point
+	// sum reads through them), then q = L y -- 8 FP64 operations an unknown
+	// and 4 a ring cell instead of 13.  Near a side the single clamp of the
+	// 13-point operator differs from composing clamped 5-point ones, so those
+	// tiles take the 13 points.
+	const bool inner = t.y * SP_TILE >= 2 && t.y * SP_TILE + SP_TILE + 2 <= w && t.z * SP_TILE >= 2 &&
+			t.z * SP_TILE + SP_TILE + 2 <= h;
+	int nn = 0;
+	if (inner) {
+#pragma unroll
+		for (int it = 0; it < NV; it++) {
+			const int f = threadIdx.x + it * SP_THREADS;
+			if (f < NG) *(uint32_t *)(fnb + 4 * f) = 0u;
+		}
+		__syncthreads();
+#pragma unroll
+		for (int e = 0; e < 4; e++)
+			if ((mown >> (8 * e)) & 1u) {
+				const int c = cown + e;
+				fnb[c] = fnb[c + 1] = fnb[c - 1] = fnb[c + RW] = fnb[c - RW] = 1;
+			}
+		__syncthreads();
+		int cnt = 0;
+#pragma unroll
+		for (int it = 0; it < NV; it++) {
+			const int f = threadIdx.x + it * SP_THREADS;
+			if (f < NG) cnt += __popc(*(const uint32_t *)(fnb + 4 * f));
+		}
+		int offn = block_scan(cnt, sw, &nn);
+#pragma unroll
+		for (int it = 0; it < NV; it++) {
+			const int f = threadIdx.x + it * SP_THREADS;
+			if (f < NG) {
+				const uint32_t m = *(const uint32_t *)(fnb + 4 * f);
+#pragma unroll
+				for (int e = 0; e < 4; e++)
+					if ((m >> (8 * e)) & 1u) lnb[offn++] = (uint16_t)(4 * f + e);
+			}
+		}
+	}
 	grid_wait();
 	grid_release();
 	if (!st[prob].inner_active) return;
@@ -2595,8 +2640,13 @@ __global__ void __launch_bounds__(SP_THREADS) k_pspmv13(const ProbDev *__restric
 		sp[c] = beta != 0 ? fma(beta, sp[c], (double)sz[c]) : (double)sz[c];
 	}
 	__syncthreads();
-	const bool inner = t.y * SP_TILE >= 2 && t.y * SP_TILE + SP_TILE + 2 <= w && t.z * SP_TILE >= 2 &&
-			t.z * SP_TILE + SP_TILE + 2 <= h;
+	if (inner) {
+		for (int k = threadIdx.x; k < nn; k += SP_THREADS) {
+			const int c = lnb[k];
+			sy[c] = fma(4.0, sp[c], -(((sp[c + 1] + sp[c - 1]) + sp[c + RW]) + sp[c - RW]));
+		}
+		__syncthreads();
+	}
 	constexpr int DI[12] = {1, 0, -1, 0, 1, 1, -1, -1, 2, 0, -2, 0};
 	constexpr int DJ[12] = {0, 1, 0, -1, 1, -1, 1, -1, 0, 2, 0, -2};
 	constexpr double CF[12] = {-8, -8, -8, -8, 2, 2, 2, 2, 1, 1, 1, 1};
@@ -2605,18 +2655,18 @@ __global__ void __launch_bounds__(SP_THREADS) k_pspmv13(const ProbDev *__restric
 		const int c = lown[k];
 		const int ry = c / RW, rx = c - ry * RW, i = x0 + rx, j = y0 + ry;
 		const double pk = sp[c];
-		double off = 0.0;
+		double qk;
 		if (inner) {
-#pragma unroll
-			for (int s2 = 0; s2 < 12; s2++) off = fma(CF[s2], sp[c + DJ[s2] * RW + DI[s2]], off);
+			qk = fma(4.0, sy[c], -(((sy[c + 1] + sy[c - 1]) + sy[c + RW]) + sy[c - RW]));
 		} else {
+			double off = 0.0;
 #pragma unroll
 			for (int s2 = 0; s2 < 12; s2++) {
 				const int qi = clampi(i + DI[s2], w), qj = clampi(j + DJ[s2], h);
 				off = fma(CF[s2], sp[(qj - y0) * RW + (qi - x0)], off);
 			}
+			qk = fma(20.0, pk, off);
 		}
-		const double qk = fma(20.0, pk, off);
 		pq = fma(pk, qk, pq);
 		const size_t g = (size_t)j * w + i;   // p and q are read at the unknowns only
 		pnew[g] = pk;
