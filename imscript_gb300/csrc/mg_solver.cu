@@ -733,6 +733,117 @@ __global__ void k_compact(const int4 *const *__restrict__ all, const int *const 
 
 // ------------------------------------------------------------------ refinement kernels
 
+// The end of a refinement residual pass: |r|^2 summed over the problem's
+// tiles; the problem's last tile decides: converged, or start an inner solve.
+__device__ void resid_finish(FF rr, bool first, const ProbDev &pr, int prob, ProbState *st,
+		const int *__restrict__ tbeg, const int *__restrict__ tcnt, double *partial, Globals *gl, double *sh)
+{
+	double tot[2];
+	if (problem_sum1_ff(rr, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
+		ProbState &s = st[prob];
+		if (first) s.bnorm2 = tot[0];
+		if (first && s.nknown == 0) s.status = SIMPOIS_SINGULAR;
+		double rel = s.bnorm2 > 0 ? sqrt(tot[0] / s.bnorm2) : 0.0;
+		if (first) s.rel_first = rel;
+		s.rel = rel;
+		bool ok = rel <= pr.rtol;
+		if (ok || !isfinite(rel) || s.outer >= MAX_OUTER || s.total_iter >= s.max_iter ||
+				s.status != SIMPOIS_OK) {
+			s.outer_active = 0;
+			s.inner_active = 0;
+			if (s.status == SIMPOIS_OK && !ok) s.status = SIMPOIS_NOT_CONVERGED;
+			atomicSub(&gl->outer_count, 1);
+		} else {
+			s.outer += 1;
+			s.iter = 0;
+			s.inner_active = 1;
+			// an FP32 inner solve stalls near TAU_MIN; the FP64 one goes to rtol
+			double tau = pr.r64 ? 0.5 * pr.rtol / rel : fmax(0.3 * pr.rtol / rel, pr.tau_min);
+			s.tau2 = tau * tau * tot[0];
+			s.rho = 0;
+			s.beta = 0;
+			s.beta_f = (float)s.beta;
+			s.pending = 0;
+			atomicAdd(&gl->inner_count, 1);
+		}
+	}
+}
+
+// The 5-point refinement residual, one tile per block: the solution's values on
+// the tile and a 1-pixel halo go to shared memory first, as float-float pairs
+// (U at the unknowns -- 0 on the first step, before any solve --, the known
+// value, or 0 for the adjoint; nothing outside the image), so each pixel reads
+// its neighbours there instead of testing and loading each from global
+// memory.  Per unknown, in difference form: r = s + sum over the in-image
+// neighbours (E, S, W, N) of (u_n - u_c); b0 = (float) r, x = xlo = 0.
+__global__ void __launch_bounds__(SP_THREADS, 8) k_resid5(const ProbDev *__restrict__ P, ProbState *st,
+		const int4 *__restrict__ tl, const int *__restrict__ tbeg, const int *__restrict__ tcnt, double *partial,
+		Globals *gl)
+{
+	constexpr int RW = SP_TILE + 2, RN = RW * RW;   // region: 34 x 34
+	constexpr int NIT = (RN + SP_THREADS - 1) / SP_THREADS;
+	__shared__ float2 sv[RN];
+	__shared__ uint8_t sm[RN];
+	__shared__ double sh[32];
+	const int4 t = tl[blockIdx.x];
+	const int prob = t.x;
+	if (!st[prob].outer_active) return;
+	// the first refinement step also forms ||b||; every block of the problem
+	// reads `outer` before the problem's last block changes it
+	const bool first = st[prob].outer == 0;
+	const ProbDev &pr = P[prob];
+	const LevelDev &L = pr.lv[0];
+	const int w = pr.w, h = pr.h, x0 = t.y * SP_TILE - 1, y0 = t.z * SP_TILE - 1;
+	const float2 *U2 = uff(pr);
+	// every mask byte of the thread's region cells first, then every value:
+	// two round trips to memory, not two per cell
+	size_t qv[NIT];
+	uint8_t mv[NIT];
+#pragma unroll
+	for (int it = 0; it < NIT; it++) {
+		const int c = threadIdx.x + it * SP_THREADS;
+		const int ry = c / RW, rx = c - ry * RW, gi = x0 + rx, gj = y0 + ry;
+		const bool in = c < RN && gi >= 0 && gi < w && gj >= 0 && gj < h;
+		qv[it] = in ? (size_t)gj * w + gi : 0;
+		mv[it] = in ? (uint8_t)(L.mask[qv[it]] ? 1 : 2) : 0;   // 1 unknown, 2 known, 0 outside
+	}
+#pragma unroll
+	for (int it = 0; it < NIT; it++) {
+		const int c = threadIdx.x + it * SP_THREADS;
+		float2 v = make_float2(0.f, 0.f);
+		if (mv[it] == 1 && !first) v = U2[qv[it]];
+		else if (mv[it] == 2 && !pr.known_zero) v.x = pr.g[qv[it]];
+		if (c < RN) {
+			sv[c] = v;
+			sm[c] = mv[it] == 1;
+		}
+	}
+	__syncthreads();
+	const int i = tile_i(t);
+	FF rr = {0.f, 0.f};   // |r|^2 from the float r
+#pragma unroll
+	for (int r = 0; r < SP_ROWS; r++) {
+		const int j = tile_j(t, r);
+		if (i >= w || j >= h) continue;
+		const size_t k = (size_t)j * w + i;
+		const int c = (j - y0) * RW + (i - x0);
+		if (!sm[c]) continue;
+		const FF uc = {sv[c].x, sv[c].y};
+		FF acc = {0.f, 0.f};
+		if (i + 1 < w) acc = ff_add(acc, ff_sub(FF{sv[c + 1].x, sv[c + 1].y}, uc));
+		if (j + 1 < h) acc = ff_add(acc, ff_sub(FF{sv[c + RW].x, sv[c + RW].y}, uc));
+		if (i > 0) acc = ff_add(acc, ff_sub(FF{sv[c - 1].x, sv[c - 1].y}, uc));
+		if (j > 0) acc = ff_add(acc, ff_sub(FF{sv[c - RW].x, sv[c - RW].y}, uc));
+		const FF rv = ff_add(FF{pr.rhs ? pr.rhs_sign * pr.rhs[k] : 0.f, 0.f}, acc);   // exact sign flip
+		const float rf = rv.hi;   // normalised: hi is the float nearest hi + lo
+		L.b[k] = rf;
+		pr.x[k] = 0.f;
+		pr.xlo[k] = 0.f;
+		ff_add_prod(rr, rf, rf);
+	}
+	resid_finish(rr, first, pr, prob, st, tbeg, tcnt, partial, gl, sh);
+}
+
 // r = rhs_sign*rhs - A U (FP64) at the unknowns; b0 = (float)r; x = 0 (the
 // biharmonic PCG: r64 = r and b0).
 // The last tile of a problem decides: converged, or start an inner solve.
@@ -847,35 +958,7 @@ __global__ void k_resid64(const ProbDev *__restrict__ P, ProbState *st, const in
 			ff_add_prod(rr, rf, rf);
 		}
 	}
-	double tot[2];
-	if (problem_sum1_ff(rr, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
-		ProbState &s = st[prob];
-		if (first) s.bnorm2 = tot[0];
-		if (first && s.nknown == 0) s.status = SIMPOIS_SINGULAR;
-		double rel = s.bnorm2 > 0 ? sqrt(tot[0] / s.bnorm2) : 0.0;
-		if (first) s.rel_first = rel;
-		s.rel = rel;
-		bool ok = rel <= pr.rtol;
-		if (ok || !isfinite(rel) || s.outer >= MAX_OUTER || s.total_iter >= s.max_iter ||
-				s.status != SIMPOIS_OK) {
-			s.outer_active = 0;
-			s.inner_active = 0;
-			if (s.status == SIMPOIS_OK && !ok) s.status = SIMPOIS_NOT_CONVERGED;
-			atomicSub(&gl->outer_count, 1);
-		} else {
-			s.outer += 1;
-			s.iter = 0;
-			s.inner_active = 1;
-			// an FP32 inner solve stalls near TAU_MIN; the FP64 one goes to rtol
-			double tau = pr.r64 ? 0.5 * pr.rtol / rel : fmax(0.3 * pr.rtol / rel, pr.tau_min);
-			s.tau2 = tau * tau * tot[0];
-			s.rho = 0;
-			s.beta = 0;
-			s.beta_f = (float)s.beta;
-			s.pending = 0;
-			atomicAdd(&gl->inner_count, 1);
-		}
-	}
+	resid_finish(rr, first, pr, prob, st, tbeg, tcnt, partial, gl, sh);
 }
 
 // After compaction: a problem without unknowns is finished before it starts;
@@ -3122,6 +3205,18 @@ void kt_refresh(const Plan &pl, cudaStream_t s)
 	for (int p = 0; p < pl.n; p++) pl.kt->active[p] = h[p].inner_active != 0;
 }
 
+// The refinement residual: the region-staged 5-point kernel, or the 13-point
+// one (FP64).
+template <int K>
+void launch_resid(const Plan &pl, int nt, cudaStream_t s)
+{
+	if constexpr (K == 0)
+		k_resid5<<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl);
+	else
+		k_resid64<K><<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl);
+	++*pl.nl;
+}
+
 // pcg = 0: the cycle is half of the biharmonic preconditioner and leaves the
 // 5-point PCG scalars alone.  step: the cycle follows k_spmv5 (whose search
 // direction is p2 when use_p2), so level 0 first takes the pending PCG step;
@@ -3278,8 +3373,7 @@ cudaError_t add_solve_loops(cudaGraph_t G, cudaStream_t cs, Plan &pl, const MgOp
 			cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
 	cudaError_t ce = cudaGraphConditionalHandleCreate(&hi, body_o, 0, cudaGraphCondAssignDefault);
 	long long c0 = *pl.nl;
-	k_resid64<K><<<nt, SP_THREADS, 0, cs>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial, pl.gl);
-	++*pl.nl;
+	launch_resid<K>(pl, nt, cs);
 	if (mode == MODE_FUSED5) {
 		launch_vcycle_fused(pl, cs);
 	} else if (mode == MODE_BIH64) {
@@ -3453,9 +3547,8 @@ int run_kind(simpois_ctx *ctx, Plan &pl, const MgOptions &opt)
 		}
 		{
 			KT_BEGIN(pl, s);
-			k_resid64<K><<<nt, SP_THREADS, 0, s>>>(pl.dp, pl.dst, pl.act[0], pl.tbeg, pl.tcnt, pl.partial,
-					pl.gl); ++*pl.nl;
-			KT_END(pl, s, "k_resid64", pl.kt->px(0) * BPX_RESID64);
+			launch_resid<K>(pl, nt, s);
+			KT_END(pl, s, K == 0 ? "k_resid5" : "k_resid64", pl.kt->px(0) * BPX_RESID64);
 		}
 		if (fused) {
 			launch_vcycle_fused(pl, s);

@@ -182,7 +182,7 @@ def test_kernel_timer_replay_is_identical(sp):
     b, rb = sp.solve(g, f, rtol=1e-6, flags=lib.FLAG_KTIMER)
     assert torch.equal(a.view(torch.int32), b.view(torch.int32))
     st = ctx.kernel_stats()
-    for name in ("k_pre5", "k_post5", "k_coarse5", "k_spmv5", "k_resid64"):
+    for name in ("k_pre5", "k_post5", "k_coarse5", "k_spmv5", "k_resid5"):
         assert st[name]["launches"] > 0 and st[name]["ms"] > 0 and st[name]["bytes"] > 0, name
 
 
