@@ -2427,11 +2427,32 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_spmv5(const ProbDev *__restri
 			gstore4(pr.q, k, n, vec, make_float4(qk[0], qk[1], qk[2], qk[3]));
 		}
 	}
-	double tot[2];
-	if (problem_sum1_ff(pq, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
+	// the tile's p.q; k_alpha5 sums the problem's tiles (a block here does not
+	// wait for an atomic to learn whether it is the problem's last)
+	const double s0 = block_sum_ff<SP_THREADS>(pq, sh);
+	if (threadIdx.x == 0) partial[2 * blockIdx.x] = s0;
+}
+
+// alpha = rho / (p.q) per problem, p.q summed over the problem's level-0 tile
+// partials of k_spmv5 in tile order -- the order and tree of problem_sum1's
+// last block, so the bits are those of the per-sweep path's k_spmv.  One
+// block per problem of the group (the problems p0 ..).
+__global__ void __launch_bounds__(SP_THREADS) k_alpha5(ProbState *st, const int *__restrict__ tbeg,
+		const int *__restrict__ tcnt, const double *partial, Globals *gl, int p0)
+{
+	__shared__ double sh[32];
+	const int prob = p0 + blockIdx.x;
+	grid_wait();
+	grid_release();
+	if (!st[prob].inner_active) return;
+	const int b0 = tbeg[prob], n = tcnt[prob];
+	double a0 = 0;
+	for (int k = threadIdx.x; k < n; k += SP_THREADS) a0 += __ldcg(partial + 2 * (b0 + k));
+	a0 = block_sum<SP_THREADS>(a0, sh);
+	if (threadIdx.x == 0) {
 		ProbState &s = st[prob];
-		double a = s.rho / tot[0];
-		if (!(tot[0] > 0) || !isfinite(a)) {
+		const double a = s.rho / a0;
+		if (!(a0 > 0) || !isfinite(a)) {
 			s.status = SIMPOIS_BREAKDOWN;
 			s.inner_active = 0;
 			s.alpha = 0;
@@ -3308,6 +3329,12 @@ void launch_iteration_fused(const Plan &pl, cudaStream_t s)
 					(const int4 *)pl.act[0], (const int *)pl.tbeg, (const int *)pl.tcnt, pl.partial, pl.gl,
 					parity); ++*pl.nl;
 			KT_END(pl, s, "k_spmv5", pl.kt->px(0) * BPX_SPMV5);
+		}
+		{
+			KT_BEGIN(pl, s);
+			launch_k(pl.pdl, k_alpha5, pl.n, SP_THREADS, 0, s, pl.dst, (const int *)pl.tbeg, (const int *)pl.tcnt,
+					(const double *)pl.partial, pl.gl, pl.p0); ++*pl.nl;
+			KT_END(pl, s, "k_alpha5", 0.0);
 		}
 		launch_vcycle_fused(pl, s, 1, parity, 1);
 	}
