@@ -121,7 +121,7 @@ struct ProbDev {
 	                     // right-hand side to the accuracy the residual needs
 	float *p2;           // fused path: second search-direction buffer
 	float *b_alt;        // fused path: the other level-0 residual buffer (k_pre5
-	                     // writes the updated r there, then swaps it with lv[0].b)
+	                     // writes the updated r there, k_rr5 swaps it with lv[0].b)
 	const CUtensorMap *tmb_alt;   // the TMA map of b_alt (swapped with lv[0].tmb)
 	double *r64, *p64, *p64b, *q64;   // 13-point: FP64 Krylov vectors (else null); p64 and p64b
 	                                 // hold p_new of even and odd iterations
@@ -1681,7 +1681,7 @@ constexpr uint32_t CLAMP_BITS4 = 0xE0E0E0E0u;
 // l (the pre-smoothed correction).
 // At level 0 with a PCG step pending (alpha set by k_spmv5) it first takes
 // that step, as k_xr would: x += alpha p and r -= alpha q on the tile (the
-// new r goes to b_alt, which the problem's last tile then swaps with lv[0].b,
+// new r goes to b_alt, which k_rr5 then swaps with lv[0].b,
 // as neighbouring tiles still read the old r of this tile's cells), with r
 // recomputed on the whole region as the right-hand side of the sweeps, and
 // |r|^2 summed and tested as in k_xr (same operations, same order).
@@ -1877,21 +1877,50 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 		C.b[(size_t)cj * C.w + ci] = 1.f * acc;
 	}
 	if (!upd) return;
-	double tot[2];
-	if (problem_sum1_ff(rr, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
+	// the tile's |r|^2; k_rr5 sums the problem's tiles and ends the step
+	const double s0 = block_sum_ff<SP_THREADS>(rr, sh);
+	if (threadIdx.x == 0) partial[2 * blockIdx.x] = s0;
+}
+
+// The sum of per-tile partials of one problem, in tile order: the order and
+// tree of problem_sum1's last block (the per-sweep kernels' reductions), so
+// the fused path's scalars carry the same bits.
+__device__ __forceinline__ double tiles_sum(const double *partial, int b0, int n, double *sh)
+{
+	double a0 = 0;
+	for (int k = threadIdx.x; k < n; k += SP_THREADS) a0 += __ldcg(partial + 2 * (b0 + k));
+	return block_sum<SP_THREADS>(a0, sh);
+}
+
+// The end of k_pre5's PCG step at level 0, one block per problem of the group
+// (the problems p0 ..) that took it in the tile kernel: |r|^2 from the tiles'
+// partials, the iteration counts, the swap of the residual buffers (every tile
+// is done with the old r), the stop test.  In its own launch, so that the
+// tile kernel's blocks exit without waiting for an atomic to learn which is
+// the last.
+__global__ void __launch_bounds__(SP_THREADS) k_rr5(ProbDev *P, ProbState *st, const int *__restrict__ tbeg,
+		const int *__restrict__ tcnt, const double *partial, Globals *gl, int p0)
+{
+	__shared__ double sh[32];
+	const int prob = p0 + blockIdx.x;
+	grid_wait();
+	grid_release();
+	if (!st[prob].inner_active || !st[prob].pending || P[prob].nfine == 0) return;
+	const double tot = tiles_sum(partial, tbeg[prob], tcnt[prob], sh);
+	if (threadIdx.x == 0) {
 		ProbState &s = st[prob];
-		s.rr = tot[0];
+		s.rr = tot;
 		s.iter += 1;
 		s.total_iter += 1;
 		s.pending = 0;
-		ProbDev &w = P[prob];   // every tile of the problem is done with the old r
+		ProbDev &w = P[prob];
 		float *nb = w.b_alt;
 		w.b_alt = w.lv[0].b;
 		w.lv[0].b = nb;
 		const CUtensorMap *nm = w.tmb_alt;   // and its TMA map
 		w.tmb_alt = w.lv[0].tmb;
 		w.lv[0].tmb = nm;
-		if (tot[0] <= s.tau2 || s.iter >= INNER_MAX || s.total_iter >= s.max_iter) {
+		if (tot <= s.tau2 || s.iter >= INNER_MAX || s.total_iter >= s.max_iter) {
 			s.inner_active = 0;
 			atomicSub(&gl->inner_count, 1);
 		}
@@ -1899,8 +1928,8 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_pre5(ProbDev *P, ProbState *s
 }
 
 // Coarse correction (injection from z2 of level l+1) and post-smoothing
-// (NU5 backward sweeps); writes z2 of level l.  At level 0 also r.z and the
-// PCG scalars beta, rho (the last tile of the problem to finish).
+// (NU5 backward sweeps); writes z2 of level l.  At level 0 also the tile's r.z
+// partial (k_beta5 forms the PCG scalars beta, rho).
 template <int NU>
 __global__ void __launch_bounds__(SP_THREADS, 8) k_post5(const ProbDev *__restrict__ P, ProbState *st,
 		const int4 *__restrict__ tl, int l, const int *__restrict__ tbeg, const int *__restrict__ tcnt,
@@ -2009,17 +2038,34 @@ __global__ void __launch_bounds__(SP_THREADS, 8) k_post5(const ProbDev *__restri
 		}
 	}
 	if (l != 0 || !pcg) return;
-	double tot[2];
-	if (problem_sum1_ff(rz, prob, tbeg, tcnt, partial, st, tot, sh) && threadIdx.x == 0) {
+	// the tile's r.z; k_beta5 sums the problem's tiles
+	const double s0 = block_sum_ff<SP_THREADS>(rz, sh);
+	if (threadIdx.x == 0) partial[2 * blockIdx.x] = s0;
+}
+
+// beta and rho from the level-0 tiles' r.z partials of k_post5, one block per
+// problem of the group (the problems p0 .. whose level 0 runs in the tile
+// kernels; k_coarse5 ends the others' iterations itself).
+__global__ void __launch_bounds__(SP_THREADS) k_beta5(const ProbDev *__restrict__ P, ProbState *st,
+		const int *__restrict__ tbeg, const int *__restrict__ tcnt, const double *partial, Globals *gl, int p0)
+{
+	__shared__ double sh[32];
+	const int prob = p0 + blockIdx.x;
+	grid_wait();
+	grid_release();
+	if (!st[prob].inner_active || P[prob].nfine == 0) return;
+	const double tot = tiles_sum(partial, tbeg[prob], tcnt[prob], sh);
+	if (threadIdx.x == 0) {
 		ProbState &s = st[prob];
-		if (!(tot[0] > 0) || !isfinite(tot[0])) {
-			if (tot[0] != 0) s.status = SIMPOIS_BREAKDOWN;
+		if (!(tot > 0) || !isfinite(tot)) {
+			// r = 0 exactly, or a preconditioner that is not positive here
+			if (tot != 0) s.status = SIMPOIS_BREAKDOWN;
 			s.inner_active = 0;
 			atomicSub(&gl->inner_count, 1);
 		} else {
-			s.beta = s.rho > 0 ? tot[0] / s.rho : 0.0;
+			s.beta = s.rho > 0 ? tot / s.rho : 0.0;
 			s.beta_f = (float)s.beta;
-			s.rho = tot[0];
+			s.rho = tot;
 		}
 	}
 }
@@ -2445,10 +2491,7 @@ __global__ void __launch_bounds__(SP_THREADS) k_alpha5(ProbState *st, const int 
 	grid_wait();
 	grid_release();
 	if (!st[prob].inner_active) return;
-	const int b0 = tbeg[prob], n = tcnt[prob];
-	double a0 = 0;
-	for (int k = threadIdx.x; k < n; k += SP_THREADS) a0 += __ldcg(partial + 2 * (b0 + k));
-	a0 = block_sum<SP_THREADS>(a0, sh);
+	const double a0 = tiles_sum(partial, tbeg[prob], tcnt[prob], sh);
 	if (threadIdx.x == 0) {
 		ProbState &s = st[prob];
 		const double a = s.rho / a0;
@@ -3253,6 +3296,12 @@ void launch_vcycle_fused(const Plan &pl, cudaStream_t s, int pcg = 1, int use_p2
 		launch_k(pl.pdl, pre, pl.nact[l], SP_THREADS, 0, s, pl.dp, pl.dst, (const int4 *)pl.act[l], l,
 				(const int *)pl.tbeg, (const int *)pl.tcnt, pl.partial, pl.gl, use_p2); ++*pl.nl;
 		KT_END(pl, s, "k_pre5", pl.kt->px(l) * (BPX_PRE5 + (l == 0 && step ? BPX_STEP : 0.0)));
+		if (l == 0 && pcg && step) {
+			KT_BEGIN(pl, s);
+			launch_k(pl.pdl, k_rr5, pl.n, SP_THREADS, 0, s, pl.dp, pl.dst, (const int *)pl.tbeg,
+					(const int *)pl.tcnt, (const double *)pl.partial, pl.gl, pl.p0); ++*pl.nl;
+			KT_END(pl, s, "k_rr5", 0.0);
+		}
 	}
 	{
 		KT_BEGIN(pl, s);
@@ -3267,6 +3316,13 @@ void launch_vcycle_fused(const Plan &pl, cudaStream_t s, int pcg = 1, int use_p2
 				(const int4 *)pl.act[l], l, (const int *)pl.tbeg, (const int *)pl.tcnt, pl.partial, pl.gl, pcg);
 		++*pl.nl;
 		KT_END(pl, s, "k_post5", pl.kt->px(l) * BPX_POST5);
+		if (l == 0 && pcg) {
+			KT_BEGIN(pl, s);
+			launch_k(pl.pdl, k_beta5, pl.n, SP_THREADS, 0, s, (const ProbDev *)pl.dp, pl.dst,
+					(const int *)pl.tbeg, (const int *)pl.tcnt, (const double *)pl.partial, pl.gl, pl.p0);
+			++*pl.nl;
+			KT_END(pl, s, "k_beta5", 0.0);
+		}
 	}
 }
 
