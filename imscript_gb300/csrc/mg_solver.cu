@@ -2112,9 +2112,9 @@ __device__ __forceinline__ float az5_code(const float *z, int code, int c, int w
 // m holds cell codes (0 at known cells)
 __device__ __forceinline__ void smem_sweep5(float *z, const float *b, const uint8_t *m, int w, int h, int colour)
 {
-	const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+	const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, nw = blockDim.x >> 5;
 	const int hw = (w + 1) >> 1;
-	for (int j = ty; j < h; j += 32)
+	for (int j = ty; j < h; j += nw)
 		for (int k = tx; k < hw; k += 32) {
 			const int i = 2 * k + ((colour ^ j) & 1);
 			const int c = j * w + i;
@@ -2298,7 +2298,7 @@ __global__ void __launch_bounds__(1024, 1) k_coarse5(const ProbDev *__restrict__
 	// levels ls.. hold at most 64 cells: warp 0 runs them alone
 	int ls = c0;
 	while (ls < L - 1 && s_w[ls] * s_h[ls] > 64) ls++;
-	const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+	const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, nw = blockDim.x >> 5;
 	// down (block-wide levels)
 	for (int l = c0; l < ls; l++) {
 		float *z = s_Z[l], *b = s_B[l];
@@ -2311,7 +2311,7 @@ __global__ void __launch_bounds__(1024, 1) k_coarse5(const ProbDev *__restrict__
 		float *bc = s_B[l + 1];
 		const uint8_t *mc = s_M[l + 1];
 		const int wc = s_w[l + 1], hc = s_h[l + 1];
-		for (int cj = ty; cj < hc; cj += 32)
+		for (int cj = ty; cj < hc; cj += nw)
 			for (int ci = tx; ci < wc; ci += 32) {
 				const int c = cj * wc + ci;
 				if (!mc[c]) continue;
@@ -2337,7 +2337,7 @@ __global__ void __launch_bounds__(1024, 1) k_coarse5(const ProbDev *__restrict__
 		const float *zc = s_Z[l + 1];
 		const uint8_t *mc = s_M[l + 1];
 		const int w = s_w[l], h = s_h[l], wc = s_w[l + 1];
-		for (int j = ty; j < h; j += 32)
+		for (int j = ty; j < h; j += nw)
 			for (int i = tx; i < w; i += 32) {
 				const int c = j * w + i, kc = (j >> 1) * wc + (i >> 1);
 				if (m[c] && mc[kc]) z[c] += zc[kc];
@@ -3076,6 +3076,11 @@ struct Plan {
 	int p0 = 0;                  // first problem of this view
 	int ngroups = 1;
 	int gp0[GMAX] = {}, gpn[GMAX] = {}, gnfine[GMAX] = {};
+	// k_coarse5's threads per block, for the view (for each group): 1024 when a
+	// problem runs level 0 in it (its PCG step and r.z are laid out for 1024
+	// threads) or when the call has at most one problem per SM (each block's
+	// levels then go faster on more warps); else 256, four blocks to an SM
+	int coarse_nt = 1024, gcoarse_nt[GMAX] = {};
 	int gbeg[GMAX][MAXLEV] = {}, gcnt[GMAX][MAXLEV] = {};
 	Globals *gls = nullptr;      // GMAX loop-counter blocks (gl == gls: group 0)
 	int *tbeg_rel = nullptr;     // level-0 tile offsets relative to the group's first tile
@@ -3090,6 +3095,7 @@ Plan group_view(const Plan &pl, int g)
 	v.n = pl.gpn[g];
 	v.p0 = pl.gp0[g];
 	v.nfine_max = pl.gnfine[g];
+	v.coarse_nt = pl.gcoarse_nt[g];
 	for (int l = 0; l < MAXLEV; l++) {
 		v.act[l] = pl.act[l] ? pl.act[l] + pl.gbeg[g][l] : nullptr;
 		v.nact[l] = pl.gcnt[g][l];
@@ -3305,7 +3311,10 @@ void launch_vcycle_fused(const Plan &pl, cudaStream_t s, int pcg = 1, int use_p2
 	}
 	{
 		KT_BEGIN(pl, s);
-		launch_k(pl.pdl, k_coarse5, pl.n, 1024, pl.coarse_smem, s, (const ProbDev *)pl.dp, pl.dst, pl.gl, pcg,
+		// (the sweeps, restrictions and injections give the same bits with any
+		// number of warps)
+		launch_k(pl.pdl, k_coarse5, pl.n, pl.coarse_nt, pl.coarse_smem, s, (const ProbDev *)pl.dp,
+				pl.dst, pl.gl, pcg,
 				use_p2, pl.p0, pl.nu); ++*pl.nl;
 		KT_END(pl, s, "k_coarse5", pl.kt->cells() * BPC_COARSE5);
 	}
@@ -3403,12 +3412,12 @@ std::string plan_signature(const simpois_ctx *ctx, const Plan &pl, int K, int fu
 {
 	std::string sig;
 	char buf[96];
-	snprintf(buf, sizeof buf, "%p/%d/%d/%d/%d/%d/%d/%d/%d/%d|", (void *)ctx->arena, pl.n, K, (int)fused,
-			pl.nfine_max, pl.nlev_max, pl.coarse_smem, opt.use_mg, pl.pdl, pl.nu);
+	snprintf(buf, sizeof buf, "%p/%d/%d/%d/%d/%d/%d/%d/%d/%d/%d|", (void *)ctx->arena, pl.n, K, (int)fused,
+			pl.nfine_max, pl.nlev_max, pl.coarse_smem, opt.use_mg, pl.pdl, pl.nu, pl.coarse_nt);
 	sig += buf;
 	const int ng = fused == MODE_FUSED5 || fused == MODE_BIH64 ? pl.ngroups : 1;
 	for (int g = 0; g < ng && ng > 1; g++) {
-		snprintf(buf, sizeof buf, "g%d:%d+%d:%d|", g, pl.gp0[g], pl.gpn[g], pl.gnfine[g]);
+		snprintf(buf, sizeof buf, "g%d:%d+%d:%d:%d|", g, pl.gp0[g], pl.gpn[g], pl.gnfine[g], pl.gcoarse_nt[g]);
 		sig += buf;
 		for (int l = 0; l < pl.nlev_max; l++) {
 			snprintf(buf, sizeof buf, "%d+%d,", pl.gbeg[g][l], pl.gcnt[g][l]);
@@ -4050,6 +4059,11 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 	pl.gp0[0] = 0;
 	pl.gpn[0] = n;
 	pl.gnfine[0] = pl.nfine_max;
+	const bool many = n > std::max(1, ctx->sm_count);
+	bool l0 = false;
+	for (int k = 0; k < n; k++) l0 = l0 || hp[k].nfine == 0;
+	pl.coarse_nt = many && !l0 ? 256 : 1024;
+	pl.gcoarse_nt[0] = pl.coarse_nt;
 	for (int l = 0; l < MAXLEV; l++) pl.gcnt[0][l] = pl.nact[l];
 	if (grouped) {
 		// contiguous problem ranges with about equal level-0 active tiles
@@ -4085,6 +4099,9 @@ int mg_solve(simpois_ctx *ctx, const MgProblem *probs, int n, const MgOptions &o
 				r += hpc[k];
 				pl.gnfine[gg] = std::max(pl.gnfine[gg], hp[k].nfine);
 			}
+			bool gl0 = false;
+			for (int k = pl.gp0[gg]; k < pl.gp0[gg] + pl.gpn[gg]; k++) gl0 = gl0 || hp[k].nfine == 0;
+			pl.gcoarse_nt[gg] = many && !gl0 ? 256 : 1024;
 		}
 		SP_CUDA(ctx, cudaMemcpyAsync(pl.tbeg_rel, hrel, sizeof(int) * n, cudaMemcpyHostToDevice, s));
 		for (int gg = 0; gg < pl.ngroups; gg++) {
